@@ -1,0 +1,226 @@
+"""Thin Python handles over the C ABI (include/crg.h) for tests and benchmarks.
+
+Every method is one or two C-ABI calls; arrays cross as raw pointers.  The
+names follow the reference interface they stand for: Scene ~ cr::scene
+(src/render/scene.h:19-53), Film ~ the renderer's film buffers
+(src/render/renderer.h:85-91), render() ~ a renderer pass.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi, check, load
+from ._abi import ptr
+
+DEFAULT_SUN = dict(
+    size=np.float32(3.14159265359) / np.float32(48.0),
+    intensity=100.0,
+    direction=(0.8 / np.sqrt(1.64), -1.0 / np.sqrt(1.64), 0.0),
+    colour=(1.0, 0.9, 0.7),
+)
+
+
+def make_sun(sun=None) -> _abi.Sun:
+    s = dict(DEFAULT_SUN)
+    if sun:
+        s.update(sun)
+    return _abi.Sun(float(s["size"]), float(s["intensity"]), tuple(map(float, s["direction"])), tuple(map(float, s["colour"])))
+
+
+def make_camera(cam: dict) -> _abi.Camera:
+    return _abi.Camera(
+        tuple(map(float, cam["position"])),
+        tuple(map(float, cam.get("rotation", (0, 0, 0)))),
+        float(cam.get("fov", 75.0)),
+        int(cam.get("mode", 0)),
+        float(cam.get("scale", 1.0)),
+        0,
+    )
+
+
+def make_settings(width, height, spp, max_bounces=8, rr_depth=0, mode=1, seed=1, aspect=1.0) -> _abi.Settings:
+    return _abi.Settings(width, height, spp, max_bounces, rr_depth, mode, seed, float(aspect))
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        check(self.lib.crg_context_create(device, C.byref(self.h)))
+
+    def check(self, status):
+        check(status, self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.crg_context_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def sync(self, stream=None):
+        self.check(self.lib.crg_stream_sync(self.h, stream))
+
+
+class DeviceBuffer:
+    def __init__(self, ctx: Context, nbytes: int):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        self.ptr = C.c_void_p()
+        ctx.check(ctx.lib.crg_device_alloc(ctx.h, self.nbytes, C.byref(self.ptr)))
+
+    @classmethod
+    def from_array(cls, ctx, a: np.ndarray, stream=None):
+        b = cls(ctx, a.nbytes)
+        b.upload(a, stream)
+        return b
+
+    def upload(self, a: np.ndarray, stream=None):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.lib.crg_memcpy_h2d(self.ctx.h, self.ptr, ptr(a), a.nbytes, stream))
+
+    def download(self, out: np.ndarray, stream=None):
+        assert out.nbytes <= self.nbytes and out.flags["C_CONTIGUOUS"]
+        self.ctx.check(self.ctx.lib.crg_memcpy_d2h(self.ctx.h, ptr(out), self.ptr, out.nbytes, stream))
+        self.ctx.sync(stream)
+        return out
+
+    def free(self):
+        if self.ptr:
+            self.ctx.lib.crg_device_free(self.ctx.h, self.ptr)
+            self.ptr = C.c_void_p()
+
+
+class Scene:
+    """cr::scene over the GPU path: geometry, materials, sky, sun, BVH."""
+
+    def __init__(self, ctx: Context, verts, mat_idx, mats):
+        self.ctx = ctx
+        self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+        self.mat_idx = np.ascontiguousarray(mat_idx, np.uint32)
+        self.mats = np.ascontiguousarray(mats)
+        self.ntri = self.verts.shape[0]
+        self.h = C.c_void_p()
+        ctx.check(
+            ctx.lib.crg_scene_create(
+                ctx.h, ptr(self.verts), self.ntri, None, ptr(self.mat_idx), ptr(self.mats), len(self.mats), C.byref(self.h)
+            )
+        )
+
+    def build(self, width=8, treelet=0, leaf_max=3, rounds=3, stream=None):
+        self.opts = _abi.BuildOpts(width, treelet, leaf_max, rounds)
+        self.ctx.check(self.ctx.lib.crg_scene_build(self.h, C.byref(self.opts), stream))
+        return self
+
+    def info(self) -> dict:
+        i = _abi.BvhInfo()
+        self.ctx.check(self.ctx.lib.crg_scene_bvh_info(self.h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def download_bvh(self):
+        i = self.info()
+        bvh2 = np.zeros((max(i["n_bvh2_nodes"], 0), 8), np.float32)
+        order = np.zeros(i["ntri"], np.uint32)
+        wide = np.zeros(i["n_wide_nodes"] * i["node_bytes"], np.uint8)
+        tris = np.zeros((i["n_tri_slots"], 12), np.float32)
+        self.ctx.check(self.ctx.lib.crg_scene_bvh_download(self.h, ptr(bvh2), ptr(order), ptr(wide), ptr(tris)))
+        return bvh2, order, wide, tris
+
+    def set_sun(self, enabled: bool, sun=None):
+        s = make_sun(sun)
+        self.ctx.check(self.ctx.lib.crg_scene_set_sun(self.h, int(enabled), C.byref(s)))
+
+    def set_skybox(self, rgba: np.ndarray | None, rot=(0.0, 0.0)):
+        if rgba is None:
+            self.ctx.check(self.ctx.lib.crg_scene_set_skybox(self.h, None, 0, 0, 0.0, 0.0))
+            return
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        h, w = rgba.shape[:2]
+        self.ctx.check(self.ctx.lib.crg_scene_set_skybox(self.h, ptr(rgba), w, h, float(rot[0]), float(rot[1])))
+
+    def intersect(self, rays: np.ndarray, any_hit=False, counted=False):
+        """Host rays in, host results out (uploads, launches, downloads)."""
+        n = len(rays)
+        rb = DeviceBuffer.from_array(self.ctx, rays)
+        ob = DeviceBuffer(self.ctx, max(n * (4 if any_hit else 16), 16))
+        extra = []
+        try:
+            if any_hit:
+                self.ctx.check(self.ctx.lib.crg_intersect_any(self.h, rb.ptr, ob.ptr, n, None))
+                out = ob.download(np.zeros(n, np.uint32))
+            elif counted:
+                nb = DeviceBuffer(self.ctx, max(4 * n, 16))
+                tb = DeviceBuffer(self.ctx, max(4 * n, 16))
+                extra = [nb, tb]
+                self.ctx.check(self.ctx.lib.crg_intersect_closest_counted(self.h, rb.ptr, ob.ptr, nb.ptr, tb.ptr, n, None))
+                out = (ob.download(np.zeros(n, _abi.HIT_DTYPE)), nb.download(np.zeros(n, np.uint32)),
+                       tb.download(np.zeros(n, np.uint32)))
+            else:
+                self.ctx.check(self.ctx.lib.crg_intersect_closest(self.h, rb.ptr, ob.ptr, n, None))
+                out = ob.download(np.zeros(n, _abi.HIT_DTYPE))
+            self.ctx.check(self.ctx.lib.crg_scene_poll_error(self.h))
+            return out
+        finally:
+            rb.free()
+            ob.free()
+            for b in extra:
+                b.free()
+
+    def set_counting(self, on: bool):
+        self.ctx.check(self.ctx.lib.crg_scene_set_counting(self.h, int(on)))
+
+    def stats(self) -> dict:
+        s = _abi.RenderStats()
+        self.ctx.check(self.ctx.lib.crg_render_stats_get(self.h, C.byref(s)))
+        return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays)
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.crg_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+class Film:
+    def __init__(self, ctx: Context, width: int, height: int, f64=False, aov=False):
+        self.ctx = ctx
+        self.width, self.height = width, height
+        self.flags = (_abi.FILM_F64 if f64 else 0) | (_abi.FILM_AOV if aov else 0)
+        self.h = C.c_void_p()
+        ctx.check(ctx.lib.crg_film_create(ctx.h, width, height, self.flags, C.byref(self.h)))
+
+    def reset(self, stream=None):
+        self.ctx.check(self.ctx.lib.crg_film_reset(self.h, stream))
+
+    @property
+    def spp(self) -> int:
+        v = C.c_uint64()
+        self.ctx.check(self.ctx.lib.crg_film_spp(self.h, C.byref(v)))
+        return v.value
+
+    def download(self, f64=False, aov=False) -> dict:
+        n = self.width * self.height
+        out = {"sum": np.zeros(n * 3, np.float32)}
+        if f64:
+            out["sum64"] = np.zeros(n * 3, np.float64)
+            out["sumsq64"] = np.zeros(n * 3, np.float64)
+        if aov:
+            for k in ("albedo", "normal", "depth"):
+                out[k] = np.zeros(n * 4, np.float32)
+        self.ctx.check(
+            self.ctx.lib.crg_film_download(
+                self.h, ptr(out["sum"]), ptr(out.get("sum64")), ptr(out.get("sumsq64")), ptr(out.get("albedo")),
+                ptr(out.get("normal")), ptr(out.get("depth")), None
+            )
+        )
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.crg_film_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def render(scene: Scene, camera: dict, settings: _abi.Settings, film: Film, stream=None):
+    cam = make_camera(camera)
+    scene.ctx.check(scene.ctx.lib.crg_render(scene.h, C.byref(cam), C.byref(settings), film.h, stream))

@@ -1,0 +1,599 @@
+// crg_api.cu — the C ABI of include/crg.h.
+//
+// Handles own their device memory; every call returns a crg_status and
+// records a message in the context.  Nothing here computes rays or samples:
+// the host side only validates arguments, copies inputs, prepares the
+// emissive-triangle table and launches kernels.
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "crg_internal.h"
+
+namespace crg {
+
+crg_status set_error(crg_context *ctx, crg_status s, const std::string &msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+crg_status cuda_error(crg_context *ctx, cudaError_t e, const char *what) {
+    const crg_status s = (e == cudaErrorMemoryAllocation) ? CRG_ERR_OOM : CRG_ERR_CUDA;
+    return set_error(ctx, s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+crg_status dev_alloc(crg_context *ctx, DevBuf &b, size_t bytes) {
+    if (b.ptr && b.bytes >= bytes) return CRG_OK;
+    dev_free(b);
+    if (bytes == 0) return CRG_OK;
+    void *p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cuda_error(ctx, e, "cudaMalloc");
+    }
+    b.ptr = p;
+    b.bytes = bytes;
+    return CRG_OK;
+}
+
+void dev_free(DevBuf &b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+namespace {
+
+// cr::sampling::build_local (src/util/sampling.h:21-33), host form.
+void build_local_host(const float n[3], float t[3], float b[3]) {
+    const float s = (n[2] < 0.0f) ? -1.0f : 1.0f;
+    const float a = -1.0f / (s + n[2]);
+    const float bb = n[0] * n[1] * a;
+    t[0] = 1.0f + s * n[0] * n[0] * a;
+    t[1] = s * bb;
+    t[2] = -s * n[0];
+    b[0] = bb;
+    b[1] = s + n[1] * n[1] * a;
+    b[2] = -n[1];
+}
+
+crg_sun default_sun() {
+    // cr::entity::sun (src/render/entities/components.h:23-29)
+    crg_sun s;
+    s.size = 3.14159265359f / 48.0f;
+    s.intensity = 100.0f;
+    const float d[3] = {0.8f, -1.0f, 0.0f};
+    const float inv = 1.0f / std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    s.direction[0] = d[0] * inv;
+    s.direction[1] = d[1] * inv;
+    s.direction[2] = d[2] * inv;
+    s.colour[0] = 1.0f;
+    s.colour[1] = 0.9f;
+    s.colour[2] = 0.7f;
+    return s;
+}
+
+void apply_sun(crg_scene *s, const crg_sun &sun) {
+    s->sun = sun;
+    const float n[3] = {-sun.direction[0], -sun.direction[1], -sun.direction[2]};
+    float t[3], b[3];
+    build_local_host(n, t, b);
+    for (int k = 0; k < 3; ++k) {
+        s->sun_frame[k] = t[k];
+        s->sun_frame[3 + k] = n[k];
+        s->sun_frame[6 + k] = b[k];
+    }
+    s->sun_cos = (float)std::cos((double)sun.size);
+    s->sun_pdf = 1.0f / (6.28318530717f * (1.0f - s->sun_cos));
+}
+
+__global__ void k_fill_f32(float *a, size_t n, float v) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+__global__ void k_display(const float *__restrict__ sum, float4 *__restrict__ out, size_t npix, float inv_n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x) {
+        const float r = fminf(fmaxf(sum[3 * i] * inv_n, 0.0f), 1.0f);
+        const float g = fminf(fmaxf(sum[3 * i + 1] * inv_n, 0.0f), 1.0f);
+        const float b = fminf(fmaxf(sum[3 * i + 2] * inv_n, 0.0f), 1.0f);
+        out[i] = make_float4(powf(r, 1.0f / 2.2f), powf(g, 1.0f / 2.2f), powf(b, 1.0f / 2.2f), 1.0f);
+    }
+}
+
+// Emissive triangles weighted by area x luminance of colour*emission (double
+// sums in primitive order; CDF and pdfs rounded to float once).
+crg_status prepare_lights(crg_scene *s, const float *verts) {
+    const uint32_t nmat = s->nmat;
+    std::vector<double> lum(nmat, 0.0);
+    for (uint32_t m = 0; m < nmat; ++m) {
+        const crg_material &mm = s->host_mats[m];
+        if (mm.emission > 0.0f) {
+            const float r = mm.colour[0] * mm.emission, g = mm.colour[1] * mm.emission, b = mm.colour[2] * mm.emission;
+            lum[m] = 0.2126 * (double)r + 0.7152 * (double)g + 0.0722 * (double)b;
+        }
+    }
+    std::vector<uint32_t> mat_idx(s->ntri);
+    if (s->ntri) {
+        const cudaError_t e = cudaMemcpy(mat_idx.data(), s->mat_idx.ptr, sizeof(uint32_t) * s->ntri, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_error(s->ctx, e, "cudaMemcpy(mat_idx)");
+    }
+    std::vector<uint32_t> prim;
+    std::vector<double> w;
+    double total = 0.0;
+    for (uint32_t p = 0; p < s->ntri; ++p) {
+        const uint32_t m = mat_idx[p];
+        if (!(lum[m] > 0.0)) continue;
+        const float *v = verts + (size_t)p * 9;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = (double)v[3 + a] - (double)v[a];
+            e2[a] = (double)v[6 + a] - (double)v[a];
+        }
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        const double ar = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        const double wt = ar * lum[m];
+        prim.push_back(p);
+        w.push_back(wt);
+        total += wt;
+    }
+    std::vector<float> mpdf(nmat, 0.0f);
+    s->nlights = 0;
+    if (total > 0.0) {
+        std::vector<float> cdf, pdf;
+        double cum = 0.0;
+        for (size_t j = 0; j < w.size(); ++j) {
+            cum += w[j];
+            cdf.push_back((float)(cum / total));
+            pdf.push_back((float)(lum[mat_idx[prim[j]]] / total));
+        }
+        cdf.back() = 1.0f;
+        for (uint32_t m = 0; m < nmat; ++m) mpdf[m] = (float)(lum[m] / total);
+        s->nlights = (uint32_t)prim.size();
+        crg_status rc;
+        if ((rc = dev_alloc(s->ctx, s->light_prim, 4 * prim.size())) != CRG_OK) return rc;
+        if ((rc = dev_alloc(s->ctx, s->light_cdf, 4 * cdf.size())) != CRG_OK) return rc;
+        if ((rc = dev_alloc(s->ctx, s->light_pdf, 4 * pdf.size())) != CRG_OK) return rc;
+        CRG_CUDA(s->ctx, cudaMemcpy(s->light_prim.ptr, prim.data(), 4 * prim.size(), cudaMemcpyHostToDevice));
+        CRG_CUDA(s->ctx, cudaMemcpy(s->light_cdf.ptr, cdf.data(), 4 * cdf.size(), cudaMemcpyHostToDevice));
+        CRG_CUDA(s->ctx, cudaMemcpy(s->light_pdf.ptr, pdf.data(), 4 * pdf.size(), cudaMemcpyHostToDevice));
+    }
+    crg_status rc;
+    if ((rc = dev_alloc(s->ctx, s->mat_light_pdf, 4 * (size_t)(nmat ? nmat : 1))) != CRG_OK) return rc;
+    if (nmat) CRG_CUDA(s->ctx, cudaMemcpy(s->mat_light_pdf.ptr, mpdf.data(), 4 * nmat, cudaMemcpyHostToDevice));
+    return CRG_OK;
+}
+
+crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
+                        crg_scene **out, crg_scene *&s) {
+    if (!ctx || !out) return set_error(ctx, CRG_ERR_INVALID_ARG, "null context or output handle");
+    if (ntri > 0 && (!mat_idx || !mats || nmat == 0))
+        return set_error(ctx, CRG_ERR_INVALID_ARG, "triangles need mat_idx and a non-empty material table");
+    if (ntri > (1u << 30)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 2^30 triangles");
+    for (uint32_t p = 0; p < ntri; ++p)
+        if (mat_idx[p] >= nmat) return set_error(ctx, CRG_ERR_INVALID_ARG, "material index out of range");
+    for (uint32_t m = 0; m < nmat; ++m)
+        if (mats[m].shade_type > CRG_SHADE_GLASS) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad shade_type");
+    s = new (std::nothrow) crg_scene();
+    if (!s) return set_error(ctx, CRG_ERR_OOM, "host allocation failed");
+    s->ctx = ctx;
+    s->ntri = ntri;
+    s->nmat = nmat;
+    s->host_mats.assign(mats, mats + nmat);
+    apply_sun(s, default_sun());
+    s->sun_enabled = 0;
+    crg_status rc;
+    if ((rc = dev_alloc(ctx, s->mat_idx, sizeof(uint32_t) * (size_t)(ntri ? ntri : 1))) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, s->mats, sizeof(crg_material) * (size_t)(nmat ? nmat : 1))) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, s->err, 64)) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, s->counters, 64)) != CRG_OK) return rc;
+    CRG_CUDA(ctx, cudaMemset(s->err.ptr, 0, 64));
+    CRG_CUDA(ctx, cudaMemset(s->counters.ptr, 0, 64));
+    if (ntri) CRG_CUDA(ctx, cudaMemcpy(s->mat_idx.ptr, mat_idx, sizeof(uint32_t) * ntri, cudaMemcpyHostToDevice));
+    if (nmat) CRG_CUDA(ctx, cudaMemcpy(s->mats.ptr, mats, sizeof(crg_material) * nmat, cudaMemcpyHostToDevice));
+    return CRG_OK;
+}
+
+void scene_free(crg_scene *s) {
+    if (!s) return;
+    DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_cdf, &s->light_pdf, &s->mat_light_pdf,
+                      &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters};
+    for (DevBuf *b : bufs) dev_free(*b);
+    delete s;
+}
+
+bool valid_opts(const crg_build_opts &o) {
+    return (o.width == 2 || o.width == 4 || o.width == 8) && o.leaf_max >= 1 && o.leaf_max <= 3 && o.treelet_rounds <= 8;
+}
+
+} // namespace
+} // namespace crg
+
+using namespace crg;
+
+extern "C" {
+
+uint32_t crg_abi_version(void) { return CRG_ABI_VERSION; }
+
+const char *crg_status_string(crg_status s) {
+    switch (s) {
+    case CRG_OK: return "OK";
+    case CRG_ERR_INVALID_ARG: return "INVALID_ARG";
+    case CRG_ERR_OOM: return "OOM";
+    case CRG_ERR_CUDA: return "CUDA";
+    case CRG_ERR_TIMEOUT: return "TIMEOUT";
+    case CRG_ERR_NOT_BUILT: return "NOT_BUILT";
+    case CRG_ERR_UNSUPPORTED: return "UNSUPPORTED";
+    case CRG_ERR_DEVICE: return "DEVICE";
+    }
+    return "UNKNOWN";
+}
+
+crg_status crg_context_create(int device, crg_context **out) {
+    if (!out) return CRG_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || device < 0 || device >= count) {
+        (void)cudaGetLastError();
+        return e != cudaSuccess ? CRG_ERR_CUDA : CRG_ERR_INVALID_ARG;
+    }
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return CRG_ERR_CUDA;
+    crg_context *ctx = new (std::nothrow) crg_context();
+    if (!ctx) return CRG_ERR_OOM;
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    *out = ctx;
+    return CRG_OK;
+}
+
+crg_status crg_context_destroy(crg_context *ctx) {
+    if (!ctx) return CRG_ERR_INVALID_ARG;
+    delete ctx;
+    return CRG_OK;
+}
+
+const char *crg_last_error_string(const crg_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr) {
+    if (!ctx || !dptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
+    *dptr = nullptr;
+    if (bytes == 0) return CRG_OK;
+    CRG_CUDA(ctx, cudaMalloc(dptr, bytes));
+    return CRG_OK;
+}
+
+crg_status crg_device_free(crg_context *ctx, void *dptr) {
+    if (!ctx) return CRG_ERR_INVALID_ARG;
+    if (dptr) CRG_CUDA(ctx, cudaFree(dptr));
+    return CRG_OK;
+}
+
+crg_status crg_memcpy_h2d(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream) {
+    if (!ctx || (bytes && (!dst || !src))) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
+    if (bytes) CRG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return CRG_OK;
+}
+
+crg_status crg_memcpy_d2h(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream) {
+    if (!ctx || (bytes && (!dst || !src))) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
+    if (bytes) CRG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return CRG_OK;
+}
+
+crg_status crg_stream_sync(crg_context *ctx, crg_stream stream) {
+    if (!ctx) return CRG_ERR_INVALID_ARG;
+    CRG_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    return CRG_OK;
+}
+
+crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri, const float *uvs, const uint32_t *mat_idx,
+                            const crg_material *mats, uint32_t nmat, crg_scene **out) {
+    (void)uvs;
+    if (ntri > 0 && !verts) return set_error(ctx, CRG_ERR_INVALID_ARG, "null vertex array");
+    if (out) *out = nullptr;
+    crg_scene *s = nullptr;
+    crg_status rc = scene_common(ctx, ntri, mat_idx, mats, nmat, out, s);
+    if (rc == CRG_OK) rc = dev_alloc(ctx, s->verts, sizeof(float) * 9 * (size_t)(ntri ? ntri : 1));
+    if (rc == CRG_OK && ntri) {
+        const cudaError_t e = cudaMemcpy(s->verts.ptr, verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts)");
+    }
+    if (rc == CRG_OK) rc = prepare_lights(s, verts);
+    if (rc != CRG_OK) {
+        scene_free(s);
+        return rc;
+    }
+    *out = s;
+    return CRG_OK;
+}
+
+crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint32_t ntri, const uint32_t *mat_idx,
+                                   const crg_material *mats, uint32_t nmat, crg_scene **out) {
+    if (ntri > 0 && !d_verts) return set_error(ctx, CRG_ERR_INVALID_ARG, "null vertex array");
+    if (out) *out = nullptr;
+    crg_scene *s = nullptr;
+    crg_status rc = scene_common(ctx, ntri, mat_idx, mats, nmat, out, s);
+    if (rc == CRG_OK) rc = dev_alloc(ctx, s->verts, sizeof(float) * 9 * (size_t)(ntri ? ntri : 1));
+    std::vector<float> hv;
+    if (rc == CRG_OK && ntri) {
+        cudaError_t e = cudaMemcpy(s->verts.ptr, d_verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyDeviceToDevice);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts)");
+        // the emissive-triangle table needs the vertices of emitters only; a
+        // host copy keeps its construction identical to crg_scene_create
+        if (rc == CRG_OK) {
+            hv.resize((size_t)ntri * 9);
+            e = cudaMemcpy(hv.data(), d_verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts to host)");
+        }
+    }
+    if (rc == CRG_OK) rc = prepare_lights(s, hv.data());
+    if (rc != CRG_OK) {
+        scene_free(s);
+        return rc;
+    }
+    *out = s;
+    return CRG_OK;
+}
+
+crg_status crg_scene_destroy(crg_scene *scene) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    scene_free(scene);
+    return CRG_OK;
+}
+
+crg_status crg_scene_build(crg_scene *scene, const crg_build_opts *opts, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    crg_build_opts o{8, 0, 3, 3};
+    if (opts) o = *opts;
+    if (!valid_opts(o)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "build options: width 2/4/8, leaf_max 1..3");
+    const crg_status rc = build_bvh(scene, o, (cudaStream_t)stream);
+    if (rc != CRG_OK) scene->built = false;
+    return rc;
+}
+
+crg_status crg_scene_set_skybox(crg_scene *scene, const float *rgba, uint32_t w, uint32_t h, float rot_u, float rot_v) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if ((w == 0) != (h == 0) || (w && !rgba)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "bad skybox size");
+    scene->sky_rot_u = rot_u;
+    scene->sky_rot_v = rot_v;
+    if (w == 0) {
+        dev_free(scene->sky);
+        scene->sky_w = scene->sky_h = 0;
+        return CRG_OK;
+    }
+    const size_t bytes = sizeof(float) * 4 * (size_t)w * h;
+    crg_status rc = dev_alloc(scene->ctx, scene->sky, bytes);
+    if (rc != CRG_OK) return rc;
+    CRG_CUDA(scene->ctx, cudaMemcpy(scene->sky.ptr, rgba, bytes, cudaMemcpyHostToDevice));
+    scene->sky_w = w;
+    scene->sky_h = h;
+    return CRG_OK;
+}
+
+crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    apply_sun(scene, sun ? *sun : default_sun());
+    scene->sun_enabled = enabled ? 1 : 0;
+    return CRG_OK;
+}
+
+crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba, const uint32_t *widths,
+                                  const uint32_t *heights) {
+    (void)rgba;
+    (void)widths;
+    (void)heights;
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (count == 0) return CRG_OK;
+    return set_error(scene->ctx, CRG_ERR_UNSUPPORTED, "textured materials are not supported by this build");
+}
+
+crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info) {
+    if (!scene || !info) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return CRG_ERR_NOT_BUILT;
+    info->ntri = scene->ntri;
+    info->width = scene->width;
+    info->n_bvh2_nodes = scene->ntri >= 2 ? scene->ntri - 1 : 0;
+    info->n_wide_nodes = scene->n_wide;
+    info->node_bytes = scene->node_bytes;
+    info->n_tri_slots = scene->ntri;
+    info->depth = scene->depth;
+    info->sah_cost = scene->sah;
+    return CRG_OK;
+}
+
+crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t *order, void *wide, float *tris) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return CRG_ERR_NOT_BUILT;
+    crg_context *ctx = scene->ctx;
+    const uint32_t n = scene->ntri;
+    if (n == 0) return CRG_OK;
+    if (bvh2 && n >= 2) CRG_CUDA(ctx, cudaMemcpy(bvh2, scene->bvh2.ptr, sizeof(float) * 8 * (size_t)(n - 1), cudaMemcpyDeviceToHost));
+    if (order) CRG_CUDA(ctx, cudaMemcpy(order, scene->order.ptr, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    if (wide) CRG_CUDA(ctx, cudaMemcpy(wide, scene->wide.ptr, (size_t)scene->node_bytes * scene->n_wide, cudaMemcpyDeviceToHost));
+    if (tris) CRG_CUDA(ctx, cudaMemcpy(tris, scene->tris.ptr, sizeof(float) * 12 * (size_t)n, cudaMemcpyDeviceToHost));
+    return CRG_OK;
+}
+
+crg_status crg_intersect_closest(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits, uint64_t n, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return set_error(scene->ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (n && (!d_rays || !d_hits)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null ray or hit array");
+    return launch_intersect(scene, d_rays, d_hits, nullptr, nullptr, nullptr, n, false, (cudaStream_t)stream);
+}
+
+crg_status crg_intersect_any(const crg_scene *scene, const crg_ray *d_rays, uint32_t *d_occluded, uint64_t n, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return set_error(scene->ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (n && (!d_rays || !d_occluded)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null ray or output array");
+    return launch_intersect(scene, d_rays, nullptr, d_occluded, nullptr, nullptr, n, true, (cudaStream_t)stream);
+}
+
+crg_status crg_intersect_closest_counted(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits, uint32_t *d_nodes,
+                                         uint32_t *d_tris, uint64_t n, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return set_error(scene->ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (n && (!d_rays || !d_hits)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null ray or hit array");
+    if (!d_nodes && !d_tris) return launch_intersect(scene, d_rays, d_hits, nullptr, nullptr, nullptr, n, false, (cudaStream_t)stream);
+    return launch_intersect(scene, d_rays, d_hits, nullptr, d_nodes, d_tris, n, false, (cudaStream_t)stream);
+}
+
+crg_status crg_scene_poll_error(crg_scene *scene) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    uint32_t e = 0;
+    CRG_CUDA(scene->ctx, cudaMemcpy(&e, scene->err.ptr, 4, cudaMemcpyDeviceToHost));
+    if (e) {
+        CRG_CUDA(scene->ctx, cudaMemset(scene->err.ptr, 0, 4));
+        return set_error(scene->ctx, CRG_ERR_DEVICE, "traversal stack overflow reported by a kernel");
+    }
+    return CRG_OK;
+}
+
+crg_status crg_film_create(crg_context *ctx, uint32_t width, uint32_t height, uint32_t flags, crg_film **out) {
+    if (!ctx || !out) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 31))
+        return set_error(ctx, CRG_ERR_INVALID_ARG, "film size must be positive and at most 2^31 pixels");
+    crg_film *f = new (std::nothrow) crg_film();
+    if (!f) return set_error(ctx, CRG_ERR_OOM, "host allocation failed");
+    f->ctx = ctx;
+    f->width = width;
+    f->height = height;
+    f->flags = flags;
+    const size_t npix = (size_t)width * height;
+    crg_status rc = dev_alloc(ctx, f->sum, sizeof(float) * 3 * npix);
+    if (rc == CRG_OK && (flags & CRG_FILM_F64)) {
+        rc = dev_alloc(ctx, f->sum64, sizeof(double) * 3 * npix);
+        if (rc == CRG_OK) rc = dev_alloc(ctx, f->sumsq64, sizeof(double) * 3 * npix);
+    }
+    if (rc == CRG_OK && (flags & CRG_FILM_AOV)) {
+        rc = dev_alloc(ctx, f->aov_albedo, sizeof(float) * 4 * npix);
+        if (rc == CRG_OK) rc = dev_alloc(ctx, f->aov_normal, sizeof(float) * 4 * npix);
+        if (rc == CRG_OK) rc = dev_alloc(ctx, f->aov_depth, sizeof(float) * 4 * npix);
+        // cr::image starts filled with FLT_MAX (src/objects/image.h:30-33)
+        if (rc == CRG_OK) {
+            k_fill_f32<<<152 * 4, 256>>>((float *)f->aov_albedo.ptr, 4 * npix, FLT_MAX);
+            k_fill_f32<<<152 * 4, 256>>>((float *)f->aov_normal.ptr, 4 * npix, FLT_MAX);
+            k_fill_f32<<<152 * 4, 256>>>((float *)f->aov_depth.ptr, 4 * npix, FLT_MAX);
+        }
+    }
+    if (rc == CRG_OK) rc = crg_film_reset(f, nullptr);
+    if (rc == CRG_OK) {
+        const cudaError_t e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "film init");
+    }
+    if (rc != CRG_OK) {
+        crg_film_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return CRG_OK;
+}
+
+crg_status crg_film_destroy(crg_film *film) {
+    if (!film) return CRG_ERR_INVALID_ARG;
+    DevBuf *bufs[] = {&film->sum, &film->sum64, &film->sumsq64, &film->aov_albedo, &film->aov_normal, &film->aov_depth};
+    for (DevBuf *b : bufs) dev_free(*b);
+    delete film;
+    return CRG_OK;
+}
+
+crg_status crg_film_reset(crg_film *film, crg_stream stream) {
+    if (!film) return CRG_ERR_INVALID_ARG;
+    const size_t npix = (size_t)film->width * film->height;
+    cudaStream_t st = (cudaStream_t)stream;
+    CRG_CUDA(film->ctx, cudaMemsetAsync(film->sum.ptr, 0, sizeof(float) * 3 * npix, st));
+    if (film->sum64.ptr) {
+        CRG_CUDA(film->ctx, cudaMemsetAsync(film->sum64.ptr, 0, sizeof(double) * 3 * npix, st));
+        CRG_CUDA(film->ctx, cudaMemsetAsync(film->sumsq64.ptr, 0, sizeof(double) * 3 * npix, st));
+    }
+    film->spp = 0;
+    return CRG_OK;
+}
+
+crg_status crg_film_spp(const crg_film *film, uint64_t *spp) {
+    if (!film || !spp) return CRG_ERR_INVALID_ARG;
+    *spp = film->spp;
+    return CRG_OK;
+}
+
+crg_status crg_film_download(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64, float *aov_albedo,
+                             float *aov_normal, float *aov_depth, crg_stream stream) {
+    if (!film) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = film->ctx;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t npix = (size_t)film->width * film->height;
+    if ((sum64 || sumsq64) && !film->sum64.ptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "film has no FP64 planes");
+    if ((aov_albedo || aov_normal || aov_depth) && !film->aov_albedo.ptr)
+        return set_error(ctx, CRG_ERR_INVALID_ARG, "film has no AOV planes");
+    if (sum_rgb) CRG_CUDA(ctx, cudaMemcpyAsync(sum_rgb, film->sum.ptr, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, st));
+    if (sum64) CRG_CUDA(ctx, cudaMemcpyAsync(sum64, film->sum64.ptr, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, st));
+    if (sumsq64) CRG_CUDA(ctx, cudaMemcpyAsync(sumsq64, film->sumsq64.ptr, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, st));
+    if (aov_albedo) CRG_CUDA(ctx, cudaMemcpyAsync(aov_albedo, film->aov_albedo.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
+    if (aov_normal) CRG_CUDA(ctx, cudaMemcpyAsync(aov_normal, film->aov_normal.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
+    if (aov_depth) CRG_CUDA(ctx, cudaMemcpyAsync(aov_depth, film->aov_depth.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
+    CRG_CUDA(ctx, cudaStreamSynchronize(st));
+    return CRG_OK;
+}
+
+crg_status crg_film_device_ptrs(crg_film *film, float **sum_rgb, double **sum64, double **sumsq64) {
+    if (!film) return CRG_ERR_INVALID_ARG;
+    if (sum_rgb) *sum_rgb = (float *)film->sum.ptr;
+    if (sum64) *sum64 = (double *)film->sum64.ptr;
+    if (sumsq64) *sumsq64 = (double *)film->sumsq64.ptr;
+    return CRG_OK;
+}
+
+crg_status crg_film_display(crg_film *film, float *d_rgba, crg_stream stream) {
+    if (!film || !d_rgba) return set_error(film ? film->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
+    const size_t npix = (size_t)film->width * film->height;
+    const float inv = film->spp ? 1.0f / (float)film->spp : 0.0f;
+    k_display<<<152 * 4, 256, 0, (cudaStream_t)stream>>>((const float *)film->sum.ptr, (float4 *)d_rgba, npix, inv);
+    CRG_CUDA(film->ctx, cudaGetLastError());
+    return CRG_OK;
+}
+
+crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_settings *settings, crg_film *film, crg_stream stream) {
+    if (!scene || !camera || !settings || !film) return set_error(scene ? scene->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
+    crg_context *ctx = scene->ctx;
+    if (!scene->built) return set_error(ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    const crg_settings &s = *settings;
+    if (s.width != film->width || s.height != film->height) return set_error(ctx, CRG_ERR_INVALID_ARG, "settings resolution differs from the film");
+    if (s.mode > CRG_MODE_EXTENDED) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad estimator mode");
+    if (camera->mode > CRG_CAMERA_ORTHOGRAPHIC) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad camera mode");
+    if (s.max_bounces > 1024) return set_error(ctx, CRG_ERR_INVALID_ARG, "max_bounces above 1024");
+    if (film->spp + s.spp > 0xFFFFFFFFull) return set_error(ctx, CRG_ERR_INVALID_ARG, "sample index would exceed 2^32");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (scene->counting) CRG_CUDA(ctx, cudaMemsetAsync(scene->counters.ptr, 0, 64, st));
+    const CamDev cam = camera_params(*camera);
+    crg_status rc = launch_render(scene, cam, s, film, st);
+    if (rc != CRG_OK) return rc;
+    film->spp += s.spp;
+    scene->last_stats.samples = (uint64_t)s.spp * s.width * s.height;
+    if (scene->counting) {
+        unsigned long long c[4];
+        CRG_CUDA(ctx, cudaMemcpyAsync(c, scene->counters.ptr, sizeof(c), cudaMemcpyDeviceToHost, st));
+        CRG_CUDA(ctx, cudaStreamSynchronize(st));
+        scene->last_stats.segments = c[1];
+        scene->last_stats.shadow_rays = c[2];
+    }
+    return CRG_OK;
+}
+
+crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats) {
+    if (!scene || !stats) return CRG_ERR_INVALID_ARG;
+    *stats = scene->last_stats;
+    return CRG_OK;
+}
+
+crg_status crg_scene_set_counting(crg_scene *scene, int enabled) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    scene->counting = enabled ? 1 : 0;
+    return CRG_OK;
+}
+
+} /* extern "C" */

@@ -1,0 +1,101 @@
+// crg_internal.h — host-side objects behind the C ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/crg.h"
+
+struct crg_context {
+    int device = 0;
+    std::string last_error;
+    int sm_count = 0;
+};
+
+// Device buffer owned by a scene or film.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct crg_scene {
+    crg_context *ctx = nullptr;
+    uint32_t ntri = 0;
+    uint32_t nmat = 0;
+    // geometry and materials (original primitive order)
+    DevBuf verts;   // float[ntri*9]
+    DevBuf mat_idx; // uint32[ntri]
+    DevBuf mats;    // crg_material[nmat]
+    std::vector<crg_material> host_mats;
+    // emissive triangles (power-weighted CDF)
+    uint32_t nlights = 0;
+    DevBuf light_prim, light_cdf, light_pdf, mat_light_pdf;
+    // environment / sun
+    DevBuf sky;
+    uint32_t sky_w = 0, sky_h = 0;
+    float sky_rot_u = 0, sky_rot_v = 0;
+    int sun_enabled = 0;
+    crg_sun sun{};
+    float sun_frame[9] = {0}; // tangent, normal, bitangent of build_local(-direction)
+    float sun_cos = 1.0f, sun_pdf = 0.0f;
+    // acceleration structure
+    bool built = false;
+    crg_build_opts opts{8, 0, 3, 3};
+    uint32_t width = 8, node_bytes = 80, n_wide = 0, depth = 0;
+    float sah = 0.0f;
+    DevBuf bvh2;   // float4[2*(ntri-1)]
+    DevBuf order;  // uint32[ntri]
+    DevBuf wide;   // node_bytes * n_wide_capacity
+    DevBuf tris;   // float4[3*ntri]
+    DevBuf err;    // uint32 device error word
+    // statistics
+    int counting = 0;
+    DevBuf counters; // unsigned long long[4]: samples, segments, shadow rays
+    crg_render_stats last_stats{};
+};
+
+struct crg_film {
+    crg_context *ctx = nullptr;
+    uint32_t width = 0, height = 0, flags = 0;
+    uint64_t spp = 0;
+    DevBuf sum;      // float[W*H*3]
+    DevBuf sum64;    // double[W*H*3]
+    DevBuf sumsq64;  // double[W*H*3]
+    DevBuf aov_albedo, aov_normal, aov_depth; // float[W*H*4]
+};
+
+namespace crg {
+
+crg_status set_error(crg_context *ctx, crg_status s, const std::string &msg);
+crg_status cuda_error(crg_context *ctx, cudaError_t e, const char *what);
+crg_status dev_alloc(crg_context *ctx, DevBuf &b, size_t bytes);
+void dev_free(DevBuf &b);
+
+// bvh_build.cu
+crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t stream);
+
+// traverse.cu
+crg_status launch_intersect(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
+                            uint32_t *nodes, uint32_t *tris, uint64_t n, bool any, cudaStream_t stream);
+
+// render.cu
+struct CamDev {
+    float pos[3];
+    float R[9];
+    float w;
+    uint32_t mode;
+    float scale;
+};
+CamDev camera_params(const crg_camera &c);
+crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film,
+                         cudaStream_t stream);
+
+} // namespace crg
+
+#define CRG_CUDA(ctx, call)                                                                                            \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) return crg::cuda_error((ctx), e_, #call);                                               \
+    } while (0)

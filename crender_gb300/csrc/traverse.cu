@@ -1,0 +1,84 @@
+// traverse.cu — batched closest-hit / any-hit queries (the rtcIntersect1 /
+// rtcOccluded1 replacements, CRender src/objects/model.cpp:5-49).
+//
+// One thread per ray; rays are two 16-byte loads, hits one 16-byte store.
+// The wide nodes are read with 16-byte vector loads through the read-only
+// path; per-thread group stack of 64 entries (overflow raises the scene's
+// error word instead of trapping).
+#include "crg_dev.cuh"
+#include "crg_internal.h"
+
+namespace crg {
+namespace {
+
+template <int W, bool ANY, bool COUNT>
+__global__ void __launch_bounds__(256) k_intersect(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris,
+                                                   const float4 *__restrict__ rays, float4 *__restrict__ hits,
+                                                   uint32_t *__restrict__ occluded, uint32_t *__restrict__ ncount,
+                                                   uint32_t *__restrict__ tcount, uint64_t n, uint32_t ntri,
+                                                   uint32_t *__restrict__ err) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 r0 = __ldg(&rays[2 * i]);
+    const float4 r1 = __ldg(&rays[2 * i + 1]);
+    float best_t = INFINITY, bu = 0.0f, bv = 0.0f;
+    uint32_t best_prim = 0xFFFFFFFFu, best_slot;
+    bool occ = false;
+    TravStats st{0, 0};
+    if (ntri > 0) {
+        const RayPre r = ray_prep(r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r0.w);
+        uint32_t e = 0;
+        traverse<W, ANY, COUNT>(nodes, tris, r, r1.w, best_t, best_prim, best_slot, bu, bv, occ, st, e);
+        if (e) atomicOr(err, e);
+    }
+    if (ANY) {
+        occluded[i] = occ ? 1u : 0u;
+    } else {
+        if (best_prim == 0xFFFFFFFFu) {
+            best_t = INFINITY;
+            bu = bv = 0.0f;
+        }
+        hits[i] = make_float4(best_t, __uint_as_float(best_prim), bu, bv);
+    }
+    if (COUNT) {
+        if (ncount) ncount[i] = st.nodes;
+        if (tcount) tcount[i] = st.tris;
+    }
+}
+
+template <int W>
+void launch_w(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded, uint32_t *nodes, uint32_t *tris,
+              uint64_t n, bool any, cudaStream_t st) {
+    const uint32_t T = 256;
+    const uint64_t blocks = (n + T - 1) / T;
+    const uint4 *nd = (const uint4 *)s->wide.ptr;
+    const float4 *tr = (const float4 *)s->tris.ptr;
+    uint32_t *err = (uint32_t *)s->err.ptr;
+    const bool count = nodes || tris;
+    if (any)
+        k_intersect<W, true, false><<<blocks, T, 0, st>>>(nd, tr, (const float4 *)rays, nullptr, occluded, nullptr, nullptr, n,
+                                                           s->ntri, err);
+    else if (count)
+        k_intersect<W, false, true><<<blocks, T, 0, st>>>(nd, tr, (const float4 *)rays, (float4 *)hits, nullptr, nodes, tris, n,
+                                                           s->ntri, err);
+    else
+        k_intersect<W, false, false><<<blocks, T, 0, st>>>(nd, tr, (const float4 *)rays, (float4 *)hits, nullptr, nullptr,
+                                                            nullptr, n, s->ntri, err);
+}
+
+} // namespace
+
+crg_status launch_intersect(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded, uint32_t *nodes,
+                            uint32_t *tris, uint64_t n, bool any, cudaStream_t st) {
+    if (n == 0) return CRG_OK;
+    switch (s->width) {
+    case 2: launch_w<2>(s, rays, hits, occluded, nodes, tris, n, any, st); break;
+    case 4: launch_w<4>(s, rays, hits, occluded, nodes, tris, n, any, st); break;
+    default: launch_w<8>(s, rays, hits, occluded, nodes, tris, n, any, st); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(s->ctx, e, "k_intersect launch");
+    return CRG_OK;
+}
+
+} // namespace crg

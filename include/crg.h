@@ -1,0 +1,286 @@
+/*
+ * crg.h — C ABI of the GB300 render core (BVH build, closest/any-hit traversal,
+ * path-traced rendering with BSDF sampling, next-event estimation and film
+ * accumulation).
+ *
+ * This is the drop-in boundary for CRender's render hot path.  Each entry point
+ * names the reference interface it replaces (paths relative to the CRender
+ * source tree).  Every call returns a crg_status; nothing throws across the ABI
+ * and nothing calls exit().  Device pointers are plain CUDA device addresses;
+ * `crg_stream` is a cudaStream_t (NULL = legacy default stream).
+ *
+ * Threading: a built scene may be queried concurrently from several host
+ * threads (queries only read it).  Mutating calls (create/build/destroy,
+ * set_skybox, set_sun) need external synchronisation, as the reference only
+ * mutates the scene while the renderer is paused (src/render/renderer.cpp:185-192).
+ */
+#ifndef CRG_H
+#define CRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRG_ABI_VERSION 1
+
+typedef struct CUstream_st *crg_stream; /* == cudaStream_t */
+
+typedef enum crg_status {
+    CRG_OK = 0,
+    CRG_ERR_INVALID_ARG = 1, /* null pointer, bad size, bad enum */
+    CRG_ERR_OOM = 2,         /* device or host allocation failed */
+    CRG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    CRG_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
+    CRG_ERR_NOT_BUILT = 5,   /* query on a scene whose BVH is not built */
+    CRG_ERR_UNSUPPORTED = 6, /* option not available in this build */
+    CRG_ERR_DEVICE = 7       /* a kernel reported an internal error word */
+} crg_status;
+
+/* ------------------------------------------------------------------ POD types */
+
+/* One ray, 32 bytes, two float4 loads.  Mirrors the fields the reference fills
+ * in RTCRayHit (src/objects/model.cpp:10-27: org, tnear = 1e-5, dir, tfar = +inf). */
+typedef struct crg_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} crg_ray;
+
+/* Closest-hit record, 16 bytes.  prim = CRG_INVALID_PRIM and t = +inf on a miss.
+ * u, v are the barycentrics of vertices 1 and 2 (Embree's convention, used by
+ * rtcInterpolate0 at src/objects/model.cpp:39-47). */
+typedef struct crg_hit {
+    float t;
+    uint32_t prim;
+    float u;
+    float v;
+} crg_hit;
+#define CRG_INVALID_PRIM 0xFFFFFFFFu
+
+/* Material record; field meaning and defaults follow
+ * cr::material::information (src/render/material/material.h:31-41). */
+typedef enum crg_shade_type {
+    CRG_SHADE_METAL = 0,  /* material.h: metal  */
+    CRG_SHADE_SMOOTH = 1, /* material.h: smooth (Lambertian) */
+    CRG_SHADE_GLASS = 2   /* material.h: glass  */
+} crg_shade_type;
+
+typedef struct crg_material {
+    uint32_t shade_type; /* crg_shade_type; default SMOOTH */
+    float ior;           /* default 1.5 */
+    float roughness;     /* default 0.5 (GGX alpha in the extended estimator) */
+    float reflectiveness;/* default 1   */
+    float emission;      /* scalar emission, default 0; radiance = colour.rgb * emission */
+    float colour[4];     /* RGBA, default (1,1,1,1); alpha 0 = pass-through */
+    int32_t tex;         /* texture index into crg_scene_set_textures, -1 = none */
+    uint32_t pad_[2];
+} crg_material; /* 48 bytes */
+
+/* Sun light; defaults follow cr::entity::sun (src/render/entities/components.h:23-29). */
+typedef struct crg_sun {
+    float size;         /* angular radius in radians, default pi/48 */
+    float intensity;    /* default 100 */
+    float direction[3]; /* default normalize(0.8, -1, 0) */
+    float colour[3];    /* default (1, 0.9, 0.7) */
+} crg_sun;
+
+/* Camera; mirrors cr::camera (src/render/camera.h:12-41): position, Euler
+ * rotation in degrees (applied as Ry(x)*Rx(y)*Rz(z), camera.cpp:54-68),
+ * vertical fov in degrees, projection mode and orthographic scale. */
+typedef enum crg_camera_mode { CRG_CAMERA_PERSPECTIVE = 0, CRG_CAMERA_ORTHOGRAPHIC = 1 } crg_camera_mode;
+typedef struct crg_camera {
+    float position[3];
+    float rotation[3];
+    float fov;
+    uint32_t mode;
+    float scale;
+    uint32_t pad_;
+} crg_camera;
+
+/* Estimator selection.
+ *  FAITHFUL  — the reference estimator of renderer.cpp:21-102 and 258-384
+ *              (Lambert via normal+sphere, mirror metal, Fresnel-less glass,
+ *              emission folded into throughput, optional sun NEE, no MIS).
+ *  EXTENDED  — same path space with emissive-triangle NEE + power-heuristic MIS,
+ *              GGX (VNDF) metal, Fresnel dielectric, two-sided shading normal. */
+typedef enum crg_mode { CRG_MODE_FAITHFUL = 0, CRG_MODE_EXTENDED = 1 } crg_mode;
+
+typedef struct crg_settings {
+    uint32_t width, height; /* film resolution (renderer::set_resolution) */
+    uint32_t spp;           /* samples per pixel added by this call */
+    uint32_t max_bounces;   /* segments per path (renderer::set_max_bounces) */
+    uint32_t rr_depth;      /* Russian roulette from this segment on; 0 = off */
+    uint32_t mode;          /* crg_mode */
+    uint32_t seed;          /* RNG stream key */
+    float aspect;           /* horizontal scale of the image plane; the reference
+                               uses 1 until set_resolution() sets W/H (renderer.cpp:199) */
+} crg_settings;
+
+/* BVH build options (the knob set the autotuner searches). */
+typedef struct crg_build_opts {
+    uint32_t width;        /* wide-BVH branching factor: 2, 4 or 8 (default 8) */
+    uint32_t treelet;      /* 1 = binned-SAH treelet restructuring passes on the LBVH */
+    uint32_t leaf_max;     /* max triangles per wide leaf slot, 1..3 (default 3) */
+    uint32_t treelet_rounds; /* restructuring rounds (default 3) */
+} crg_build_opts;
+
+/* Film flags. */
+#define CRG_FILM_F64 1u  /* also keep FP64 sum and FP64 sum of squares per channel */
+#define CRG_FILM_AOV 2u  /* keep first-hit albedo / normal / depth AOVs */
+
+typedef struct crg_context crg_context;
+typedef struct crg_scene crg_scene;
+typedef struct crg_film crg_film;
+
+/* ------------------------------------------------------------------ context */
+
+/* Creates a context on CUDA device `device` (the thread pool of
+ * src/objects/thread_pool.cpp:3-24 is replaced by kernel launches). */
+crg_status crg_context_create(int device, crg_context **out);
+crg_status crg_context_destroy(crg_context *ctx);
+/* Last error message of this context (never NULL). */
+const char *crg_last_error_string(const crg_context *ctx);
+const char *crg_status_string(crg_status s);
+uint32_t crg_abi_version(void);
+
+/* Device memory helpers for callers without their own allocator. */
+crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr);
+crg_status crg_device_free(crg_context *ctx, void *dptr);
+crg_status crg_memcpy_h2d(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream);
+crg_status crg_memcpy_d2h(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream);
+crg_status crg_stream_sync(crg_context *ctx, crg_stream stream);
+
+/* ------------------------------------------------------------------ scene */
+
+/* Creates a scene from de-indexed triangles, as cr::registry::register_model
+ * stores them after persist_and_expand (src/render/entities/registry.cpp:51-97):
+ *   verts   : host float[ntri*9] (v0.xyz v1.xyz v2.xyz per triangle)
+ *   uvs     : optional host float[ntri*6] per-corner texture coordinates
+ *   mat_idx : host uint32[ntri] per-primitive material index
+ *             (cr::entity::model_materials::indices, components.h:82-97)
+ *   mats    : host crg_material[nmat]
+ * The data are copied to the device; the caller keeps its host arrays.
+ * Replaces cr::model::instance_geometry's shared Embree buffers
+ * (src/objects/model.cpp:52-97) and the material table of the registry. */
+crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri, const float *uvs,
+                            const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
+                            crg_scene **out);
+/* Same, with verts already resident on the device (float[ntri*9] device pointer). */
+crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint32_t ntri,
+                                   const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
+                                   crg_scene **out);
+crg_status crg_scene_destroy(crg_scene *scene);
+
+/* Builds the acceleration structure: LBVH (Morton codes, radix sort, Karras
+ * hierarchy, optional treelet restructuring) collapsed to a compressed wide BVH.
+ * Replaces rtcCommitScene (src/objects/model.cpp:94).  opts may be NULL. */
+crg_status crg_scene_build(crg_scene *scene, const crg_build_opts *opts, crg_stream stream);
+
+/* Equirectangular skybox, host RGBA32F [h][w][4]; replaces cr::scene::set_skybox
+ * and set_skybox_rotation (src/render/scene.cpp:36-65).  A 1x1 image is a
+ * constant environment.  w = h = 0 removes it (misses return black). */
+crg_status crg_scene_set_skybox(crg_scene *scene, const float *rgba, uint32_t w, uint32_t h,
+                                float rot_u, float rot_v);
+/* Sun light for the faithful estimator; replaces cr::scene::set_sun_enabled
+ * and cr::registry::set_sun (scene.cpp:113-121, registry.cpp:248-256). sun may be NULL (defaults). */
+crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun);
+/* Diffuse textures (RGBA32F), referenced by crg_material::tex. */
+crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba,
+                                  const uint32_t *widths, const uint32_t *heights);
+
+/* Introspection of the built structure (for parity checks against a CPU build). */
+typedef struct crg_bvh_info {
+    uint32_t ntri;
+    uint32_t width;
+    uint32_t n_bvh2_nodes;   /* internal nodes of the binary LBVH (ntri-1, or 0) */
+    uint32_t n_wide_nodes;
+    uint32_t node_bytes;     /* bytes per wide node */
+    uint32_t n_tri_slots;    /* triangles in the wide-BVH triangle array */
+    uint32_t depth;          /* wide-BVH depth (levels) */
+    float sah_cost;          /* SAH cost of the binary tree (Ci=1.2, Ct=1) */
+} crg_bvh_info;
+crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info);
+/* Copies to host: bvh2 = float[n_bvh2_nodes*8] (lo.xyz,left, hi.xyz,right; child
+ * ints stored as raw bits, leaves tagged with bit 31), order = uint32[ntri] sorted
+ * primitive order, wide = bytes[n_wide_nodes*node_bytes], tris = float[n_tri_slots*12].
+ * Any pointer may be NULL. */
+crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t *order, void *wide,
+                                  float *tris);
+
+/* ------------------------------------------------------------------ queries */
+
+/* Batched closest hit.  Replaces cr::scene::cast_ray -> cr::model::intersect
+ * -> rtcIntersect1 (src/render/scene.cpp:79-98, src/objects/model.cpp:5-49).
+ * d_rays/d_hits are device arrays of n records.  Ties at equal t go to the
+ * smaller primitive index. */
+crg_status crg_intersect_closest(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits,
+                                 uint64_t n, crg_stream stream);
+/* Batched any hit (occlusion): d_occluded[i] = 1 if some triangle is hit with
+ * tmin < t < tmax.  The reference traces its shadow rays with closest hit
+ * (src/render/renderer.cpp:330-345); this is the rtcOccluded1 equivalent. */
+crg_status crg_intersect_any(const crg_scene *scene, const crg_ray *d_rays, uint32_t *d_occluded,
+                             uint64_t n, crg_stream stream);
+/* Instrumented closest hit: also returns per-ray counts of wide nodes visited and
+ * triangles tested (device uint32 arrays, may be NULL). */
+crg_status crg_intersect_closest_counted(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits,
+                                         uint32_t *d_nodes, uint32_t *d_tris, uint64_t n,
+                                         crg_stream stream);
+
+/* Reads and clears the scene's device error word, which a kernel sets instead
+ * of trapping when a traversal stack would overflow.  Returns CRG_ERR_DEVICE
+ * when it was set.  Synchronises with the device. */
+crg_status crg_scene_poll_error(crg_scene *scene);
+
+/* ------------------------------------------------------------------ film */
+
+/* Film: FP32 RGB running sum (renderer.h:85 _raw_buffer), pixel (x, y) stored
+ * at ((W-1-x) + (H-1-y)*W) as renderer.cpp:358-362 does; optional FP64 sum and
+ * sum of squares; optional AOVs (albedo, normal*0.5+0.5, min(depth,200)/200 as
+ * renderer.cpp:367-369). */
+crg_status crg_film_create(crg_context *ctx, uint32_t width, uint32_t height, uint32_t flags,
+                           crg_film **out);
+crg_status crg_film_destroy(crg_film *film);
+/* Zeroes the sums and the sample count (renderer::start, renderer.cpp:154-170). */
+crg_status crg_film_reset(crg_film *film, crg_stream stream);
+/* Samples per pixel accumulated so far (renderer::current_sample_count). */
+crg_status crg_film_spp(const crg_film *film, uint64_t *spp);
+/* Copies to host; any pointer may be NULL.  sum_rgb float[W*H*3]; sum64,
+ * sumsq64 double[W*H*3]; aov_* float[W*H*4] RGBA as cr::image stores them. */
+crg_status crg_film_download(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64,
+                             float *aov_albedo, float *aov_normal, float *aov_depth, crg_stream stream);
+/* Device pointers of the film arrays (valid until crg_film_destroy). */
+crg_status crg_film_device_ptrs(crg_film *film, float **sum_rgb, double **sum64, double **sumsq64);
+/* Display transform clamp(sum/spp, 0, 1)^(1/2.2) into a device RGBA32F
+ * buffer (renderer.cpp:371-383, the image behind renderer::current_progress). */
+crg_status crg_film_display(crg_film *film, float *d_rgba, crg_stream stream);
+
+/* ------------------------------------------------------------------ render */
+
+/* Renders settings->spp more samples per pixel into the film with the
+ * one-thread-per-pixel megakernel.  Replaces one or more passes of the
+ * renderer's management loop (src/render/renderer.cpp:116-144, 240-384).
+ * Sample indices continue from the film's current count, so repeated calls
+ * draw fresh, reproducible random numbers. */
+crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_settings *settings,
+                      crg_film *film, crg_stream stream);
+
+/* Statistics of the last render on this scene (renderer::current_stats,
+ * renderer.cpp:396-404): segments traced (the reference's ray count,
+ * renderer.cpp:271-272/356) and shadow rays traced. */
+typedef struct crg_render_stats {
+    uint64_t samples;
+    uint64_t segments;
+    uint64_t shadow_rays;
+} crg_render_stats;
+crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats);
+/* Turn on per-launch segment/shadow-ray counting for crg_render (small cost). */
+crg_status crg_scene_set_counting(crg_scene *scene, int enabled);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRG_H */

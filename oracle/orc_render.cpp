@@ -1,0 +1,690 @@
+/*
+ * orc_render.cpp — CPU oracle of the integrator.  TEST INFRASTRUCTURE ONLY.
+ *
+ * FAITHFUL mode restates cr::renderer::_sample_pixel and process_hit
+ * (src/render/renderer.cpp:21-102, 258-384) with CRender's sampling helpers
+ * (src/util/sampling.h:21-183) and camera (src/render/camera.cpp:14-68).
+ * The only deliberate difference is the random number source: the reference
+ * draws from a thread_local std::mt19937 whose stream depends on the thread
+ * schedule (renderer.cpp:6-11); here every draw is a pure function of
+ * (pixel, sample, dimension group, seed) so the GPU can reproduce it.
+ *
+ * EXTENDED mode keeps the same path space and adds power-heuristic MIS
+ * between BSDF sampling and emissive-triangle next-event estimation, a GGX
+ * microfacet metal sampled by visible normals (Heitz, "Sampling the GGX
+ * Distribution of Visible Normals", JCGT 7(4), 2018; D as in
+ * sampling.h:93-106), an exact unpolarised Fresnel dielectric, and Russian
+ * roulette.  Lambertian surfaces scatter into the hemisphere of the geometric
+ * normal as in the reference; GGX and glass use the normal facing the ray.
+ * Its expectation equals the faithful estimator's on Lambertian scenes
+ * without sun.
+ *
+ * Random dimension groups per sample: 0 = pixel jitter; 1 + 2i = BSDF at
+ * segment i (x, y direction, z lobe, w roulette); 2 + 2i = light sample at
+ * segment i (x light, y z point) — the faithful sun uses (x, y).
+ */
+#include "orc.h"
+#include "orc_math.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace orc_internal {
+bool closest(const orc_bvh *b, const crg_ray &ray, crg_hit &hit);
+bool any(const orc_bvh *b, const crg_ray &ray);
+const float *verts(const orc_bvh *b);
+} // namespace orc_internal
+
+using namespace orc;
+
+namespace {
+
+const float kInf = std::numeric_limits<float>::infinity();
+
+struct CamParams {
+    float pos[3];
+    float R[3][3]; /* row-major rotation Ry(x) * Rx(y) * Rz(z) */
+    float w;       /* 1 / tan(fov / 2) */
+    uint32_t mode;
+    float scale;
+};
+
+CamParams camera_params(const crg_camera &c) {
+    CamParams p;
+    for (int a = 0; a < 3; ++a) p.pos[a] = c.position[a];
+    const double k = 3.14159265358979323846 / 180.0;
+    const double ax = c.rotation[0] * k, ay = c.rotation[1] * k, az = c.rotation[2] * k;
+    const double Ry[3][3] = {{std::cos(ax), 0, std::sin(ax)}, {0, 1, 0}, {-std::sin(ax), 0, std::cos(ax)}};
+    const double Rx[3][3] = {{1, 0, 0}, {0, std::cos(ay), -std::sin(ay)}, {0, std::sin(ay), std::cos(ay)}};
+    const double Rz[3][3] = {{std::cos(az), -std::sin(az), 0}, {std::sin(az), std::cos(az), 0}, {0, 0, 1}};
+    double T[3][3], R[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            T[i][j] = 0;
+            for (int m = 0; m < 3; ++m) T[i][j] += Ry[i][m] * Rx[m][j];
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            R[i][j] = 0;
+            for (int m = 0; m < 3; ++m) R[i][j] += T[i][m] * Rz[m][j];
+            p.R[i][j] = (float)R[i][j];
+        }
+    p.w = (float)(1.0 / std::tan(0.5 * (double)c.fov * k));
+    p.mode = c.mode;
+    p.scale = c.scale;
+    return p;
+}
+
+/* camera::get_ray (camera.cpp:14-39) */
+void camera_ray(const CamParams &c, float x, float y, float aspect, v3 &o, v3 &d) {
+    if (c.mode == CRG_CAMERA_ORTHOGRAPHIC) {
+        const float u = 2.0f * x - 1.0f;
+        const float v = 2.0f * y - 1.0f;
+        const float su = c.scale * u, sv = c.scale * v;
+        float org[3];
+        for (int i = 0; i < 3; ++i) org[i] = ((c.R[i][0] * su + c.R[i][1] * sv) + c.R[i][2] * 0.0f) + c.pos[i];
+        o = mk(org[0], org[1], org[2]);
+        d = normalize(mk(c.R[0][2], c.R[1][2], c.R[2][2]));
+        return;
+    }
+    const float u = (2.0f * x - 1.0f) * aspect;
+    const float v = 2.0f * y - 1.0f;
+    float dir[3];
+    for (int i = 0; i < 3; ++i) dir[i] = (c.R[i][0] * u + c.R[i][1] * v) + c.R[i][2] * c.w;
+    o = mk(c.pos[0], c.pos[1], c.pos[2]);
+    d = normalize(mk(dir[0], dir[1], dir[2]));
+}
+
+struct Scene {
+    const orc_bvh *bvh = nullptr;
+    const float *verts = nullptr;
+    const uint32_t *mat_idx = nullptr;
+    const crg_material *mats = nullptr;
+    uint32_t nmat = 0;
+    const float *sky = nullptr;
+    uint32_t sky_w = 0, sky_h = 0;
+    float sky_rot_u = 0, sky_rot_v = 0;
+    bool sun_on = false;
+    crg_sun sun{};
+    onb sun_frame{};
+    float sun_cos = 1, sun_pdf = 0;
+    /* emissive triangles (extended mode) */
+    std::vector<uint32_t> light_prim;
+    std::vector<float> light_cdf, light_pdf;
+    std::vector<float> mat_light_pdf;
+};
+
+/* image::get_uv (src/objects/image.h:104-109): nearest texel, modulo wrap. */
+uint64_t texel_index(float u, uint32_t n) {
+    const float f = u * (float)n;
+    uint64_t i = 0;
+    if (f >= 0.0f) i = f < 4.6e18f ? (uint64_t)f : 0;
+    return i % n;
+}
+
+v3 sample_sky(const Scene &S, v3 d) {
+    if (!S.sky) return mk(0, 0, 0);
+    const float dy = clampf(d.y, -1.0f, 1.0f);
+    const float u = 0.5f + std::atan2(d.z, d.x) * kInvTau;
+    const float v = 0.5f - std::asin(dy) * kInvPi;
+    const uint64_t x = texel_index(u + S.sky_rot_u, S.sky_w);
+    const uint64_t y = texel_index(v + S.sky_rot_v, S.sky_h);
+    const float *t = S.sky + (x + y * S.sky_w) * 4;
+    return mk(t[0], t[1], t[2]);
+}
+
+struct Ctx {
+    const Scene *S;
+    const crg_settings *set;
+    uint32_t pix, sample;
+    uint64_t segments = 0, shadow = 0;
+};
+
+bool cast(const Scene &S, v3 o, v3 d, float tmax, crg_hit &h) {
+    crg_ray r{{o.x, o.y, o.z}, 1e-5f, {d.x, d.y, d.z}, tmax};
+    return orc_internal::closest(S.bvh, r, h);
+}
+
+void tri_verts(const Scene &S, uint32_t prim, v3 &a, v3 &b, v3 &c) {
+    const float *v = S.verts + (size_t)prim * 9;
+    a = mk(v[0], v[1], v[2]);
+    b = mk(v[3], v[4], v[5]);
+    c = mk(v[6], v[7], v[8]);
+}
+
+/* sampling.h:156-166 (cr::sampling::sphere) */
+v3 sphere(float u1, float u2) {
+    const float cos_t = 2.0f * u1 - 1.0f;
+    const float sin_t = std::sqrt(1.0f - cos_t * cos_t);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    return mk(sin_t * cp, cos_t, sin_t * sp);
+}
+
+struct Aov {
+    v3 albedo{0, 0, 0}, normal{0, 0, 0};
+    float depth = 0;
+};
+
+/* ------------------------------------------------------------ faithful */
+
+v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
+    const Scene &S = *C.S;
+    const crg_settings &set = *C.set;
+    v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
+    for (uint32_t i = 0; i < set.max_bounces; ++i) {
+        crg_hit h;
+        C.segments++;
+        if (!cast(S, o, d, kInf, h)) {
+            const v3 env = sample_sky(S, d);
+            if (i == 0) aov.albedo = env;
+            L = add(L, mulv(T, env));
+            break;
+        }
+        const v3 p = add(o, mul(d, h.t));
+        v3 a, b, c;
+        tri_verts(S, h.prim, a, b, c);
+        const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+        const crg_material &m = S.mats[S.mat_idx[h.prim]];
+        const float *col = m.colour;
+        if (col[3] == 0.0f) {
+            o = add(p, mul(d, 0.1f));
+            continue;
+        }
+        v3 albedo = mk(col[0], col[1], col[2]);
+        const f4 g = rand4(C.pix, C.sample, 1 + 2 * i, set.seed);
+        v3 no, nd;
+        if (m.shade_type == CRG_SHADE_GLASS) {
+            const v3 reflected = reflect(d, Ng);
+            v3 out_n = Ng;
+            float eta = 1.0f / m.ior;
+            if (dot(d, Ng) > 0.0f) {
+                out_n = neg(Ng);
+                eta = m.ior;
+            }
+            const v3 uv = normalize(d);
+            const float dt = dot(uv, out_n);
+            const float disc = 1.0f - (eta * eta) * (1.0f - dt * dt);
+            no = add(p, mul(out_n, -0.0001f));
+            if (disc > 0.0f) nd = sub(mul(sub(uv, mul(out_n, dt)), eta), mul(out_n, std::sqrt(disc)));
+            else nd = reflected;
+        } else if (m.shade_type == CRG_SHADE_METAL) {
+            no = add(p, mul(Ng, 0.0001f));
+            nd = reflect(d, Ng);
+            albedo = mul(albedo, m.reflectiveness);
+        } else {
+            const v3 hc = add(Ng, sphere(g.x, g.y));
+            const float l2 = dot(hc, hc);
+            nd = l2 > 0.0f ? mul(hc, 1.0f / std::sqrt(l2)) : Ng;
+            no = add(p, mul(Ng, 0.0001f));
+        }
+        if (i == 0) {
+            aov.albedo = albedo;
+            aov.normal = Ng;
+            aov.depth = h.t;
+        }
+        T = mulv(T, albedo);
+        L = add(L, mul(T, m.emission));
+        if (S.sun_on) {
+            /* renderer.cpp:315-354 */
+            v3 so = add(p, mul(Ng, 0.001f));
+            const f4 g2 = rand4(C.pix, C.sample, 2 + 2 * i, set.seed);
+            float sp, cp;
+            sincos2pi(g2.x, &sp, &cp);
+            const float ct = 1.0f - g2.y * (1.0f - S.sun_cos);
+            const float st = std::sqrt(1.0f - ct * ct);
+            const v3 lv = mk(cp * st, ct, sp * st);
+            const onb &F = S.sun_frame;
+            const v3 sd = mk((F.t.x * lv.x + F.n.x * lv.y) + F.b.x * lv.z, (F.t.y * lv.x + F.n.y * lv.y) + F.b.y * lv.z,
+                             (F.t.z * lv.x + F.n.z * lv.y) + F.b.z * lv.z);
+            const float cosine = clampf(dot(Ng, sd), 0.0f, 1.0f);
+            crg_hit sh;
+            C.shadow++;
+            bool blocked = cast(S, so, sd, kInf, sh);
+            while (blocked) {
+                const crg_material &sm = S.mats[S.mat_idx[sh.prim]];
+                if (sm.colour[3] != 0.0f) break;
+                so = add(add(so, mul(sd, sh.t)), mul(sd, 0.1f));
+                C.shadow++;
+                blocked = cast(S, so, sd, kInf, sh);
+            }
+            if (!blocked) {
+                const v3 ms = mk(-S.sun.direction[0], -S.sun.direction[1], -S.sun.direction[2]);
+                v3 sky = mk(0, 0, 0);
+                if (dot(sd, ms) > S.sun_cos)
+                    sky = mk(S.sun.colour[0] * S.sun.intensity, S.sun.colour[1] * S.sun.intensity,
+                             S.sun.colour[2] * S.sun.intensity);
+                const v3 tc = mulv(T, mk(col[0], col[1], col[2]));
+                L = add(L, mk(((tc.x * cosine) * sky.x) / S.sun_pdf, ((tc.y * cosine) * sky.y) / S.sun_pdf,
+                              ((tc.z * cosine) * sky.z) / S.sun_pdf));
+            }
+        }
+        o = no;
+        d = nd;
+        if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
+            const float q = minf(maxf(maxf(T.x, T.y), T.z), 0.95f);
+            if (g.w >= q) break;
+            T = mk(T.x / q, T.y / q, T.z / q);
+        }
+    }
+    return L;
+}
+
+/* ------------------------------------------------------------ extended */
+
+float ggx_D(float nh, float a) { /* sampling.h:93-106 */
+    const float a2 = a * a;
+    const float dd = (nh * a2 - nh) * nh + 1.0f;
+    return a2 / ((dd * dd) * kPi);
+}
+float ggx_lambda(v3 w, float a) {
+    const float s2 = w.x * w.x + w.y * w.y;
+    const float z2 = w.z * w.z;
+    return (std::sqrt(1.0f + ((a * a) * s2) / z2) - 1.0f) * 0.5f;
+}
+v3 schlick(v3 f0, float c) {
+    const float m = 1.0f - clampf(c, 0.0f, 1.0f);
+    const float m2 = m * m;
+    const float m5 = (m2 * m2) * m;
+    return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+v3 sample_vndf(v3 ve, float a, float u1, float u2) {
+    const v3 vh = normalize(mk(a * ve.x, a * ve.y, ve.z));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    const v3 t1v = lensq > 0.0f ? mul(mk(-vh.y, vh.x, 0.0f), 1.0f / std::sqrt(lensq)) : mk(1, 0, 0);
+    const v3 t2v = cross(vh, t1v);
+    const float r = std::sqrt(u1);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    const float t1 = r * cp;
+    float t2 = r * sp;
+    const float sw = 0.5f * (1.0f + vh.z);
+    t2 = (1.0f - sw) * std::sqrt(1.0f - t1 * t1) + sw * t2;
+    const v3 nh = add(add(mul(t1v, t1), mul(t2v, t2)), mul(vh, std::sqrt(maxf(0.0f, (1.0f - t1 * t1) - t2 * t2))));
+    return normalize(mk(a * nh.x, a * nh.y, maxf(0.0f, nh.z)));
+}
+float fresnel_dielectric(float ci, float eta, float *st2_out) {
+    ci = clampf(ci, 0.0f, 1.0f);
+    const float st2 = (eta * eta) * (1.0f - ci * ci);
+    *st2_out = st2;
+    if (st2 >= 1.0f) return 1.0f;
+    const float ct = std::sqrt(1.0f - st2);
+    const float rs = (eta * ci - ct) / (eta * ci + ct);
+    const float rp = (ci - eta * ct) / (ci + eta * ct);
+    return 0.5f * (rs * rs + rp * rp);
+}
+v3 to_local(const onb &F, v3 w) { return mk(dot(w, F.t), dot(w, F.b), dot(w, F.n)); }
+v3 from_local(const onb &F, v3 l) { return add(add(mul(F.t, l.x), mul(F.b, l.y)), mul(F.n, l.z)); }
+
+uint32_t pick_light(const Scene &S, float u) {
+    uint32_t lo = 0, hi = (uint32_t)S.light_cdf.size() - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (u < S.light_cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+/* Emissive-triangle NEE; bsdf 0 = Lambert (albedo), 1 = GGX (F0, alpha, frame, wol). */
+v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, v3 wol, float alpha) {
+    const Scene &S = *C.S;
+    const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.set->seed);
+    const uint32_t j = pick_light(S, g.x);
+    const uint32_t prim = S.light_prim[j];
+    v3 a, b, c;
+    tri_verts(S, prim, a, b, c);
+    const float su = std::sqrt(g.y);
+    const float b0 = 1.0f - su, b1 = su * (1.0f - g.z), b2 = su * g.z;
+    const v3 pl = add(add(mul(a, b0), mul(b, b1)), mul(c, b2));
+    const v3 po = add(p, mul(n, 1e-4f));
+    const v3 w = sub(pl, po);
+    const float d2 = dot(w, w);
+    if (!(d2 > 0.0f)) return mk(0, 0, 0);
+    const float dist = std::sqrt(d2);
+    const v3 wi = mul(w, 1.0f / dist);
+    const float cos_s = dot(wi, n);
+    if (!(cos_s > 0.0f)) return mk(0, 0, 0);
+    const v3 Ngl = normalize(cross(sub(b, a), sub(c, a)));
+    const float cos_l = absf(dot(Ngl, wi));
+    if (!(cos_l > 0.0f)) return mk(0, 0, 0);
+    C.shadow++;
+    crg_ray sr{{po.x, po.y, po.z}, 1e-5f, {wi.x, wi.y, wi.z}, dist * 0.999f};
+    if (orc_internal::any(S.bvh, sr)) return mk(0, 0, 0);
+    const crg_material &lm = S.mats[S.mat_idx[prim]];
+    const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
+    const float p_light = (S.light_pdf[j] * d2) / cos_l;
+    v3 f;
+    float p_bsdf, cos_i;
+    if (bsdf == 0) {
+        f = mul(albedo, kInvPi);
+        p_bsdf = cos_s * kInvPi;
+        cos_i = cos_s;
+    } else {
+        const v3 wil = to_local(F, wi);
+        if (!(wil.z > 0.0f)) return mk(0, 0, 0);
+        const v3 h = normalize(add(wol, wil));
+        const float woh = dot(wol, h);
+        const float D = ggx_D(h.z, alpha);
+        const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
+        const float G2 = 1.0f / ((1.0f + lo_) + li);
+        const float G1 = 1.0f / (1.0f + lo_);
+        const v3 Fr = schlick(albedo, woh);
+        f = mul(Fr, (D * G2) / ((4.0f * wol.z) * wil.z));
+        p_bsdf = (G1 * D) / (4.0f * wol.z);
+        cos_i = wil.z;
+    }
+    const float w_mis = (p_light * p_light) / (p_light * p_light + p_bsdf * p_bsdf);
+    return mul(mulv(mulv(T, f), Le), (cos_i * w_mis) / p_light);
+}
+
+v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
+    const Scene &S = *C.S;
+    const crg_settings &set = *C.set;
+    v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
+    float prev_pdf = 0.0f;
+    bool prev_delta = true;
+    for (uint32_t i = 0; i < set.max_bounces; ++i) {
+        crg_hit h;
+        C.segments++;
+        if (!cast(S, o, d, kInf, h)) {
+            const v3 env = sample_sky(S, d);
+            if (i == 0) aov.albedo = env;
+            L = add(L, mulv(T, env));
+            break;
+        }
+        const v3 p = add(o, mul(d, h.t));
+        v3 a, b, c;
+        tri_verts(S, h.prim, a, b, c);
+        const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+        const uint32_t mi = S.mat_idx[h.prim];
+        const crg_material &m = S.mats[mi];
+        const float *col = m.colour;
+        if (col[3] == 0.0f) {
+            o = add(p, mul(d, 0.1f));
+            continue;
+        }
+        const v3 rgb = mk(col[0], col[1], col[2]);
+        const float cos_nd = dot(Ng, d);
+        const v3 n = cos_nd < 0.0f ? Ng : neg(Ng);
+        if (i == 0) {
+            aov.albedo = rgb;
+            aov.normal = Ng;
+            aov.depth = h.t;
+        }
+        if (m.emission > 0.0f) {
+            const v3 Le = mk(col[0] * m.emission, col[1] * m.emission, col[2] * m.emission);
+            if (prev_delta) {
+                L = add(L, mulv(T, Le));
+            } else {
+                const float cos_l = absf(cos_nd);
+                if (cos_l > 0.0f) {
+                    const float pl = (S.mat_light_pdf[mi] * (h.t * h.t)) / cos_l;
+                    const float w = (prev_pdf * prev_pdf) / (prev_pdf * prev_pdf + pl * pl);
+                    L = add(L, mul(mulv(T, Le), w));
+                }
+            }
+        }
+        const f4 g = rand4(C.pix, C.sample, 1 + 2 * i, set.seed);
+        const v3 wo = neg(d);
+        /* NEE at hit i estimates light arriving along segment i + 1, which
+         * only exists when i + 1 < max_bounces. */
+        const bool have_lights = !S.light_prim.empty() && i + 1 < set.max_bounces;
+        if (m.shade_type == CRG_SHADE_SMOOTH) {
+            /* Lambert scatters into the hemisphere of the geometric normal
+             * whichever side was hit, as the reference does
+             * (renderer.cpp:93-97): the same integral, estimated better. */
+            const onb F = build_local(Ng);
+            if (have_lights) L = add(L, nee(C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f));
+            float sp, cp;
+            sincos2pi(g.y, &sp, &cp);
+            const float r = std::sqrt(g.x);
+            const v3 l = mk(r * cp, r * sp, std::sqrt(maxf(0.0f, 1.0f - g.x)));
+            d = from_local(F, l);
+            o = add(p, mul(Ng, 1e-4f));
+            prev_pdf = l.z * kInvPi;
+            prev_delta = false;
+            T = mulv(T, rgb);
+        } else if (m.shade_type == CRG_SHADE_METAL) {
+            const v3 f0 = mul(rgb, m.reflectiveness);
+            const float alpha = m.roughness;
+            if (alpha < 1e-4f) {
+                d = reflect(d, n);
+                o = add(p, mul(n, 1e-4f));
+                T = mulv(T, f0);
+                prev_delta = true;
+            } else {
+                const onb F = build_local(n);
+                const v3 wol = to_local(F, wo);
+                if (!(wol.z > 0.0f)) break;
+                if (have_lights) L = add(L, nee(C, i, p, n, T, 1, f0, F, wol, alpha));
+                const v3 hh = sample_vndf(wol, alpha, g.x, g.y);
+                const float woh = dot(wol, hh);
+                const float k2 = 2.0f * woh;
+                const v3 wil = mk(hh.x * k2 - wol.x, hh.y * k2 - wol.y, hh.z * k2 - wol.z);
+                if (!(wil.z > 0.0f)) break;
+                const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
+                const float G1 = 1.0f / (1.0f + lo_);
+                const float G2 = 1.0f / ((1.0f + lo_) + li);
+                const v3 Fr = schlick(f0, woh);
+                T = mulv(T, mul(Fr, G2 / G1));
+                prev_pdf = (G1 * ggx_D(hh.z, alpha)) / (4.0f * wol.z);
+                prev_delta = false;
+                d = from_local(F, wil);
+                o = add(p, mul(n, 1e-4f));
+            }
+        } else {
+            const float eta = cos_nd < 0.0f ? 1.0f / m.ior : m.ior;
+            const float ci = -dot(d, n);
+            float st2;
+            const float Fr = fresnel_dielectric(ci, eta, &st2);
+            if (g.z < Fr) {
+                d = reflect(d, n);
+                o = add(p, mul(n, 1e-4f));
+            } else {
+                const float cic = clampf(ci, 0.0f, 1.0f);
+                const float ct = std::sqrt(1.0f - st2);
+                d = add(mul(d, eta), mul(n, eta * cic - ct));
+                o = add(p, mul(n, -1e-4f));
+            }
+            T = mulv(T, rgb);
+            prev_delta = true;
+        }
+        if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
+            const float q = minf(maxf(maxf(T.x, T.y), T.z), 0.95f);
+            if (g.w >= q) break;
+            T = mk(T.x / q, T.y / q, T.z / q);
+        }
+    }
+    return L;
+}
+
+void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
+    orc_bvh *bvh = nullptr;
+    orc_bvh_build(D.verts, D.ntri, D.build, &bvh);
+    *bvh_out = bvh;
+    S.bvh = bvh;
+    S.verts = D.verts;
+    S.mat_idx = D.mat_idx;
+    S.mats = D.mats;
+    S.nmat = D.nmat;
+    S.sky = (D.skybox && D.sky_w && D.sky_h) ? D.skybox : nullptr;
+    S.sky_w = D.sky_w;
+    S.sky_h = D.sky_h;
+    S.sky_rot_u = D.sky_rot_u;
+    S.sky_rot_v = D.sky_rot_v;
+    S.sun_on = D.sun_enabled != 0;
+    S.sun = D.sun;
+    /* registry.cpp:44-48: sun frame = build_local(-direction) */
+    S.sun_frame = build_local(mk(-D.sun.direction[0], -D.sun.direction[1], -D.sun.direction[2]));
+    S.sun_cos = (float)std::cos((double)D.sun.size);
+    S.sun_pdf = 1.0f / (kTau * (1.0f - S.sun_cos));
+    /* emissive triangles, power weighted (area x luminance) */
+    std::vector<double> lum(D.nmat, 0.0);
+    for (uint32_t m = 0; m < D.nmat; ++m) {
+        const crg_material &mm = D.mats[m];
+        if (mm.emission > 0.0f) {
+            const float r = mm.colour[0] * mm.emission, g = mm.colour[1] * mm.emission, b = mm.colour[2] * mm.emission;
+            lum[m] = 0.2126 * (double)r + 0.7152 * (double)g + 0.0722 * (double)b;
+        }
+    }
+    std::vector<double> w;
+    double total = 0.0;
+    for (uint32_t p = 0; p < D.ntri; ++p) {
+        const uint32_t m = D.mat_idx[p];
+        if (!(lum[m] > 0.0)) continue;
+        const float *v = D.verts + (size_t)p * 9;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = (double)v[3 + a] - (double)v[a];
+            e2[a] = (double)v[6 + a] - (double)v[a];
+        }
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                     cz = e1[0] * e2[1] - e1[1] * e2[0];
+        const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        const double wt = area * lum[m];
+        S.light_prim.push_back(p);
+        w.push_back(wt);
+        total += wt;
+    }
+    S.mat_light_pdf.assign(D.nmat, 0.0f);
+    if (!(total > 0.0)) {
+        S.light_prim.clear();
+        return;
+    }
+    double cum = 0.0;
+    for (size_t j = 0; j < w.size(); ++j) {
+        cum += w[j];
+        S.light_cdf.push_back((float)(cum / total));
+        S.light_pdf.push_back((float)(lum[D.mat_idx[S.light_prim[j]]] / total));
+    }
+    S.light_cdf.back() = 1.0f;
+    for (uint32_t m = 0; m < D.nmat; ++m) S.mat_light_pdf[m] = (float)(lum[m] / total);
+}
+
+} // namespace
+
+extern "C" {
+
+void orc_sincos2pi(float u, float *s, float *c) { sincos2pi(u, s, c); }
+
+void orc_rand4(uint32_t pixel, uint32_t sample, uint32_t group, uint32_t seed, float *out4) {
+    const f4 r = rand4(pixel, sample, group, seed);
+    out4[0] = r.x;
+    out4[1] = r.y;
+    out4[2] = r.z;
+    out4[3] = r.w;
+}
+
+void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx, float jy,
+                    float *org, float *dir) {
+    const CamParams cp = camera_params(*cam);
+    const float x = ((float)px + jx) / (float)set->width;
+    const float y = ((float)py + jy) / (float)set->height;
+    v3 o, d;
+    camera_ray(cp, x, y, set->aspect, o, d);
+    org[0] = o.x; org[1] = o.y; org[2] = o.z;
+    dir[0] = d.x; dir[1] = d.y; dir[2] = d.z;
+}
+
+int orc_render_rows(const orc_scene_desc *desc, const crg_camera *cam, const crg_settings *set, orc_film *film,
+                    uint32_t y0, uint32_t y1, int nthreads) {
+    if (!desc || !cam || !set || !film || !film->sum_rgb) return CRG_ERR_INVALID_ARG;
+    if (set->width != film->width || set->height != film->height) return CRG_ERR_INVALID_ARG;
+    if (y1 > set->height) y1 = set->height;
+    Scene S;
+    orc_bvh *bvh = nullptr;
+    prepare(*desc, S, &bvh);
+    const CamParams cp = camera_params(*cam);
+    const uint32_t W = set->width, H = set->height;
+    const uint64_t npix = (uint64_t)W * (y1 > y0 ? (y1 - y0) : 0);
+    std::atomic<uint64_t> seg{0}, shad{0};
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<uint64_t> next{0};
+    auto work = [&]() {
+        uint64_t my_seg = 0, my_sh = 0;
+        for (;;) {
+            const uint64_t s0 = next.fetch_add(64);
+            if (s0 >= npix) break;
+            const uint64_t e0 = std::min<uint64_t>(npix, s0 + 64);
+            for (uint64_t q = s0; q < e0; ++q) {
+                const uint32_t px = (uint32_t)(q % W), py = y0 + (uint32_t)(q / W);
+                const uint32_t pix = py * W + px;
+                const uint64_t fidx = (uint64_t)(W - 1 - px) + (uint64_t)(H - 1 - py) * W;
+                float acc[3] = {film->sum_rgb[fidx * 3], film->sum_rgb[fidx * 3 + 1], film->sum_rgb[fidx * 3 + 2]};
+                Aov aov;
+                for (uint32_t s = 0; s < set->spp; ++s) {
+                    Ctx C{&S, set, pix, (uint32_t)(film->spp + s)};
+                    const f4 g0 = rand4(pix, C.sample, 0, set->seed);
+                    const float x = ((float)px + g0.x) / (float)W;
+                    const float y = ((float)py + g0.y) / (float)H;
+                    v3 o, d;
+                    camera_ray(cp, x, y, set->aspect, o, d);
+                    aov = Aov();
+                    const v3 L = set->mode == CRG_MODE_EXTENDED ? trace_extended(C, o, d, aov)
+                                                                : trace_faithful(C, o, d, aov);
+                    acc[0] += L.x;
+                    acc[1] += L.y;
+                    acc[2] += L.z;
+                    if (film->sum64) {
+                        film->sum64[fidx * 3] += (double)L.x;
+                        film->sum64[fidx * 3 + 1] += (double)L.y;
+                        film->sum64[fidx * 3 + 2] += (double)L.z;
+                    }
+                    if (film->sumsq64) {
+                        film->sumsq64[fidx * 3] += (double)L.x * (double)L.x;
+                        film->sumsq64[fidx * 3 + 1] += (double)L.y * (double)L.y;
+                        film->sumsq64[fidx * 3 + 2] += (double)L.z * (double)L.z;
+                    }
+                    my_seg += C.segments;
+                    my_sh += C.shadow;
+                }
+                film->sum_rgb[fidx * 3] = acc[0];
+                film->sum_rgb[fidx * 3 + 1] = acc[1];
+                film->sum_rgb[fidx * 3 + 2] = acc[2];
+                if (set->spp > 0) {
+                    /* renderer.cpp:367-369 */
+                    if (film->aov_albedo) {
+                        float *t = film->aov_albedo + fidx * 4;
+                        t[0] = aov.albedo.x; t[1] = aov.albedo.y; t[2] = aov.albedo.z; t[3] = 1.0f;
+                    }
+                    if (film->aov_normal) {
+                        float *t = film->aov_normal + fidx * 4;
+                        t[0] = aov.normal.x * 0.5f + 0.5f;
+                        t[1] = aov.normal.y * 0.5f + 0.5f;
+                        t[2] = aov.normal.z * 0.5f + 0.5f;
+                        t[3] = 1.0f;
+                    }
+                    if (film->aov_depth) {
+                        float *t = film->aov_depth + fidx * 4;
+                        const float dv = minf(aov.depth, 200.0f) / 200.0f;
+                        t[0] = dv; t[1] = dv; t[2] = dv; t[3] = 1.0f;
+                    }
+                }
+            }
+        }
+        seg += my_seg;
+        shad += my_sh;
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work);
+    for (auto &t : th) t.join();
+    film->segments += seg.load();
+    film->shadow_rays += shad.load();
+    orc_bvh_free(bvh);
+    return CRG_OK;
+}
+
+int orc_render(const orc_scene_desc *desc, const crg_camera *cam, const crg_settings *set, orc_film *film,
+               int nthreads) {
+    const int rc = orc_render_rows(desc, cam, set, film, 0, set ? set->height : 0, nthreads);
+    if (rc == CRG_OK) film->spp += set->spp;
+    return rc;
+}
+
+} /* extern "C" */
