@@ -79,7 +79,8 @@ class BvhInfo(C.Structure):
 
 
 class RenderStats(C.Structure):
-    _fields_ = [("samples", C.c_uint64), ("segments", C.c_uint64), ("shadow_rays", C.c_uint64)]
+    _fields_ = [("samples", C.c_uint64), ("segments", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64)]
 
 
 # numpy views of the same layouts
@@ -131,6 +132,8 @@ CRG_SIGNATURES = [
     ("crg_memcpy_h2d", C.c_int, [vp, vp, vp, C.c_size_t, c_stream]),
     ("crg_memcpy_d2h", C.c_int, [vp, vp, vp, C.c_size_t, c_stream]),
     ("crg_stream_sync", C.c_int, [vp, c_stream]),
+    ("crg_host_alloc", C.c_int, [vp, C.c_size_t, P(vp)]),
+    ("crg_host_free", C.c_int, [vp, vp]),
     ("crg_scene_create", C.c_int, [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, P(vp)]),
     ("crg_scene_create_device", C.c_int, [vp, vp, C.c_uint32, vp, vp, C.c_uint32, P(vp)]),
     ("crg_scene_destroy", C.c_int, [vp]),

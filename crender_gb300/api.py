@@ -92,6 +92,25 @@ class DeviceBuffer:
             self.ptr = C.c_void_p()
 
 
+class PinnedArray:
+    """numpy view of page-locked host memory from crg_host_alloc."""
+
+    def __init__(self, ctx: Context, shape, dtype):
+        self.ctx = ctx
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        self.ptr = C.c_void_p()
+        ctx.check(ctx.lib.crg_host_alloc(ctx.h, max(nbytes, 1), C.byref(self.ptr)))
+        buf = (C.c_uint8 * max(nbytes, 1)).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, np.uint8, nbytes).view(dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.ctx.lib.crg_host_free(self.ctx.h, self.ptr)
+            self.ptr = C.c_void_p()
+
+
 class Scene:
     """cr::scene over the GPU path: geometry, materials, sky, sun, BVH."""
 
@@ -173,7 +192,8 @@ class Scene:
     def stats(self) -> dict:
         s = _abi.RenderStats()
         self.ctx.check(self.ctx.lib.crg_render_stats_get(self.h, C.byref(s)))
-        return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays)
+        return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays,
+                    nodes_visited=s.nodes_visited, tris_tested=s.tris_tested)
 
     def close(self):
         if self.h:

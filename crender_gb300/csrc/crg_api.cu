@@ -285,6 +285,20 @@ crg_status crg_memcpy_d2h(crg_context *ctx, void *dst, const void *src, size_t b
     return CRG_OK;
 }
 
+crg_status crg_host_alloc(crg_context *ctx, size_t bytes, void **hptr) {
+    if (!ctx || !hptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
+    *hptr = nullptr;
+    if (bytes == 0) return CRG_OK;
+    CRG_CUDA(ctx, cudaHostAlloc(hptr, bytes, cudaHostAllocDefault));
+    return CRG_OK;
+}
+
+crg_status crg_host_free(crg_context *ctx, void *hptr) {
+    if (!ctx) return CRG_ERR_INVALID_ARG;
+    if (hptr) CRG_CUDA(ctx, cudaFreeHost(hptr));
+    return CRG_OK;
+}
+
 crg_status crg_stream_sync(crg_context *ctx, crg_stream stream) {
     if (!ctx) return CRG_ERR_INVALID_ARG;
     CRG_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
@@ -575,11 +589,13 @@ crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_sett
     film->spp += s.spp;
     scene->last_stats.samples = (uint64_t)s.spp * s.width * s.height;
     if (scene->counting) {
-        unsigned long long c[4];
+        unsigned long long c[8];
         CRG_CUDA(ctx, cudaMemcpyAsync(c, scene->counters.ptr, sizeof(c), cudaMemcpyDeviceToHost, st));
         CRG_CUDA(ctx, cudaStreamSynchronize(st));
         scene->last_stats.segments = c[1];
         scene->last_stats.shadow_rays = c[2];
+        scene->last_stats.nodes_visited = c[3];
+        scene->last_stats.tris_tested = c[4];
     }
     return CRG_OK;
 }

@@ -86,25 +86,12 @@ struct Hit {
     uint32_t prim, slot;
 };
 
-template <int W>
-__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, uint32_t &err) {
-    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
-    bool occ;
-    TravStats st;
-    traverse<W, false, false>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, err);
-    return h.prim != 0xFFFFFFFFu;
-}
+struct PathCtx;
 
-template <int W>
-__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, uint32_t &err) {
-    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
-    float t, u, v;
-    uint32_t p, sl;
-    bool occ;
-    TravStats st;
-    traverse<W, true, false>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, err);
-    return occ;
-}
+template <int W, bool CNT>
+__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C);
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C);
 
 __device__ __forceinline__ void slot_verts(const SceneDev &S, uint32_t slot, v3 &a, v3 &b, v3 &c) {
     const float4 x = __ldg(&S.tris[slot * 3 + 0]);
@@ -158,16 +145,45 @@ struct PathCtx {
     uint32_t pix, sample, seed;
     uint32_t segments, shadow;
     uint32_t err;
+    unsigned long long nodes, tris; // traversal work, counted only in the instrumented variant
 };
 
+template <int W, bool CNT>
+__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C) {
+    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+    bool occ;
+    TravStats st{0, 0};
+    traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
+    if (CNT) {
+        C.nodes += st.nodes;
+        C.tris += st.tris;
+    }
+    return h.prim != 0xFFFFFFFFu;
+}
+
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C) {
+    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+    float t, u, v;
+    uint32_t p, sl;
+    bool occ;
+    TravStats st{0, 0};
+    traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
+    if (CNT) {
+        C.nodes += st.nodes;
+        C.tris += st.tris;
+    }
+    return occ;
+}
+
 // ------------------------------------------------------------------ faithful
-template <int W>
+template <int W, bool CNT>
 __device__ v3 trace_faithful(const SceneDev &S, const crg_settings &set, PathCtx &C, v3 o, v3 d, Aov &aov) {
     v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
     for (uint32_t i = 0; i < set.max_bounces; ++i) {
         Hit h;
         C.segments++;
-        if (!closest<W>(S, o, d, INFINITY, h, C.err)) {
+        if (!closest<W, CNT>(S, o, d, INFINITY, h, C)) {
             const v3 env = sample_sky(S, d);
             if (i == 0) aov.albedo = env;
             L = add(L, mulv(T, env));
@@ -232,12 +248,12 @@ __device__ v3 trace_faithful(const SceneDev &S, const crg_settings &set, PathCtx
             const float cosine = clampf(dot(Ng, sd), 0.0f, 1.0f);
             Hit sh;
             C.shadow++;
-            bool blocked = closest<W>(S, so, sd, INFINITY, sh, C.err);
+            bool blocked = closest<W, CNT>(S, so, sd, INFINITY, sh, C);
             while (blocked) {
                 if (S.mats[__ldg(&S.mat_idx[sh.prim])].colour[3] != 0.0f) break;
                 so = add(add(so, mul(sd, sh.t)), mul(sd, 0.1f));
                 C.shadow++;
-                blocked = closest<W>(S, so, sd, INFINITY, sh, C.err);
+                blocked = closest<W, CNT>(S, so, sd, INFINITY, sh, C);
             }
             if (!blocked) {
                 const v3 ms = mk(S.sun_neg_dir[0], S.sun_neg_dir[1], S.sun_neg_dir[2]);
@@ -314,7 +330,7 @@ __device__ __forceinline__ uint32_t pick_light(const SceneDev &S, float u) {
     return lo;
 }
 
-template <int W>
+template <int W, bool CNT>
 __device__ v3 nee(const SceneDev &S, PathCtx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, v3 wol,
                   float alpha) {
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
@@ -337,7 +353,7 @@ __device__ v3 nee(const SceneDev &S, PathCtx &C, uint32_t i, v3 p, v3 n, v3 T, i
     const float cos_l = absf(dot(Ngl, wi));
     if (!(cos_l > 0.0f)) return mk(0, 0, 0);
     C.shadow++;
-    if (occluded<W>(S, po, wi, dist * 0.999f, C.err)) return mk(0, 0, 0);
+    if (occluded<W, CNT>(S, po, wi, dist * 0.999f, C)) return mk(0, 0, 0);
     const crg_material &lm = S.mats[__ldg(&S.mat_idx[prim])];
     const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
     const float p_light = (__ldg(&S.light_pdf[j]) * d2) / cos_l;
@@ -365,7 +381,7 @@ __device__ v3 nee(const SceneDev &S, PathCtx &C, uint32_t i, v3 p, v3 n, v3 T, i
     return mul(mulv(mulv(T, f), Le), (cos_i * w_mis) / p_light);
 }
 
-template <int W>
+template <int W, bool CNT>
 __device__ v3 trace_extended(const SceneDev &S, const crg_settings &set, PathCtx &C, v3 o, v3 d, Aov &aov) {
     v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
     float prev_pdf = 0.0f;
@@ -373,7 +389,7 @@ __device__ v3 trace_extended(const SceneDev &S, const crg_settings &set, PathCtx
     for (uint32_t i = 0; i < set.max_bounces; ++i) {
         Hit h;
         C.segments++;
-        if (!closest<W>(S, o, d, INFINITY, h, C.err)) {
+        if (!closest<W, CNT>(S, o, d, INFINITY, h, C)) {
             const v3 env = sample_sky(S, d);
             if (i == 0) aov.albedo = env;
             L = add(L, mulv(T, env));
@@ -418,7 +434,7 @@ __device__ v3 trace_extended(const SceneDev &S, const crg_settings &set, PathCtx
         const uint32_t shade = m.shade_type;
         if (shade == CRG_SHADE_SMOOTH) {
             const onb F = build_local(Ng);
-            if (have_lights) L = add(L, nee<W>(S, C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f));
+            if (have_lights) L = add(L, nee<W, CNT>(S, C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f));
             float sp, cp;
             sincos2pi(g.y, &sp, &cp);
             const float r = sqrtf(g.x);
@@ -440,7 +456,7 @@ __device__ v3 trace_extended(const SceneDev &S, const crg_settings &set, PathCtx
                 const onb F = build_local(n);
                 const v3 wol = to_local(F, wo);
                 if (!(wol.z > 0.0f)) break;
-                if (have_lights) L = add(L, nee<W>(S, C, i, p, n, T, 1, f0, F, wol, alpha));
+                if (have_lights) L = add(L, nee<W, CNT>(S, C, i, p, n, T, 1, f0, F, wol, alpha));
                 const v3 hh = sample_vndf(wol, alpha, g.x, g.y);
                 const float woh = dot(wol, hh);
                 const float k2 = 2.0f * woh;
@@ -500,11 +516,11 @@ __device__ __forceinline__ void camera_ray(const CamDev &c, float x, float y, fl
                      (c.R[6] * u + c.R[7] * v) + c.R[8] * c.w));
 }
 
-template <int W, int MODE>
+template <int W, int MODE, bool CNT>
 __global__ void __launch_bounds__(128) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
-    PathCtx C{pix, 0, set.seed, 0, 0, 0};
+    PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
     if (pix < Wd * Hd) {
         const uint32_t px = pix % Wd, py = pix / Wd;
         const size_t fidx = (size_t)(Wd - 1 - px) + (size_t)(Hd - 1 - py) * Wd;
@@ -525,7 +541,7 @@ __global__ void __launch_bounds__(128) k_render(SceneDev S, CamDev cam, crg_sett
             aov.albedo = mk(0, 0, 0);
             aov.normal = mk(0, 0, 0);
             aov.depth = 0.0f;
-            const v3 L = MODE == CRG_MODE_EXTENDED ? trace_extended<W>(S, set, C, o, d, aov) : trace_faithful<W>(S, set, C, o, d, aov);
+            const v3 L = MODE == CRG_MODE_EXTENDED ? trace_extended<W, CNT>(S, set, C, o, d, aov) : trace_faithful<W, CNT>(S, set, C, o, d, aov);
             acc[0] += L.x;
             acc[1] += L.y;
             acc[2] += L.z;
@@ -552,16 +568,20 @@ __global__ void __launch_bounds__(128) k_render(SceneDev S, CamDev cam, crg_sett
         }
     }
     if (C.err) atomicOr(S.err, C.err);
-    if (S.counters) {
-        unsigned long long seg = C.segments, sh = C.shadow;
+    if (CNT) {
+        unsigned long long seg = C.segments, sh = C.shadow, nd = C.nodes, tr = C.tris;
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
             seg += __shfl_xor_sync(0xFFFFFFFFu, seg, off);
             sh += __shfl_xor_sync(0xFFFFFFFFu, sh, off);
+            nd += __shfl_xor_sync(0xFFFFFFFFu, nd, off);
+            tr += __shfl_xor_sync(0xFFFFFFFFu, tr, off);
         }
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(&S.counters[1], seg);
             atomicAdd(&S.counters[2], sh);
+            atomicAdd(&S.counters[3], nd);
+            atomicAdd(&S.counters[4], tr);
         }
     }
 }
@@ -572,8 +592,13 @@ void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, con
     const uint32_t T = 128;
     const uint64_t npix = (uint64_t)set.width * set.height;
     const uint32_t blocks = (uint32_t)((npix + T - 1) / T);
-    if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-    else k_render<W, CRG_MODE_FAITHFUL><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+    if (S.counters) {
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, true><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, true><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+    } else {
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, false><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, false><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+    }
 }
 
 } // namespace

@@ -133,3 +133,21 @@ def soup_rays(n, seed, shadow=False):
     r["tmin"] = np.float32(1e-5)
     r["tmax"] = rng.uniform(0.1, 1.0, n).astype(np.float32) if shadow else np.float32(np.inf)
     return r
+
+
+def closed_box(albedo=0.5, emission=1.0):
+    """Furnace scene: the six inward-facing faces of the unit cube, every face
+    Lambertian with the given albedo and emission, camera inside.  Every path
+    of the reference estimator hits a wall at every segment, so one sample is
+    exactly sum_{k=1..B} albedo^k * emission (renderer.cpp:310-311)."""
+    tris = []
+    tris += _quad([(0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)], (0, 1, 0))
+    tris += _quad([(0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)], (0, -1, 0))
+    tris += _quad([(0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1)], (0, 0, -1))
+    tris += _quad([(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)], (0, 0, 1))
+    tris += _quad([(0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)], (1, 0, 0))
+    tris += _quad([(1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)], (-1, 0, 0))
+    verts = np.asarray(tris, np.float64).astype(np.float32)
+    mats = material_table([{"colour": (albedo, albedo, albedo, 1.0), "emission": emission}])
+    camera = dict(position=(0.5, 0.5, 0.3), rotation=(0.0, 0.0, 0.0), fov=60.0)
+    return dict(verts=np.ascontiguousarray(verts), mat_idx=np.zeros(12, np.uint32), mats=mats, camera=camera)

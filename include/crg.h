@@ -153,6 +153,9 @@ crg_status crg_device_free(crg_context *ctx, void *dptr);
 crg_status crg_memcpy_h2d(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream);
 crg_status crg_memcpy_d2h(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream);
 crg_status crg_stream_sync(crg_context *ctx, crg_stream stream);
+/* Page-locked host memory (fast, asynchronous host<->device copies). */
+crg_status crg_host_alloc(crg_context *ctx, size_t bytes, void **hptr);
+crg_status crg_host_free(crg_context *ctx, void *hptr);
 
 /* ------------------------------------------------------------------ scene */
 
@@ -275,9 +278,12 @@ typedef struct crg_render_stats {
     uint64_t samples;
     uint64_t segments;
     uint64_t shadow_rays;
+    uint64_t nodes_visited; /* wide nodes loaded by all traversals (counting mode) */
+    uint64_t tris_tested;   /* triangles tested by all traversals (counting mode) */
 } crg_render_stats;
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats);
-/* Turn on per-launch segment/shadow-ray counting for crg_render (small cost). */
+/* Turn on per-launch counting of segments, shadow rays, nodes visited and
+ * triangles tested for crg_render (runs an instrumented kernel variant). */
 crg_status crg_scene_set_counting(crg_scene *scene, int enabled);
 
 #ifdef __cplusplus

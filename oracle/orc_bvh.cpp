@@ -539,8 +539,10 @@ inline bool accept(float t, uint32_t prim, float tmin, float best_t, uint32_t be
     return t == best_t && best_prim != CRG_INVALID_PRIM && prim < best_prim;
 }
 
-bool slab(const RayPre &r, const Box &b, float tmax) {
-    float t0 = r.tmin, t1 = tmax;
+bool slab(const RayPre &r, const Box &b, float tmax, float *tnear = nullptr) {
+    /* the far bound keeps the tolerance after clamping to the best hit so far,
+     * so a box holding an exact t-tie is never culled by slab rounding */
+    float t0 = r.tmin, t1 = tmax * 1.00000036f;
     for (int a = 0; a < 3; ++a) {
         float tn = (b.lo[a] - r.o[a]) * r.invd[a];
         float tf = (b.hi[a] - r.o[a]) * r.invd[a];
@@ -550,6 +552,7 @@ bool slab(const RayPre &r, const Box &b, float tmax) {
         t1 = tf < t1 ? tf : t1;
         if (t0 > t1) return false;
     }
+    if (tnear) *tnear = t0;
     return true;
 }
 
@@ -563,12 +566,21 @@ void trace(const orc_bvh &B, const crg_ray &ray, crg_hit &hit, bool &occl) {
     const RayPre r = prep(ray);
     float best_t = r.tmax;
     uint32_t best_prim = CRG_INVALID_PRIM;
+    /* front-to-back: children are tested on push, the nearer one popped first;
+     * entries carry their entry distance and are skipped once beyond best_t */
     uint32_t stack[128];
+    float stack_t[128];
     int sp = 0;
-    stack[sp++] = B.root();
+    {
+        float t0;
+        if (!slab(r, B.box_of(B.root()), best_t, &t0)) return;
+        stack[sp] = B.root();
+        stack_t[sp++] = t0;
+    }
     while (sp > 0) {
-        const uint32_t x = stack[--sp];
-        if (!slab(r, B.box_of(x), best_t)) continue;
+        --sp;
+        const uint32_t x = stack[sp];
+        if (stack_t[sp] > best_t * 1.00000036f) continue;
         if (x & LEAF) {
             const uint32_t prim = B.order[x & ~LEAF];
             const float *v = &B.verts[(size_t)prim * 9];
@@ -588,8 +600,22 @@ void trace(const orc_bvh &B, const crg_ray &ray, crg_hit &hit, bool &occl) {
             }
         } else {
             if (sp + 2 > 128) continue; /* cannot happen for n < 2^30 */
-            stack[sp++] = B.right[x];
-            stack[sp++] = B.left[x];
+            float tl = 0.0f, tr = 0.0f;
+            const bool hl = slab(r, B.box_of(B.left[x]), best_t, &tl);
+            const bool hr = slab(r, B.box_of(B.right[x]), best_t, &tr);
+            if (hl && hr) {
+                const bool left_first = tl <= tr;
+                stack[sp] = left_first ? B.right[x] : B.left[x];
+                stack_t[sp++] = left_first ? tr : tl;
+                stack[sp] = left_first ? B.left[x] : B.right[x];
+                stack_t[sp++] = left_first ? tl : tr;
+            } else if (hl) {
+                stack[sp] = B.left[x];
+                stack_t[sp++] = tl;
+            } else if (hr) {
+                stack[sp] = B.right[x];
+                stack_t[sp++] = tr;
+            }
         }
     }
 }
