@@ -105,6 +105,7 @@ MODE_FAITHFUL, MODE_EXTENDED = 0, 1
 CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
 FILM_F64, FILM_AOV = 1, 2
 INVALID_PRIM = 0xFFFFFFFF
+NOALLOC_MAX_TRIS = 16384
 
 STATUS = {
     0: "OK",
@@ -143,6 +144,7 @@ CRG_SIGNATURES = [
     ("crg_scene_set_textures", C.c_int, [vp, C.c_uint32, P(vp), vp, vp]),
     ("crg_scene_bvh_info", C.c_int, [vp, P(BvhInfo)]),
     ("crg_scene_bvh_download", C.c_int, [vp, vp, vp, vp, vp]),
+    ("crg_build_bvh_noalloc", C.c_int, [vp, C.c_uint32, P(BuildOpts), vp, C.c_size_t, vp, vp, P(BvhInfo), c_stream]),
     ("crg_intersect_closest", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_any", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_closest_counted", C.c_int, [vp, vp, vp, vp, vp, C.c_uint64, c_stream]),

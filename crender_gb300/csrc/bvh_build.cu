@@ -16,6 +16,7 @@
 // CPU run of the same algorithm.
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 
 #include "crg_dev.cuh"
 #include "crg_internal.h"
@@ -786,3 +787,188 @@ crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t st) {
 }
 
 } // namespace crg
+
+// ----------------------------------------------------------------- build without allocation
+// crg_build_bvh_noalloc: the same pipeline as build_bvh for callers that may
+// not allocate device memory (see include/crg.h).  Its scratch lives in one
+// file-scope __device__ array sized for CRG_NOALLOC_MAX_TRIS triangles; every
+// GPU that loads this library holds it until the process exits.
+namespace crg {
+namespace {
+
+constexpr size_t kNaN = CRG_NOALLOC_MAX_TRIS; // max triangles
+constexpr size_t kNaN1 = kNaN + 1;
+constexpr size_t kNaBlk = (kNaN + kSortTile - 1) / kSortTile;
+constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+// section sizes in bytes, each rounded to 256
+constexpr size_t kNaTbox = na_round(sizeof(float4) * 2 * kNaN);
+constexpr size_t kNaNbox = na_round(sizeof(float4) * 2 * kNaN);
+constexpr size_t kNaCb = na_round(sizeof(uint32_t) * 8);
+constexpr size_t kNaKey = na_round(sizeof(uint32_t) * kNaN);
+constexpr size_t kNaHist = na_round(sizeof(uint32_t) * 256 * kNaBlk);
+constexpr size_t kNaU32N = na_round(sizeof(uint32_t) * kNaN);
+constexpr size_t kNaU32N1 = na_round(sizeof(uint32_t) * kNaN1);
+constexpr size_t kNaEnts = na_round(sizeof(uint32_t) * 8 * kNaN1);
+constexpr size_t kNaTotals = na_round(sizeof(uint32_t) * 2);
+constexpr size_t kNaBytes = kNaTbox + kNaNbox + kNaCb + 4 * kNaKey + kNaHist + 5 * kNaU32N + 2 * kNaU32N1 + kNaEnts +
+                            3 * kNaU32N1 + kNaTotals;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// Device address of g_noalloc_scratch per device, fetched once with that
+// device current (the host-side symbol is only a stand-in).
+constexpr int kNaMaxDevices = 64;
+unsigned char *g_noalloc_ptr[kNaMaxDevices] = {nullptr};
+std::mutex g_noalloc_mutex;
+
+crg_status noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return CRG_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            (void)cudaGetLastError();
+            return CRG_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = (unsigned char *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return CRG_OK;
+}
+
+} // namespace
+} // namespace crg
+
+extern "C" crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri, const crg_build_opts *opts,
+                                            void *d_wide, size_t wide_bytes, float *d_tris, uint32_t *d_order,
+                                            crg_bvh_info *info, crg_stream stream) {
+    using namespace crg;
+    crg_build_opts o{8, 0, 3, 3};
+    if (opts) o = *opts;
+    if (!((o.width == 2 || o.width == 4 || o.width == 8) && o.leaf_max >= 1 && o.leaf_max <= 3 && o.treelet_rounds <= 8))
+        return CRG_ERR_INVALID_ARG;
+    if (ntri > CRG_NOALLOC_MAX_TRIS) return CRG_ERR_INVALID_ARG;
+    const uint32_t n = ntri;
+    const uint32_t node_bytes = ((24 + 7 * o.width) + 15) / 16 * 16;
+    const uint32_t nint = n >= 2 ? n - 1 : 1;
+    if (n > 0 && (!d_verts || !d_wide || !d_tris || !d_order)) return CRG_ERR_INVALID_ARG;
+    if (n > 0 && wide_bytes < (size_t)node_bytes * nint) return CRG_ERR_INVALID_ARG;
+    if (info) {
+        *info = crg_bvh_info{};
+        info->ntri = n;
+        info->width = o.width;
+        info->node_bytes = node_bytes;
+        info->n_bvh2_nodes = n >= 2 ? n - 1 : 0;
+        info->n_tri_slots = n;
+    }
+    if (n == 0) return CRG_OK;
+    unsigned char *base = nullptr;
+    if (noalloc_scratch(&base) != CRG_OK) return CRG_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *cur_p = base;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = cur_p;
+        cur_p += bytes;
+        return p;
+    };
+    float4 *tbox = (float4 *)take(kNaTbox);
+    float4 *nbox = (float4 *)take(kNaNbox);
+    uint32_t *cb = (uint32_t *)take(kNaCb);
+    uint32_t *k0 = (uint32_t *)take(kNaKey), *v0 = (uint32_t *)take(kNaKey);
+    uint32_t *k1 = (uint32_t *)take(kNaKey), *v1 = (uint32_t *)take(kNaKey);
+    uint32_t *hist = (uint32_t *)take(kNaHist);
+    uint32_t *parent = (uint32_t *)take(kNaU32N), *leaf_parent = (uint32_t *)take(kNaU32N);
+    uint32_t *count = (uint32_t *)take(kNaU32N), *visits = (uint32_t *)take(kNaU32N);
+    float *cost = (float *)take(kNaU32N);
+    uint32_t *lvl0 = (uint32_t *)take(kNaU32N1), *lvl1 = (uint32_t *)take(kNaU32N1);
+    uint32_t *ents = (uint32_t *)take(kNaEnts);
+    uint32_t *nent = (uint32_t *)take(kNaU32N1), *ic = (uint32_t *)take(kNaU32N1), *tc = (uint32_t *)take(kNaU32N1);
+    uint32_t *totals = (uint32_t *)take(kNaTotals);
+
+#define NA_CHECK(call)                                                                                                 \
+    do {                                                                                                               \
+        if ((call) != cudaSuccess) {                                                                                   \
+            (void)cudaGetLastError();                                                                                  \
+            return CRG_ERR_CUDA;                                                                                       \
+        }                                                                                                              \
+    } while (0)
+    // state that must start at zero / at the identity of min/max
+    NA_CHECK(cudaMemsetAsync(cb, 0xFF, 3 * sizeof(uint32_t), st));
+    NA_CHECK(cudaMemsetAsync(cb + 3, 0x00, 3 * sizeof(uint32_t), st));
+    const uint32_t T = 256;
+    const uint32_t nblk = (n + kSortTile - 1) / kSortTile;
+    k_bounds<<<grid_for(n, T), T, 0, st>>>(d_verts, n, tbox, cb);
+    k_morton<<<grid_for(n, T), T, 0, st>>>(tbox, n, cb, k0, v0);
+    {
+        uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
+        for (int pass = 0; pass < 4; ++pass) {
+            k_hist<<<nblk, kSortThreads, 0, st>>>(ki, n, pass * 8, hist);
+            k_scan<<<1, 1024, 0, st>>>(hist, 256 * nblk, nullptr);
+            k_scatter<<<nblk, kSortThreads, 0, st>>>(ki, vi, n, pass * 8, hist, ko, vo);
+            std::swap(ki, ko);
+            std::swap(vi, vo);
+        }
+        NA_CHECK(cudaMemcpyAsync(d_order, v0, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    Tree Tr{tbox, d_order, nbox, parent, leaf_parent, count, cost};
+    if (n >= 2) {
+        k_karras<<<grid_for(n - 1, T), T, 0, st>>>(k0, (int)n, nbox, parent, leaf_parent);
+        NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+        k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 0);
+        NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+        k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
+        if (o.treelet) {
+            uint32_t gamma = 7;
+            for (uint32_t round = 0; round < o.treelet_rounds; ++round) {
+                NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+                k_treelet<<<grid_for(n, 128), 128, 0, st>>>(Tr, n, visits, gamma);
+                gamma *= 2;
+            }
+            NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+            k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
+        }
+    } else {
+        k_fill<<<1, 32, 0, st>>>(leaf_parent, 1, NONE);
+    }
+    NA_CHECK(cudaGetLastError());
+    Collapse Cc{Tr, d_verts, o.width, o.leaf_max, node_bytes};
+    k_fill<<<1, 32, 0, st>>>(lvl0, 1, n >= 2 ? 0u : LEAF);
+    uint32_t L = 1, node_start = 0, next_start = 1, tri_start = 0, depth = 0;
+    uint32_t *cur = lvl0, *nxt = lvl1;
+    while (L > 0) {
+        k_collapse_count<<<grid_for(L, 128), 128, 0, st>>>(Cc, cur, L, ents, nent, ic, tc);
+        k_scan<<<1, 1024, 0, st>>>(ic, L, totals);
+        k_scan<<<1, 1024, 0, st>>>(tc, L, totals + 1);
+        k_collapse_emit<<<grid_for(L, 64), 64, 0, st>>>(Cc, cur, L, ents, nent, ic, tc, node_start, next_start, tri_start,
+                                                       (uint8_t *)d_wide, (float4 *)d_tris, nxt);
+        uint32_t h[2];
+        NA_CHECK(cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, st));
+        NA_CHECK(cudaStreamSynchronize(st));
+        NA_CHECK(cudaGetLastError());
+        depth++;
+        node_start = next_start;
+        next_start += h[0];
+        tri_start += h[1];
+        L = h[0];
+        std::swap(cur, nxt);
+        if (next_start > nint + 1) return CRG_ERR_DEVICE;
+    }
+    if (tri_start != n) return CRG_ERR_DEVICE;
+    if (info) {
+        info->n_wide_nodes = next_start;
+        info->depth = depth;
+        if (n >= 2) {
+            float c0 = 0.0f;
+            float4 r[2];
+            NA_CHECK(cudaMemcpyAsync(&c0, cost, sizeof(float), cudaMemcpyDeviceToHost, st));
+            NA_CHECK(cudaMemcpyAsync(r, nbox, sizeof(r), cudaMemcpyDeviceToHost, st));
+            NA_CHECK(cudaStreamSynchronize(st));
+            const float dx = r[1].x - r[0].x, dy = r[1].y - r[0].y, dz = r[1].z - r[0].z;
+            const float ra = 2.0f * ((dx * dy + dy * dz) + dz * dx);
+            info->sah_cost = ra > 0.0f ? c0 / ra : 0.0f;
+        }
+    }
+#undef NA_CHECK
+    return CRG_OK;
+}

@@ -214,6 +214,42 @@ crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info);
 crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t *order, void *wide,
                                   float *tris);
 
+/* ------------------------------------------------------------------ build without allocation */
+
+/* Largest triangle count crg_build_bvh_noalloc accepts. */
+#define CRG_NOALLOC_MAX_TRIS 16384u
+
+/* Builds the same wide BVH as crg_scene_create + crg_scene_build, for callers
+ * that cannot allocate device memory themselves: a host application whose own
+ * pool owns the GPU's memory, or an interactive loop that must not pay the
+ * device-wide synchronisation of cudaMalloc/cudaFree when a model is added.
+ * This entry point calls no cudaMalloc, cudaFree or other allocating routine.
+ * It has no counterpart in the reference.
+ *
+ *   d_verts    : device float[ntri*9], de-indexed triangles
+ *   ntri       : at most CRG_NOALLOC_MAX_TRIS (larger counts return
+ *                CRG_ERR_INVALID_ARG without touching the device)
+ *   opts       : as crg_scene_build (NULL = defaults)
+ *   d_wide     : device buffer of at least node_bytes * max(1, ntri - 1) bytes,
+ *                node_bytes = 80 / 64 / 48 for width 8 / 4 / 2 (wide_bytes
+ *                gives its size)
+ *   d_tris     : device float[ntri*12] (triangle array in wide-leaf order)
+ *   d_order    : device uint32[ntri] (Morton order of the primitives)
+ *   info       : optional; filled like crg_scene_bvh_info
+ *
+ * Scratch (sort keys, tree arrays, collapse levels) lives in one fixed device
+ * array inside the library, about 2.5 MB, which every GPU that loads the
+ * library holds until the process exits.  All calls share it and it keeps the
+ * last call's contents: the call clears what must start at zero, but two calls
+ * whose work overlaps on the GPU (different streams or threads at once) race
+ * on it and must be serialised by the caller.  The first call on each device
+ * looks the array's device address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  The call
+ * synchronises `stream` once per BVH level, as crg_scene_build does. */
+crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri, const crg_build_opts *opts,
+                                 void *d_wide, size_t wide_bytes, float *d_tris, uint32_t *d_order,
+                                 crg_bvh_info *info, crg_stream stream);
+
 /* ------------------------------------------------------------------ queries */
 
 /* Batched closest hit.  Replaces cr::scene::cast_ray -> cr::model::intersect
