@@ -593,7 +593,11 @@ __global__ void k_collapse_emit(Collapse C, const uint32_t *__restrict__ level, 
         uint32_t toff = 0;
         for (int s = 0; s < W; ++s) {
             const int i = slot_child[s];
-            if (i < 0) continue;
+            if (i < 0) {
+                // empty slot: inverted box (lo 255, hi 0) fails every slab test
+                for (int a = 0; a < 3; ++a) put_byte(w, 24 + W + a * W + s, 255u);
+                continue;
+            }
             const uint32_t x = e[i];
             const bool leafslot = (x & LEAF) || count_of_cg(C.T, x) <= C.leaf_max;
             uint32_t meta;

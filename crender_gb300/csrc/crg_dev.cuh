@@ -109,6 +109,7 @@ struct RayPre {
     float ix, iy, iz; // 1 / dir (dir components below 2^-80 clamped)
     float Sx, Sy, Sz;
     float tmin;
+    float okx, oky, okz; // origin permuted to (kx, ky, kz)
     int kx, ky, kz;
     float dx, dy, dz;
 };
@@ -137,24 +138,41 @@ __device__ __forceinline__ RayPre ray_prep(float ox, float oy, float oz, float d
     r.Sx = comp(dx, dy, dz, kx) / dkz;
     r.Sy = comp(dx, dy, dz, ky) / dkz;
     r.Sz = 1.0f / dkz;
+    r.okx = comp(ox, oy, oz, kx);
+    r.oky = comp(ox, oy, oz, ky);
+    r.okz = comp(ox, oy, oz, kz);
     r.tmin = tmin;
     return r;
 }
 
-// Woop, Benthin & Wald 2013 watertight test (bit-identical to the CPU form).
-__device__ __forceinline__ bool watertight(const RayPre &r, float4 a, float4 b, float4 c, float &t, float &u, float &v) {
-    const float Ax_ = a.x - r.ox, Ay_ = a.y - r.oy, Az_ = a.z - r.oz;
-    const float Bx_ = b.x - r.ox, By_ = b.y - r.oy, Bz_ = b.z - r.oz;
-    const float Cx_ = c.x - r.ox, Cy_ = c.y - r.oy, Cz_ = c.z - r.oz;
-    const float Akz = comp(Ax_, Ay_, Az_, r.kz), Bkz = comp(Bx_, By_, Bz_, r.kz), Ckz = comp(Cx_, Cy_, Cz_, r.kz);
-    const float Ax = comp(Ax_, Ay_, Az_, r.kx) - r.Sx * Akz;
-    const float Ay = comp(Ax_, Ay_, Az_, r.ky) - r.Sy * Akz;
-    const float Bx = comp(Bx_, By_, Bz_, r.kx) - r.Sx * Bkz;
-    const float By = comp(Bx_, By_, Bz_, r.ky) - r.Sy * Bkz;
-    const float Cx = comp(Cx_, Cy_, Cz_, r.kx) - r.Sx * Ckz;
-    const float Cy = comp(Cx_, Cy_, Cz_, r.ky) - r.Sy * Ckz;
-    float U = Cx * By - Cy * Bx;
-    float V = Ax * Cy - Ay * Cx;
+// Woop, Benthin & Wald 2013 watertight test.  Paired __fadd2_rn / __fmul2_rn
+// round each lane exactly like the scalar operation, so the result is
+// bit-identical to the CPU form: A[k] - o[k], A[kx] - Sx * A[kz], ...
+// Returns false unless the ray crosses the triangle; t is always computed,
+// u and v only by the caller through bary() after acceptance.
+struct TriHit {
+    float t, V, W, det;
+};
+__device__ __forceinline__ bool watertight(const RayPre &r, float4 a, float4 b, float4 c, TriHit &h) {
+    const float2 nko = make_float2(-r.okx, -r.okx), nyo = make_float2(-r.oky, -r.oky), nzo = make_float2(-r.okz, -r.okz);
+    // permuted, origin-relative coordinates of A and B in pairs, C alone
+    const float2 ABkx = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.kx), comp(b.x, b.y, b.z, r.kx)), nko);
+    const float2 ABky = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.ky), comp(b.x, b.y, b.z, r.ky)), nyo);
+    const float2 ABkz = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.kz), comp(b.x, b.y, b.z, r.kz)), nzo);
+    const float Ckx = comp(c.x, c.y, c.z, r.kx) - r.okx;
+    const float Cky = comp(c.x, c.y, c.z, r.ky) - r.oky;
+    const float Ckz = comp(c.x, c.y, c.z, r.kz) - r.okz;
+    // shear: X - S * Xkz, as X + (-S) * Xkz (identical IEEE result)
+    const float2 ABx = __fadd2_rn(ABkx, __fmul2_rn(make_float2(-r.Sx, -r.Sx), ABkz));
+    const float2 ABy = __fadd2_rn(ABky, __fmul2_rn(make_float2(-r.Sy, -r.Sy), ABkz));
+    const float Cx = Ckx - r.Sx * Ckz;
+    const float Cy = Cky - r.Sy * Ckz;
+    const float Ax = ABx.x, Bx = ABx.y, Ay = ABy.x, By = ABy.y;
+    // U = Cx*By - Cy*Bx, V = Ax*Cy - Ay*Cx (paired), W = Bx*Ay - By*Ax
+    const float2 p1 = __fmul2_rn(make_float2(Cx, Ax), make_float2(By, Cy));
+    const float2 p2 = __fmul2_rn(make_float2(Cy, Ay), make_float2(Bx, Cx));
+    const float2 UV = __fadd2_rn(p1, make_float2(-p2.x, -p2.y));
+    float U = UV.x, V = UV.y;
     float W = Bx * Ay - By * Ax;
     if (U == 0.0f || V == 0.0f || W == 0.0f) {
         U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
@@ -164,13 +182,14 @@ __device__ __forceinline__ bool watertight(const RayPre &r, float4 a, float4 b, 
     if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
     const float det = (U + V) + W;
     if (det == 0.0f) return false;
-    const float Az = r.Sz * Akz;
-    const float Bz = r.Sz * Bkz;
+    const float2 ABz = __fmul2_rn(make_float2(r.Sz, r.Sz), ABkz);
     const float Cz = r.Sz * Ckz;
-    const float T = (U * Az + V * Bz) + W * Cz;
-    t = T / det;
-    u = V / det;
-    v = W / det;
+    const float2 q = __fmul2_rn(make_float2(U, V), ABz);
+    const float T = (q.x + q.y) + W * Cz;
+    h.t = T / det;
+    h.V = V;
+    h.W = W;
+    h.det = det;
     return true;
 }
 
@@ -183,7 +202,8 @@ __device__ __forceinline__ bool accept_hit(float t, uint32_t prim, float tmin, f
 // ------------------------------------------------------------------ wide BVH
 // Node of width W: 24-byte header {float p[3]; u8 e[3]; u8 imask; u32
 // child_base; u32 tri_base}, then meta[W], qlo[3][W], qhi[3][W], padded to a
-// multiple of 16 bytes.  Child box a-axis = p + 2^(e-127) * q.
+// multiple of 16 bytes.  Child box a-axis = p + 2^(e-127) * q.  Empty slots
+// carry the inverted box (qlo 255, qhi 0) and meta 0.
 template <int W> struct NodeLayout {
     static constexpr int BYTES = ((24 + 7 * W) + 15) / 16 * 16;
     static constexpr int WORDS = BYTES / 4;
@@ -194,100 +214,102 @@ template <int W> __device__ __forceinline__ uint32_t nbyte(const uint32_t *w, in
     return (w[b >> 2] >> ((b & 3) * 8)) & 0xFFu;
 }
 
+// Byte k of `word` as an exact float: 2^23 + q assembled by PRMT, minus 2^23.
+__device__ __forceinline__ float2 qpair(uint32_t word, int k) {
+    const float2 biased = make_float2(__uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k)),
+                                      __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | (k + 1))));
+    return __fadd2_rn(biased, make_float2(-8388608.0f, -8388608.0f));
+}
+
 struct TravStats {
     uint32_t nodes, tris;
 };
 
 constexpr int kStack = 64;
 
-// Closest hit (ANY = false) or occlusion (ANY = true) through a W-wide
-// compressed BVH.  Children are visited in the octant order of Ylitie et al.
-// 2017: internal child with code c sets hit bit 24 + (c ^ oct); the highest
-// bit is taken first.  Returns the error flag (stack overflow) in *err.
-template <int W, bool ANY, bool COUNT>
-__device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris,
-                                         const RayPre &r, float tmax, float &best_t, uint32_t &best_prim,
-                                         uint32_t &best_slot, float &best_u, float &best_v, bool &occluded,
-                                         TravStats &st, uint32_t &err) {
+// Per-ray traversal state (resumable).
+struct Trav {
+    uint2 ng; // {child_base, internal hits (traversal order) << 24 | imask}
+    uint2 tg; // {tri_base, pending triangle bits}
+    int sp;
+    float best_t, tmax;
+    uint32_t best_prim, best_slot;
+    float best_V, best_W, best_det;
+    uint32_t oct;
+    bool occluded;
+};
+
+__device__ __forceinline__ void trav_init(Trav &T, const RayPre &r, float tmax) {
+    T.oct = (r.dx < 0.0f ? 4u : 0u) | (r.dy < 0.0f ? 2u : 0u) | (r.dz < 0.0f ? 1u : 0u);
+    T.ng = make_uint2(0u, (1u << (24 + (0u ^ T.oct))) | 1u); // the root as child code 0 of a virtual parent
+    T.tg = make_uint2(0u, 0u);
+    T.sp = 0;
+    T.best_t = tmax;
+    T.tmax = tmax;
+    T.best_prim = 0xFFFFFFFFu;
+    T.best_slot = 0xFFFFFFFFu;
+    T.best_V = T.best_W = 0.0f;
+    T.best_det = 1.0f;
+    T.occluded = false;
+}
+
+// Visits one wide node: returns its {internal group, triangle group}.
+template <int W>
+__device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint32_t child, const RayPre &r, uint32_t oct,
+                                           float tfar, uint2 &ng, uint2 &tg) {
     using L = NodeLayout<W>;
-    const uint32_t oct = (r.dx < 0.0f ? 4u : 0u) | (r.dy < 0.0f ? 2u : 0u) | (r.dz < 0.0f ? 1u : 0u);
-    best_t = tmax;
-    best_prim = 0xFFFFFFFFu;
-    best_slot = 0xFFFFFFFFu;
-    occluded = false;
-    uint2 stack[kStack];
-    int sp = 0;
-    // current node group {child_base, hits << 24 | imask}; the root is the
-    // single internal child (code 0) of a virtual parent.
-    uint2 ng = make_uint2(0u, (1u << (24 + (0u ^ oct))) | 1u);
-    uint2 tg = make_uint2(0u, 0u);
-    for (;;) {
-        // triangles of the current group
-        while (tg.y != 0u) {
-            const int i = __ffs(tg.y) - 1;
-            tg.y &= tg.y - 1u;
-            const uint32_t slot = tg.x + (uint32_t)i;
-            const float4 a = __ldg(&tris[slot * 3 + 0]);
-            const float4 b = __ldg(&tris[slot * 3 + 1]);
-            const float4 c = __ldg(&tris[slot * 3 + 2]);
-            const uint32_t prim = __float_as_uint(a.w);
-            if (COUNT) st.tris++;
-            float t, u, v;
-            if (!watertight(r, a, b, c, t, u, v)) continue;
-            if (ANY) {
-                if (t > r.tmin && t < tmax) { occluded = true; return; }
-                continue;
-            }
-            if (accept_hit(t, prim, r.tmin, best_t, best_prim)) {
-                best_t = t;
-                best_prim = prim;
-                best_slot = slot;
-                best_u = u;
-                best_v = v;
-            }
-        }
-        // next internal child
-        if ((ng.y >> 24) == 0u) {
-            if (sp == 0) break;
-            ng = stack[--sp];
-        }
-        const uint32_t hb = ng.y >> 24;
-        const uint32_t pos = 31u - __clz(hb);
-        const uint32_t code = pos ^ oct;
-        ng.y &= ~(1u << (24 + pos));
-        const uint32_t child = ng.x + __popc(ng.y & ((1u << code) - 1u) & 0xFFu);
-        if ((ng.y >> 24) != 0u) {
-            if (sp < kStack) stack[sp++] = ng;
-            else err = 1u;
-        }
-        // load and decode the node
-        uint32_t w[L::WORDS];
-        const uint4 *np = nodes + (size_t)child * L::VEC;
+    uint32_t w[L::WORDS];
+    const uint4 *np = nodes + (size_t)child * L::VEC;
 #pragma unroll
-        for (int k = 0; k < L::VEC; ++k) {
-            const uint4 q = __ldg(np + k);
-            w[4 * k + 0] = q.x;
-            w[4 * k + 1] = q.y;
-            w[4 * k + 2] = q.z;
-            w[4 * k + 3] = q.w;
+    for (int k = 0; k < L::VEC; ++k) {
+        const uint4 q = __ldg(np + k);
+        w[4 * k + 0] = q.x;
+        w[4 * k + 1] = q.y;
+        w[4 * k + 2] = q.z;
+        w[4 * k + 3] = q.w;
+    }
+    const float px = __uint_as_float(w[0]), py = __uint_as_float(w[1]), pz = __uint_as_float(w[2]);
+    const uint32_t eb = w[3];
+    const float sx = __uint_as_float((eb & 0xFFu) << 23) * r.ix;
+    const float sy = __uint_as_float(((eb >> 8) & 0xFFu) << 23) * r.iy;
+    const float sz = __uint_as_float(((eb >> 16) & 0xFFu) << 23) * r.iz;
+    const float ox = (px - r.ox) * r.ix;
+    const float oy = (py - r.oy) * r.iy;
+    const float oz = (pz - r.oz) * r.iz;
+    const uint32_t imask = eb >> 24;
+    uint32_t bits = 0u;
+    if constexpr (W == 8 || W == 4) {
+        // word-aligned quantized planes: pick near/far words once per axis
+        constexpr int QW = W / 4; // words per axis row
+        constexpr int LO = (24 + W) / 4, HI = (24 + 4 * W) / 4, ME = 24 / 4;
+        const bool nxs = r.ix < 0.0f, nys = r.iy < 0.0f, nzs = r.iz < 0.0f;
+        const float2 sx2 = make_float2(sx, sx), sy2 = make_float2(sy, sy), sz2 = make_float2(sz, sz);
+        const float2 ox2 = make_float2(ox, ox), oy2 = make_float2(oy, oy), oz2 = make_float2(oz, oz);
+#pragma unroll
+        for (int p = 0; p < W / 2; ++p) {
+            const int wi = (2 * p) >> 2, bo = (2 * p) & 3;
+            const uint32_t lx = w[LO + 0 * QW + wi], hx = w[HI + 0 * QW + wi];
+            const uint32_t ly = w[LO + 1 * QW + wi], hy = w[HI + 1 * QW + wi];
+            const uint32_t lz = w[LO + 2 * QW + wi], hz = w[HI + 2 * QW + wi];
+            const float2 txn = __ffma2_rn(qpair(nxs ? hx : lx, bo), sx2, ox2);
+            const float2 txf = __ffma2_rn(qpair(nxs ? lx : hx, bo), sx2, ox2);
+            const float2 tyn = __ffma2_rn(qpair(nys ? hy : ly, bo), sy2, oy2);
+            const float2 tyf = __ffma2_rn(qpair(nys ? ly : hy, bo), sy2, oy2);
+            const float2 tzn = __ffma2_rn(qpair(nzs ? hz : lz, bo), sz2, oz2);
+            const float2 tzf = __ffma2_rn(qpair(nzs ? lz : hz, bo), sz2, oz2);
+            const uint32_t mw = w[ME + wi];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float tn = fmaxf(fmaxf(h ? txn.y : txn.x, h ? tyn.y : tyn.x), fmaxf(h ? tzn.y : tzn.x, r.tmin));
+                const float tf = fminf(fminf(h ? txf.y : txf.x, h ? tyf.y : tyf.x), fminf(h ? tzf.y : tzf.x, tfar));
+                const uint32_t meta = (mw >> (8 * (bo + h))) & 0xFFu;
+                if (tn <= tf * 1.00000095f) bits |= (meta >> 5) << (meta & 31u);
+            }
         }
-        if (COUNT) st.nodes++;
-        const float px = __uint_as_float(w[0]), py = __uint_as_float(w[1]), pz = __uint_as_float(w[2]);
-        const uint32_t eb = w[3];
-        const float sx = __uint_as_float((eb & 0xFFu) << 23) * r.ix;
-        const float sy = __uint_as_float(((eb >> 8) & 0xFFu) << 23) * r.iy;
-        const float sz = __uint_as_float(((eb >> 16) & 0xFFu) << 23) * r.iz;
-        const float ox = (px - r.ox) * r.ix;
-        const float oy = (py - r.oy) * r.iy;
-        const float oz = (pz - r.oz) * r.iz;
-        const uint32_t imask = eb >> 24;
-        const uint32_t cbase = w[4], tbase = w[5];
-        const float tfar_lim = best_t;
-        uint32_t hit_int = 0u, hit_tri = 0u;
+    } else {
 #pragma unroll
         for (int s = 0; s < W; ++s) {
             const uint32_t meta = nbyte<W>(w, 24 + s);
-            if (meta == 0u) continue;
             const float qlx = (float)nbyte<W>(w, 24 + W + 0 * W + s);
             const float qly = (float)nbyte<W>(w, 24 + W + 1 * W + s);
             const float qlz = (float)nbyte<W>(w, 24 + W + 2 * W + s);
@@ -301,15 +323,91 @@ __device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const 
             const float tz0 = __fmaf_rn(r.iz >= 0.0f ? qlz : qhz, sz, oz);
             const float tz1 = __fmaf_rn(r.iz >= 0.0f ? qhz : qlz, sz, oz);
             const float tn = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, r.tmin));
-            const float tf = fminf(fminf(tx1, ty1), fminf(tz1, tfar_lim));
-            if (!(tn <= tf * 1.00000095f)) continue;
-            const uint32_t lo5 = meta & 31u;
-            if (lo5 >= 24u) hit_int |= 1u << ((lo5 - 24u) ^ oct);
-            else hit_tri |= (meta >> 5) << lo5;
+            const float tf = fminf(fminf(tx1, ty1), fminf(tz1, tfar));
+            if (tn <= tf * 1.00000095f) bits |= (meta >> 5) << (meta & 31u);
         }
-        ng = make_uint2(cbase, (hit_int << 24) | imask);
-        tg = make_uint2(tbase, hit_tri);
     }
+    // internal hits by octant code -> traversal order (bit position code ^ oct)
+    uint32_t m = bits >> 24;
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    ng = make_uint2(w[4], (m << 24) | imask);
+    tg = make_uint2(w[5], bits & 0x00FFFFFFu);
+}
+
+// Runs up to `iters` traversal iterations (each: the pending triangle group,
+// then one node).  Returns true when the ray is finished.  Children are
+// visited in the octant order of Ylitie et al. 2017: the highest set hit bit
+// (position code ^ oct) first.  A full stack raises *err instead of trapping.
+template <int W, bool ANY, bool COUNT>
+__device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const uint4 *__restrict__ nodes,
+                                          const float4 *__restrict__ tris, const RayPre &r, int iters, TravStats &st,
+                                          uint32_t &err) {
+    for (int it = 0; it < iters; ++it) {
+        while (T.tg.y != 0u) {
+            const int i = __ffs(T.tg.y) - 1;
+            T.tg.y &= T.tg.y - 1u;
+            const uint32_t slot = T.tg.x + (uint32_t)i;
+            const float4 a = __ldg(&tris[slot * 3 + 0]);
+            const float4 b = __ldg(&tris[slot * 3 + 1]);
+            const float4 c = __ldg(&tris[slot * 3 + 2]);
+            if (COUNT) st.tris++;
+            TriHit h;
+            if (!watertight(r, a, b, c, h)) continue;
+            if (ANY) {
+                if (h.t > r.tmin && h.t < T.tmax) {
+                    T.occluded = true;
+                    return true;
+                }
+                continue;
+            }
+            const uint32_t prim = __float_as_uint(a.w);
+            if (accept_hit(h.t, prim, r.tmin, T.best_t, T.best_prim)) {
+                T.best_t = h.t;
+                T.best_prim = prim;
+                T.best_slot = slot;
+                T.best_V = h.V;
+                T.best_W = h.W;
+                T.best_det = h.det;
+            }
+        }
+        if ((T.ng.y >> 24) == 0u) {
+            if (T.sp == 0) return true;
+            T.ng = stack[--T.sp];
+        }
+        const uint32_t hb = T.ng.y >> 24;
+        const uint32_t pos = 31u - __clz(hb);
+        const uint32_t code = pos ^ T.oct;
+        T.ng.y &= ~(1u << (24 + pos));
+        const uint32_t child = T.ng.x + __popc(T.ng.y & ((1u << code) - 1u) & 0xFFu);
+        if ((T.ng.y >> 24) != 0u) {
+            if (T.sp < kStack) stack[T.sp++] = T.ng;
+            else err = 1u;
+        }
+        if (COUNT) st.nodes++;
+        visit_node<W>(nodes, child, r, T.oct, T.best_t, T.ng, T.tg);
+    }
+    return false;
+}
+
+// Closest hit (ANY = false) or occlusion (ANY = true) of one ray, to completion.
+template <int W, bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris,
+                                         const RayPre &r, float tmax, float &best_t, uint32_t &best_prim,
+                                         uint32_t &best_slot, float &best_u, float &best_v, bool &occluded,
+                                         TravStats &st, uint32_t &err) {
+    Trav T;
+    uint2 stack[kStack];
+    trav_init(T, r, tmax);
+    while (!trav_step<W, ANY, COUNT>(T, stack, nodes, tris, r, 1 << 30, st, err)) {
+    }
+    best_t = T.best_t;
+    best_prim = T.best_prim;
+    best_slot = T.best_slot;
+    best_u = T.best_V / T.best_det;
+    best_v = T.best_W / T.best_det;
+    occluded = T.occluded;
 }
 
 } // namespace crg

@@ -18,7 +18,8 @@
  *   7. greedy collapse to a W-wide BVH (largest-area child expanded first),
  *      child slots assigned to the 8 octant directions as in Ylitie, Karras &
  *      Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed
- *      Wide BVHs", HPG 2017, with 8-bit quantized child boxes.
+ *      Wide BVHs", HPG 2017, with 8-bit quantized child boxes (empty slots
+ *      carry the inverted box lo = 255, hi = 0, which no ray can hit).
  * This replaces what rtcCommitScene does for CRender (src/objects/model.cpp:52-97).
  *
  * Queries use the binary tree with a conservative slab test (tmax scaled by
@@ -416,7 +417,11 @@ void collapse(orc_bvh &B) {
             nd[15] = imask;
             for (int s = 0; s < (int)W; ++s) {
                 const int i = slot_child[s];
-                if (i < 0) continue;
+                if (i < 0) {
+                    /* empty slot: inverted box (lo 255, hi 0) fails every slab test */
+                    for (int a = 0; a < 3; ++a) nd[24 + W + a * W + s] = 255;
+                    continue;
+                }
                 const uint32_t x = e[i];
                 const Box &cb = B.box_of(x);
                 const bool leafslot = (x & LEAF) || B.count_of(x) <= leaf_max;

@@ -36,6 +36,12 @@ def slot_box(d, k, s):
     return lo, hi
 
 
+def empty_slots_inverted(d, W):
+    """Empty slots (meta 0) must carry qlo = 255, qhi = 0 on every axis."""
+    empty = d["meta"] == 0
+    return bool((d["qlo"].transpose(0, 2, 1)[empty] == 255).all() and (d["qhi"].transpose(0, 2, 1)[empty] == 0).all())
+
+
 def children(d, k, W):
     """[(slot, kind, index, count)] kind 'node' (index = child node) or 'tris' (index = first slot)."""
     out = []
@@ -63,6 +69,7 @@ def validate(wide: np.ndarray, tris: np.ndarray, W: int, ntri: int, verts: np.nd
         return 0
     d = decode(wide, W)
     n = d["n"]
+    assert empty_slots_inverted(d, W), "an empty slot does not carry the inverted box"
     seen_nodes = np.zeros(n, np.int32)
     seen_tris = np.zeros(ntri, np.int32)
     seen_nodes[0] = 1
