@@ -145,34 +145,29 @@ __device__ __forceinline__ RayPre ray_prep(float ox, float oy, float oz, float d
     return r;
 }
 
-// Woop, Benthin & Wald 2013 watertight test.  Paired __fadd2_rn / __fmul2_rn
-// round each lane exactly like the scalar operation, so the result is
-// bit-identical to the CPU form: A[k] - o[k], A[kx] - Sx * A[kz], ...
-// Returns false unless the ray crosses the triangle; t is always computed,
-// u and v only by the caller through bary() after acceptance.
+// Woop, Benthin & Wald 2013 watertight test, bit-identical to the CPU form
+// (scalar operations only: paired FP32 multiplies and adds may be fused into
+// an FMA by the compiler, which would change the rounding).  Returns false
+// unless the ray crosses the triangle; fills t and the scaled barycentrics
+// (V, W, det) from which u = V / det and v = W / det are formed on acceptance.
 struct TriHit {
     float t, V, W, det;
 };
 __device__ __forceinline__ bool watertight(const RayPre &r, float4 a, float4 b, float4 c, TriHit &h) {
-    const float2 nko = make_float2(-r.okx, -r.okx), nyo = make_float2(-r.oky, -r.oky), nzo = make_float2(-r.okz, -r.okz);
-    // permuted, origin-relative coordinates of A and B in pairs, C alone
-    const float2 ABkx = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.kx), comp(b.x, b.y, b.z, r.kx)), nko);
-    const float2 ABky = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.ky), comp(b.x, b.y, b.z, r.ky)), nyo);
-    const float2 ABkz = __fadd2_rn(make_float2(comp(a.x, a.y, a.z, r.kz), comp(b.x, b.y, b.z, r.kz)), nzo);
-    const float Ckx = comp(c.x, c.y, c.z, r.kx) - r.okx;
-    const float Cky = comp(c.x, c.y, c.z, r.ky) - r.oky;
+    const float Akx = comp(a.x, a.y, a.z, r.kx) - r.okx, Aky = comp(a.x, a.y, a.z, r.ky) - r.oky;
+    const float Akz = comp(a.x, a.y, a.z, r.kz) - r.okz;
+    const float Bkx = comp(b.x, b.y, b.z, r.kx) - r.okx, Bky = comp(b.x, b.y, b.z, r.ky) - r.oky;
+    const float Bkz = comp(b.x, b.y, b.z, r.kz) - r.okz;
+    const float Ckx = comp(c.x, c.y, c.z, r.kx) - r.okx, Cky = comp(c.x, c.y, c.z, r.ky) - r.oky;
     const float Ckz = comp(c.x, c.y, c.z, r.kz) - r.okz;
-    // shear: X - S * Xkz, as X + (-S) * Xkz (identical IEEE result)
-    const float2 ABx = __fadd2_rn(ABkx, __fmul2_rn(make_float2(-r.Sx, -r.Sx), ABkz));
-    const float2 ABy = __fadd2_rn(ABky, __fmul2_rn(make_float2(-r.Sy, -r.Sy), ABkz));
+    const float Ax = Akx - r.Sx * Akz;
+    const float Ay = Aky - r.Sy * Akz;
+    const float Bx = Bkx - r.Sx * Bkz;
+    const float By = Bky - r.Sy * Bkz;
     const float Cx = Ckx - r.Sx * Ckz;
     const float Cy = Cky - r.Sy * Ckz;
-    const float Ax = ABx.x, Bx = ABx.y, Ay = ABy.x, By = ABy.y;
-    // U = Cx*By - Cy*Bx, V = Ax*Cy - Ay*Cx (paired), W = Bx*Ay - By*Ax
-    const float2 p1 = __fmul2_rn(make_float2(Cx, Ax), make_float2(By, Cy));
-    const float2 p2 = __fmul2_rn(make_float2(Cy, Ay), make_float2(Bx, Cx));
-    const float2 UV = __fadd2_rn(p1, make_float2(-p2.x, -p2.y));
-    float U = UV.x, V = UV.y;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
     if (U == 0.0f || V == 0.0f || W == 0.0f) {
         U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
@@ -182,10 +177,10 @@ __device__ __forceinline__ bool watertight(const RayPre &r, float4 a, float4 b, 
     if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
     const float det = (U + V) + W;
     if (det == 0.0f) return false;
-    const float2 ABz = __fmul2_rn(make_float2(r.Sz, r.Sz), ABkz);
+    const float Az = r.Sz * Akz;
+    const float Bz = r.Sz * Bkz;
     const float Cz = r.Sz * Ckz;
-    const float2 q = __fmul2_rn(make_float2(U, V), ABz);
-    const float T = (q.x + q.y) + W * Cz;
+    const float T = (U * Az + V * Bz) + W * Cz;
     h.t = T / det;
     h.V = V;
     h.W = W;
