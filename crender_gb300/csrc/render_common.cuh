@@ -1,0 +1,520 @@
+// render_common.cuh — per-bounce path shading shared by the megakernel
+// (render.cu) and the wavefront form (wavefront.cu), so both evaluate the
+// same operations in the same order and produce bit-identical images.
+//
+// FAITHFUL follows process_hit / _sample_pixel (CRender
+// src/render/renderer.cpp:21-102, 258-384); EXTENDED adds emissive-triangle
+// NEE with power-heuristic MIS, GGX (VNDF sampling, Heitz 2018), a Fresnel
+// dielectric and Russian roulette.  Random dimension groups: 0 = pixel
+// jitter, 1 + 2i = BSDF at segment i, 2 + 2i = light sample at segment i.
+#pragma once
+#include <cmath>
+
+#include "crg_dev.cuh"
+#include "crg_internal.h"
+
+namespace crg {
+namespace rc {
+
+struct SceneDev {
+    const uint4 *nodes;
+    const float4 *tris;
+    const uint32_t *mat_idx;
+    const crg_material *mats;
+    const uint32_t *light_prim;
+    const float *light_cdf;
+    const float *light_pdf;
+    const float *mat_light_pdf;
+    const float4 *sky;
+    const float *verts;
+    uint32_t nlights, ntri;
+    uint32_t sky_w, sky_h;
+    float sky_rot_u, sky_rot_v;
+    int sun_on;
+    float sun_frame[9]; // t, n, b
+    float sun_cos, sun_pdf;
+    float sun_neg_dir[3];
+    float sun_rad[3];
+    uint32_t *err;
+    unsigned long long *counters;
+};
+
+struct FilmDev {
+    float *sum;
+    double *sum64, *sumsq64;
+    float *aov_albedo, *aov_normal, *aov_depth;
+    uint32_t width, height;
+};
+
+struct Hit {
+    float t, u, v;
+    uint32_t prim, slot;
+};
+
+struct PathCtx;
+
+template <int W, bool CNT>
+__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C);
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C);
+
+__device__ __forceinline__ void slot_verts(const SceneDev &S, uint32_t slot, v3 &a, v3 &b, v3 &c) {
+    const float4 x = __ldg(&S.tris[slot * 3 + 0]);
+    const float4 y = __ldg(&S.tris[slot * 3 + 1]);
+    const float4 z = __ldg(&S.tris[slot * 3 + 2]);
+    a = mk(x.x, x.y, x.z);
+    b = mk(y.x, y.y, y.z);
+    c = mk(z.x, z.y, z.z);
+}
+
+__device__ __forceinline__ void prim_verts(const SceneDev &S, uint32_t prim, v3 &a, v3 &b, v3 &c) {
+    const float *v = S.verts + (size_t)prim * 9;
+    a = mk(__ldg(v + 0), __ldg(v + 1), __ldg(v + 2));
+    b = mk(__ldg(v + 3), __ldg(v + 4), __ldg(v + 5));
+    c = mk(__ldg(v + 6), __ldg(v + 7), __ldg(v + 8));
+}
+
+// image::get_uv (src/objects/image.h:104-109)
+__device__ __forceinline__ uint32_t texel_index(float u, uint32_t n) {
+    const float f = u * (float)n;
+    unsigned long long i = 0;
+    if (f >= 0.0f) i = f < 4.6e18f ? (unsigned long long)f : 0ull;
+    return (uint32_t)(i % n);
+}
+
+__device__ __forceinline__ v3 sample_sky(const SceneDev &S, v3 d) {
+    if (S.sky_w == 0) return mk(0, 0, 0);
+    const float dy = clampf(d.y, -1.0f, 1.0f);
+    const float u = 0.5f + atan2f(d.z, d.x) * kInvTau;
+    const float v = 0.5f - asinf(dy) * kInvPi;
+    const uint32_t x = texel_index(u + S.sky_rot_u, S.sky_w);
+    const uint32_t y = texel_index(v + S.sky_rot_v, S.sky_h);
+    const float4 t = __ldg(&S.sky[x + (size_t)y * S.sky_w]);
+    return mk(t.x, t.y, t.z);
+}
+
+__device__ __forceinline__ v3 sphere(float u1, float u2) {
+    const float cos_t = 2.0f * u1 - 1.0f;
+    const float sin_t = sqrtf(1.0f - cos_t * cos_t);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    return mk(sin_t * cp, cos_t, sin_t * sp);
+}
+
+struct Aov {
+    v3 albedo, normal;
+    float depth;
+};
+
+struct PathCtx {
+    uint32_t pix, sample, seed;
+    uint32_t segments, shadow;
+    uint32_t err;
+    unsigned long long nodes, tris; // traversal work, counted only in the instrumented variant
+};
+
+template <int W, bool CNT>
+__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C) {
+    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+    bool occ;
+    TravStats st{0, 0};
+    traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
+    if (CNT) {
+        C.nodes += st.nodes;
+        C.tris += st.tris;
+    }
+    return h.prim != 0xFFFFFFFFu;
+}
+
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C) {
+    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+    float t, u, v;
+    uint32_t p, sl;
+    bool occ;
+    TravStats st{0, 0};
+    traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
+    if (CNT) {
+        C.nodes += st.nodes;
+        C.tris += st.tris;
+    }
+    return occ;
+}
+
+// ------------------------------------------------------------------ path state
+// One path between bounces.  Shading a bounce (shade_faithful / shade_extended)
+// consumes the closest hit (or miss) of the current segment, updates the
+// state, and may ask for one shadow test (NeeReq) whose contribution the
+// caller adds to L if the test passes, before the next segment.
+struct PathState {
+    v3 o, d, T, L;
+    float prev_pdf;
+    uint32_t prev_delta;
+};
+struct NeeReq {
+    v3 o, d, c;
+    float tmax;
+    uint32_t kind; // 0 none, 1 emitter (any hit below tmax), 2 sun (closest hit with alpha pass-through)
+};
+
+__device__ __forceinline__ void path_start(PathState &ps, v3 o, v3 d) {
+    ps.o = o;
+    ps.d = d;
+    ps.T = mk(1, 1, 1);
+    ps.L = mk(0, 0, 0);
+    ps.prev_pdf = 0.0f;
+    ps.prev_delta = 1u;
+}
+
+// ------------------------------------------------------------------ faithful
+// process_hit + the bounce body of _sample_pixel (renderer.cpp:21-102, 272-355).
+__device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set, const PathCtx &C, uint32_t i, PathState &ps,
+                               bool found, const Hit &h, Aov &aov, NeeReq &nr) {
+    nr.kind = 0;
+    if (!found) {
+        const v3 env = sample_sky(S, ps.d);
+        if (i == 0) aov.albedo = env;
+        ps.L = add(ps.L, mulv(ps.T, env));
+        return false;
+    }
+    const v3 p = add(ps.o, mul(ps.d, h.t));
+    v3 a, b, c;
+    slot_verts(S, h.slot, a, b, c);
+    const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+    const crg_material &m = S.mats[__ldg(&S.mat_idx[h.prim])];
+    const float c0 = m.colour[0], c1 = m.colour[1], c2 = m.colour[2], c3 = m.colour[3];
+    if (c3 == 0.0f) {
+        ps.o = add(p, mul(ps.d, 0.1f));
+        return true;
+    }
+    v3 albedo = mk(c0, c1, c2);
+    const f4 g = rand4(C.pix, C.sample, 1 + 2 * i, C.seed);
+    v3 no, nd;
+    const uint32_t shade = m.shade_type;
+    if (shade == CRG_SHADE_GLASS) {
+        const v3 reflected = reflect(ps.d, Ng);
+        v3 out_n = Ng;
+        float eta = 1.0f / m.ior;
+        if (dot(ps.d, Ng) > 0.0f) {
+            out_n = neg(Ng);
+            eta = m.ior;
+        }
+        const v3 uv = normalize(ps.d);
+        const float dt = dot(uv, out_n);
+        const float disc = 1.0f - (eta * eta) * (1.0f - dt * dt);
+        no = add(p, mul(out_n, -0.0001f));
+        if (disc > 0.0f) nd = sub(mul(sub(uv, mul(out_n, dt)), eta), mul(out_n, sqrtf(disc)));
+        else nd = reflected;
+    } else if (shade == CRG_SHADE_METAL) {
+        no = add(p, mul(Ng, 0.0001f));
+        nd = reflect(ps.d, Ng);
+        albedo = mul(albedo, m.reflectiveness);
+    } else {
+        const v3 hc = add(Ng, sphere(g.x, g.y));
+        const float l2 = dot(hc, hc);
+        nd = l2 > 0.0f ? mul(hc, 1.0f / sqrtf(l2)) : Ng;
+        no = add(p, mul(Ng, 0.0001f));
+    }
+    if (i == 0) {
+        aov.albedo = albedo;
+        aov.normal = Ng;
+        aov.depth = h.t;
+    }
+    ps.T = mulv(ps.T, albedo);
+    ps.L = add(ps.L, mul(ps.T, m.emission));
+    if (S.sun_on) {
+        // renderer.cpp:315-354; the shadow ray is a closest-hit cast that steps
+        // through alpha surfaces; the contribution is added when it escapes
+        const v3 so = add(p, mul(Ng, 0.001f));
+        const f4 g2 = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
+        float sp, cp;
+        sincos2pi(g2.x, &sp, &cp);
+        const float ct = 1.0f - g2.y * (1.0f - S.sun_cos);
+        const float st = sqrtf(1.0f - ct * ct);
+        const v3 lv = mk(cp * st, ct, sp * st);
+        const float *F = S.sun_frame;
+        const v3 sd = mk((F[0] * lv.x + F[3] * lv.y) + F[6] * lv.z, (F[1] * lv.x + F[4] * lv.y) + F[7] * lv.z,
+                         (F[2] * lv.x + F[5] * lv.y) + F[8] * lv.z);
+        const float cosine = clampf(dot(Ng, sd), 0.0f, 1.0f);
+        const v3 ms = mk(S.sun_neg_dir[0], S.sun_neg_dir[1], S.sun_neg_dir[2]);
+        v3 sky = mk(0, 0, 0);
+        if (dot(sd, ms) > S.sun_cos) sky = mk(S.sun_rad[0], S.sun_rad[1], S.sun_rad[2]);
+        const v3 tc = mulv(ps.T, mk(c0, c1, c2));
+        nr.kind = 2;
+        nr.o = so;
+        nr.d = sd;
+        nr.tmax = INFINITY;
+        nr.c = mk(((tc.x * cosine) * sky.x) / S.sun_pdf, ((tc.y * cosine) * sky.y) / S.sun_pdf,
+                  ((tc.z * cosine) * sky.z) / S.sun_pdf);
+    }
+    ps.o = no;
+    ps.d = nd;
+    if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
+        const float q = mn(mx(mx(ps.T.x, ps.T.y), ps.T.z), 0.95f);
+        if (g.w >= q) return false;
+        ps.T = mk(ps.T.x / q, ps.T.y / q, ps.T.z / q);
+    }
+    return true;
+}
+
+// ------------------------------------------------------------------ extended
+__device__ __forceinline__ float ggx_D(float nh, float a) {
+    const float a2 = a * a;
+    const float dd = (nh * a2 - nh) * nh + 1.0f;
+    return a2 / ((dd * dd) * kPi);
+}
+__device__ __forceinline__ float ggx_lambda(v3 w, float a) {
+    const float s2 = w.x * w.x + w.y * w.y;
+    const float z2 = w.z * w.z;
+    return (sqrtf(1.0f + ((a * a) * s2) / z2) - 1.0f) * 0.5f;
+}
+__device__ __forceinline__ v3 schlick(v3 f0, float c) {
+    const float m = 1.0f - clampf(c, 0.0f, 1.0f);
+    const float m2 = m * m;
+    const float m5 = (m2 * m2) * m;
+    return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+__device__ __forceinline__ v3 sample_vndf(v3 ve, float a, float u1, float u2) {
+    const v3 vh = normalize(mk(a * ve.x, a * ve.y, ve.z));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    const v3 t1v = lensq > 0.0f ? mul(mk(-vh.y, vh.x, 0.0f), 1.0f / sqrtf(lensq)) : mk(1, 0, 0);
+    const v3 t2v = cross(vh, t1v);
+    const float r = sqrtf(u1);
+    float sp, cp;
+    sincos2pi(u2, &sp, &cp);
+    const float t1 = r * cp;
+    float t2 = r * sp;
+    const float sw = 0.5f * (1.0f + vh.z);
+    t2 = (1.0f - sw) * sqrtf(1.0f - t1 * t1) + sw * t2;
+    const v3 nh = add(add(mul(t1v, t1), mul(t2v, t2)), mul(vh, sqrtf(mx(0.0f, (1.0f - t1 * t1) - t2 * t2))));
+    return normalize(mk(a * nh.x, a * nh.y, mx(0.0f, nh.z)));
+}
+__device__ __forceinline__ float fresnel_dielectric(float ci, float eta, float &st2_out) {
+    ci = clampf(ci, 0.0f, 1.0f);
+    const float st2 = (eta * eta) * (1.0f - ci * ci);
+    st2_out = st2;
+    if (st2 >= 1.0f) return 1.0f;
+    const float ct = sqrtf(1.0f - st2);
+    const float rs = (eta * ci - ct) / (eta * ci + ct);
+    const float rp = (ci - eta * ct) / (ci + eta * ct);
+    return 0.5f * (rs * rs + rp * rp);
+}
+__device__ __forceinline__ v3 to_local(const onb &F, v3 w) { return mk(dot(w, F.t), dot(w, F.b), dot(w, F.n)); }
+__device__ __forceinline__ v3 from_local(const onb &F, v3 l) { return add(add(mul(F.t, l.x), mul(F.b, l.y)), mul(F.n, l.z)); }
+
+__device__ __forceinline__ uint32_t pick_light(const SceneDev &S, float u) {
+    uint32_t lo = 0, hi = S.nlights - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (u < __ldg(&S.light_cdf[mid])) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Emissive-triangle NEE at p: fills nr (kind 1) with the shadow ray and the
+// contribution it carries if unoccluded; bsdf 0 = Lambert (albedo), 1 = GGX.
+__device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo,
+                            const onb &F, v3 wol, float alpha, NeeReq &nr) {
+    nr.kind = 0;
+    const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
+    const uint32_t j = pick_light(S, g.x);
+    const uint32_t prim = __ldg(&S.light_prim[j]);
+    v3 a, b, c;
+    prim_verts(S, prim, a, b, c);
+    const float su = sqrtf(g.y);
+    const float b0 = 1.0f - su, b1 = su * (1.0f - g.z), b2 = su * g.z;
+    const v3 pl = add(add(mul(a, b0), mul(b, b1)), mul(c, b2));
+    const v3 po = add(p, mul(n, 1e-4f));
+    const v3 w = sub(pl, po);
+    const float d2 = dot(w, w);
+    if (!(d2 > 0.0f)) return;
+    const float dist = sqrtf(d2);
+    const v3 wi = mul(w, 1.0f / dist);
+    const float cos_s = dot(wi, n);
+    if (!(cos_s > 0.0f)) return;
+    const v3 Ngl = normalize(cross(sub(b, a), sub(c, a)));
+    const float cos_l = absf(dot(Ngl, wi));
+    if (!(cos_l > 0.0f)) return;
+    const crg_material &lm = S.mats[__ldg(&S.mat_idx[prim])];
+    const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
+    const float p_light = (__ldg(&S.light_pdf[j]) * d2) / cos_l;
+    v3 f;
+    float p_bsdf, cos_i;
+    if (bsdf == 0) {
+        f = mul(albedo, kInvPi);
+        p_bsdf = cos_s * kInvPi;
+        cos_i = cos_s;
+    } else {
+        const v3 wil = to_local(F, wi);
+        if (!(wil.z > 0.0f)) return;
+        const v3 hv = normalize(add(wol, wil));
+        const float woh = dot(wol, hv);
+        const float D = ggx_D(hv.z, alpha);
+        const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
+        const float G2 = 1.0f / ((1.0f + lo_) + li);
+        const float G1 = 1.0f / (1.0f + lo_);
+        const v3 Fr = schlick(albedo, woh);
+        f = mul(Fr, (D * G2) / ((4.0f * wol.z) * wil.z));
+        p_bsdf = (G1 * D) / (4.0f * wol.z);
+        cos_i = wil.z;
+    }
+    const float w_mis = (p_light * p_light) / (p_light * p_light + p_bsdf * p_bsdf);
+    nr.kind = 1;
+    nr.o = po;
+    nr.d = wi;
+    nr.tmax = dist * 0.999f;
+    nr.c = mul(mulv(mulv(T, f), Le), (cos_i * w_mis) / p_light);
+}
+
+// Extended estimator bounce: MIS-weighted emission, emissive-triangle NEE,
+// Lambert (geometric-normal hemisphere) / GGX VNDF / Fresnel dielectric, RR.
+__device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set, const PathCtx &C, uint32_t i, PathState &ps,
+                               bool found, const Hit &h, Aov &aov, NeeReq &nr) {
+    nr.kind = 0;
+    if (!found) {
+        const v3 env = sample_sky(S, ps.d);
+        if (i == 0) aov.albedo = env;
+        ps.L = add(ps.L, mulv(ps.T, env));
+        return false;
+    }
+    const v3 p = add(ps.o, mul(ps.d, h.t));
+    v3 a, b, c;
+    slot_verts(S, h.slot, a, b, c);
+    const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+    const uint32_t mi = __ldg(&S.mat_idx[h.prim]);
+    const crg_material &m = S.mats[mi];
+    const float c0 = m.colour[0], c1 = m.colour[1], c2 = m.colour[2], c3 = m.colour[3];
+    if (c3 == 0.0f) {
+        ps.o = add(p, mul(ps.d, 0.1f));
+        return true;
+    }
+    const v3 rgb = mk(c0, c1, c2);
+    const float cos_nd = dot(Ng, ps.d);
+    const v3 n = cos_nd < 0.0f ? Ng : neg(Ng);
+    if (i == 0) {
+        aov.albedo = rgb;
+        aov.normal = Ng;
+        aov.depth = h.t;
+    }
+    const float emission = m.emission;
+    if (emission > 0.0f) {
+        const v3 Le = mk(c0 * emission, c1 * emission, c2 * emission);
+        if (ps.prev_delta) {
+            ps.L = add(ps.L, mulv(ps.T, Le));
+        } else {
+            const float cos_l = absf(cos_nd);
+            if (cos_l > 0.0f) {
+                const float pl = (__ldg(&S.mat_light_pdf[mi]) * (h.t * h.t)) / cos_l;
+                const float w = (ps.prev_pdf * ps.prev_pdf) / (ps.prev_pdf * ps.prev_pdf + pl * pl);
+                ps.L = add(ps.L, mul(mulv(ps.T, Le), w));
+            }
+        }
+    }
+    const f4 g = rand4(C.pix, C.sample, 1 + 2 * i, C.seed);
+    const v3 wo = neg(ps.d);
+    const bool have_lights = S.nlights > 0 && i + 1 < set.max_bounces;
+    const uint32_t shade = m.shade_type;
+    if (shade == CRG_SHADE_SMOOTH) {
+        const onb F = build_local(Ng);
+        if (have_lights) nee_prepare(S, C, i, p, Ng, ps.T, 0, rgb, F, mk(0, 0, 0), 0.0f, nr);
+        float sp, cp;
+        sincos2pi(g.y, &sp, &cp);
+        const float r = sqrtf(g.x);
+        const v3 l = mk(r * cp, r * sp, sqrtf(mx(0.0f, 1.0f - g.x)));
+        ps.d = from_local(F, l);
+        ps.o = add(p, mul(Ng, 1e-4f));
+        ps.prev_pdf = l.z * kInvPi;
+        ps.prev_delta = 0u;
+        ps.T = mulv(ps.T, rgb);
+    } else if (shade == CRG_SHADE_METAL) {
+        const v3 f0 = mul(rgb, m.reflectiveness);
+        const float alpha = m.roughness;
+        if (alpha < 1e-4f) {
+            ps.d = reflect(ps.d, n);
+            ps.o = add(p, mul(n, 1e-4f));
+            ps.T = mulv(ps.T, f0);
+            ps.prev_delta = 1u;
+        } else {
+            const onb F = build_local(n);
+            const v3 wol = to_local(F, wo);
+            if (!(wol.z > 0.0f)) return false;
+            if (have_lights) nee_prepare(S, C, i, p, n, ps.T, 1, f0, F, wol, alpha, nr);
+            const v3 hh = sample_vndf(wol, alpha, g.x, g.y);
+            const float woh = dot(wol, hh);
+            const float k2 = 2.0f * woh;
+            const v3 wil = mk(hh.x * k2 - wol.x, hh.y * k2 - wol.y, hh.z * k2 - wol.z);
+            if (!(wil.z > 0.0f)) return false;
+            const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
+            const float G1 = 1.0f / (1.0f + lo_);
+            const float G2 = 1.0f / ((1.0f + lo_) + li);
+            const v3 Fr = schlick(f0, woh);
+            ps.T = mulv(ps.T, mul(Fr, G2 / G1));
+            ps.prev_pdf = (G1 * ggx_D(hh.z, alpha)) / (4.0f * wol.z);
+            ps.prev_delta = 0u;
+            ps.d = from_local(F, wil);
+            ps.o = add(p, mul(n, 1e-4f));
+        }
+    } else {
+        const float eta = cos_nd < 0.0f ? 1.0f / m.ior : m.ior;
+        const float ci = -dot(ps.d, n);
+        float st2;
+        const float Fr = fresnel_dielectric(ci, eta, st2);
+        if (g.z < Fr) {
+            ps.d = reflect(ps.d, n);
+            ps.o = add(p, mul(n, 1e-4f));
+        } else {
+            const float cic = clampf(ci, 0.0f, 1.0f);
+            const float ct = sqrtf(1.0f - st2);
+            ps.d = add(mul(ps.d, eta), mul(n, eta * cic - ct));
+            ps.o = add(p, mul(n, -1e-4f));
+        }
+        ps.T = mulv(ps.T, rgb);
+        ps.prev_delta = 1u;
+    }
+    if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
+        const float q = mn(mx(mx(ps.T.x, ps.T.y), ps.T.z), 0.95f);
+        if (g.w >= q) return false;
+        ps.T = mk(ps.T.x / q, ps.T.y / q, ps.T.z / q);
+    }
+    return true;
+}
+
+// The shadow test a NeeReq asks for: kind 1 = any hit below tmax; kind 2 =
+// closest hits stepping 0.1 past alpha-zero surfaces (renderer.cpp:330-345).
+template <int W, bool CNT>
+__device__ __forceinline__ bool shadow_visible(const SceneDev &S, const NeeReq &nr, PathCtx &C) {
+    if (nr.kind == 1) {
+        C.shadow++;
+        return !occluded<W, CNT>(S, nr.o, nr.d, nr.tmax, C);
+    }
+    v3 so = nr.o;
+    for (;;) {
+        Hit sh;
+        C.shadow++;
+        if (!closest<W, CNT>(S, so, nr.d, INFINITY, sh, C)) return true;
+        if (S.mats[__ldg(&S.mat_idx[sh.prim])].colour[3] != 0.0f) return false;
+        so = add(add(so, mul(nr.d, sh.t)), mul(nr.d, 0.1f));
+    }
+}
+
+// camera::get_ray (camera.cpp:14-39)
+__device__ __forceinline__ void camera_ray(const CamDev &c, float x, float y, float aspect, v3 &o, v3 &d) {
+    if (c.mode == CRG_CAMERA_ORTHOGRAPHIC) {
+        const float u = 2.0f * x - 1.0f;
+        const float v = 2.0f * y - 1.0f;
+        const float su = c.scale * u, sv = c.scale * v;
+        o = mk(((c.R[0] * su + c.R[1] * sv) + c.R[2] * 0.0f) + c.pos[0], ((c.R[3] * su + c.R[4] * sv) + c.R[5] * 0.0f) + c.pos[1],
+               ((c.R[6] * su + c.R[7] * sv) + c.R[8] * 0.0f) + c.pos[2]);
+        d = normalize(mk(c.R[2], c.R[5], c.R[8]));
+        return;
+    }
+    const float u = (2.0f * x - 1.0f) * aspect;
+    const float v = 2.0f * y - 1.0f;
+    o = mk(c.pos[0], c.pos[1], c.pos[2]);
+    d = normalize(mk((c.R[0] * u + c.R[1] * v) + c.R[2] * c.w, (c.R[3] * u + c.R[4] * v) + c.R[5] * c.w,
+                     (c.R[6] * u + c.R[7] * v) + c.R[8] * c.w));
+}
+
+} // namespace rc
+} // namespace crg

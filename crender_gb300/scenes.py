@@ -17,6 +17,7 @@ per-primitive material index, and a crg_material table.
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -151,3 +152,174 @@ def closed_box(albedo=0.5, emission=1.0):
     mats = material_table([{"colour": (albedo, albedo, albedo, 1.0), "emission": emission}])
     camera = dict(position=(0.5, 0.5, 0.3), rotation=(0.0, 0.0, 0.0), fov=60.0)
     return dict(verts=np.ascontiguousarray(verts), mat_idx=np.zeros(12, np.uint32), mats=mats, camera=camera)
+
+
+# ----------------------------------------------------------------------------- displaced scene
+_ICO_V = None
+
+
+def _icosahedron():
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+    return v, f
+
+
+def geodesic_grid(freq: int):
+    """Grid points of a unit geodesic icosphere: each icosahedron face split
+    into a freq x freq triangular grid projected onto the sphere.  Returns
+    (points [20, P, 3] float64, local triangles [freq^2, 3] indices into a
+    face's points)."""
+    v, f = _icosahedron()
+    i, j = np.meshgrid(np.arange(freq + 1), np.arange(freq + 1), indexing="ij")
+    keep = (i + j) <= freq
+    i, j = i[keep], j[keep]
+    lut = -np.ones((freq + 1, freq + 1), np.int64)
+    lut[i, j] = np.arange(i.size)
+    # grid triangles: up (i,j),(i+1,j),(i,j+1); down (i+1,j),(i+1,j+1),(i,j+1)
+    ui, uj = np.meshgrid(np.arange(freq), np.arange(freq), indexing="ij")
+    up = (ui + uj) <= freq - 1
+    dn = (ui + uj) <= freq - 2
+    tri_up = np.stack([lut[ui[up], uj[up]], lut[ui[up] + 1, uj[up]], lut[ui[up], uj[up] + 1]], 1)
+    tri_dn = np.stack([lut[ui[dn] + 1, uj[dn]], lut[ui[dn] + 1, uj[dn] + 1], lut[ui[dn], uj[dn] + 1]], 1)
+    local = np.concatenate([tri_up, tri_dn])
+    pts = np.empty((len(f), i.size, 3))
+    for k, (a, b, c) in enumerate(f):
+        A, B, C = v[a], v[b], v[c]
+        P = A + np.outer(i / freq, B - A) + np.outer(j / freq, C - A)
+        pts[k] = P / np.linalg.norm(P, axis=1, keepdims=True)
+    return pts, local
+
+
+def grid_triangles(pts, local):
+    """De-indexed triangles [20 * len(local), 3, 3] wound away from the origin."""
+    T = pts[:, local].reshape(-1, 3, 3)
+    n = np.cross(T[:, 1] - T[:, 0], T[:, 2] - T[:, 0])
+    flip = np.einsum("ij,ij->i", n, T.mean(axis=1)) < 0
+    T[flip] = T[flip][:, [0, 2, 1]]
+    return T
+
+
+def geodesic_sphere(freq: int):
+    """Unit geodesic icosphere, 20 * freq^2 triangles wound outward, float64 [n, 3, 3]."""
+    return grid_triangles(*geodesic_grid(freq))
+
+
+def _lattice_value(ix, iy, iz, seed):
+    """Hash of integer lattice points to [-1, 1] (splitmix64-style finaliser)."""
+    h = (ix.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) ^ (iy.astype(np.uint64) * np.uint64(0xC2B2AE3D27D4EB4F)) \
+        ^ (iz.astype(np.uint64) * np.uint64(0x165667B19E3779F9)) ^ np.uint64(seed * 0x27D4EB2F165667C5 & 0xFFFFFFFFFFFFFFFF)
+    h ^= h >> np.uint64(30)
+    h *= np.uint64(0xBF58476D1CE4E5B9)
+    h ^= h >> np.uint64(27)
+    h *= np.uint64(0x94D049BB133111EB)
+    h ^= h >> np.uint64(31)
+    return (h >> np.uint64(11)).astype(np.float64) / float(1 << 53) * 2.0 - 1.0
+
+
+def value_noise(p, seed):
+    """Trilinear value noise with smoothstep weights, in [-1, 1]."""
+    with np.errstate(over="ignore"):
+        fl = np.floor(p)
+        f = p - fl
+        w = f * f * (3.0 - 2.0 * f)
+        i0 = fl.astype(np.int64)
+        acc = 0.0
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    val = _lattice_value(i0[:, 0] + dx, i0[:, 1] + dy, i0[:, 2] + dz, seed)
+                    wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                    wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                    wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                    acc = acc + val * wx * wy * wz
+    return acc
+
+
+def fbm(p, octaves=6, seed=7, base=2.0):
+    """Sum of octaves of value noise, gain 1/2, lacunarity 2, normalised to [-1, 1]."""
+    total, norm, amp, freq = 0.0, 0.0, 1.0, base
+    for o in range(octaves):
+        total = total + amp * value_noise(p * freq, seed + 101 * o)
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return total / norm
+
+
+def displaced_scene(freq=458, amplitude=0.05, seed=7, light_freq=8, n_materials=1024):
+    """The displaced-mesh scene: a geodesic icosphere (20 * freq^2 triangles;
+    freq = 458 gives 4,195,280, the icosphere count nearest 4,194,304) displaced
+    radially by fBm (6 octaves, amplitude 0.05, seed 7), on a 2-triangle
+    ground quad; per-triangle materials drawn by seed from a palette (60%
+    Lambert albedo U[0.1, 0.9], 25% GGX metal roughness U[0.05, 0.5], 15%
+    dielectric IOR 1.5); one emissive sphere light (tessellated, centre
+    (2.5, 3.0, -1.5), radius 0.5, radiance 20 x (1, 0.95, 0.9)); constant
+    environment of radiance 1 (a 1x1 skybox)."""
+    cache = _cache_path("displaced", freq, amplitude, seed, light_freq, n_materials)
+    if cache and os.path.exists(cache):
+        with np.load(cache) as z:
+            out = {k: z[k] for k in ("verts", "mat_idx", "mats", "skybox")}
+        out.update(camera=dict(position=(0.0, 0.25, -3.4), rotation=(0.0, 0.0, 0.0), fov=45.0),
+                   width=1920, height=1080, spp=256, max_bounces=16)
+        return out
+    rng = np.random.default_rng(seed)
+    pts, local = geodesic_grid(freq)  # displacement on the unique grid points
+    flat = pts.reshape(-1, 3)
+    flat = flat * (1.0 + amplitude * fbm(flat, 6, seed))[:, None]
+    sphere = grid_triangles(flat.reshape(pts.shape), local).reshape(-1, 9)
+    ground = np.asarray(_quad([(-12, -1.1, -12), (12, -1.1, -12), (12, -1.1, 12), (-12, -1.1, 12)], (0, 1, 0)))
+    L = geodesic_sphere(light_freq).reshape(-1, 3) * 0.5 + np.array([2.5, 3.0, -1.5])
+    light = L.reshape(-1, 9)
+    verts = np.concatenate([sphere, ground, light]).astype(np.float32)
+    # palette: Lambert, GGX metal, glass; then ground and light materials
+    n_l, n_g = int(n_materials * 0.6), int(n_materials * 0.25)
+    n_d = n_materials - n_l - n_g
+    rows = []
+    for _ in range(n_l):
+        rows.append({"colour": tuple(rng.uniform(0.1, 0.9, 3)) + (1.0,)})
+    for _ in range(n_g):
+        rows.append({"shade_type": SHADE_METAL, "roughness": float(rng.uniform(0.05, 0.5)),
+                     "colour": tuple(rng.uniform(0.5, 1.0, 3)) + (1.0,)})
+    for _ in range(n_d):
+        rows.append({"shade_type": SHADE_GLASS, "ior": 1.5, "colour": (1.0, 1.0, 1.0, 1.0)})
+    ground_m = len(rows)
+    rows.append({"colour": (0.5, 0.5, 0.5, 1.0)})
+    light_m = len(rows)
+    rows.append({"colour": (1.0, 0.95, 0.9, 1.0), "emission": 20.0})
+    mats = material_table(rows)
+    ns = sphere.shape[0]
+    u = rng.random(ns)
+    cat = np.where(u < 0.6, 0, np.where(u < 0.85, 1, 2))
+    pick = rng.random(ns)
+    base = np.array([0, n_l, n_l + n_g])
+    size = np.array([n_l, n_g, n_d])
+    mat_idx = np.concatenate([
+        (base[cat] + np.minimum((pick * size[cat]).astype(np.int64), size[cat] - 1)).astype(np.uint32),
+        np.full(2, ground_m, np.uint32),
+        np.full(light.shape[0], light_m, np.uint32),
+    ])
+    camera = dict(position=(0.0, 0.25, -3.4), rotation=(0.0, 0.0, 0.0), fov=45.0)
+    sky = np.ones((1, 1, 4), np.float32)
+    out = dict(verts=np.ascontiguousarray(verts), mat_idx=mat_idx, mats=mats, camera=camera, skybox=sky,
+               width=1920, height=1080, spp=256, max_bounces=16)
+    if cache:
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        tmp = cache + f".{os.getpid()}.npz"
+        np.savez(tmp, verts=out["verts"], mat_idx=mat_idx, mats=mats, skybox=sky)
+        os.replace(tmp, cache)
+    return out
+
+
+def _cache_path(*key):
+    """Scenes are pure functions of their parameters; a generated one may be
+    kept under $CRG_SCENE_CACHE (default /tmp/crg_scene_cache) for reuse by
+    later processes.  CRG_SCENE_CACHE="" disables the cache."""
+    root = os.environ.get("CRG_SCENE_CACHE", "/tmp/crg_scene_cache")
+    if not root:
+        return None
+    return os.path.join(root, "_".join(str(k) for k in key) + ".npz")
