@@ -78,6 +78,15 @@ class BvhInfo(C.Structure):
     ]
 
 
+class View(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("pad_", C.c_uint32), ("camera", Camera), ("settings", Settings)]
+
+
+class WavefrontOpts(C.Structure):
+    _fields_ = [("path_pool", C.c_uint32), ("chunk_samples", C.c_uint32), ("block_size", C.c_uint32),
+                ("fetch", C.c_uint32), ("max_iterations", C.c_uint32)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("segments", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64)]
@@ -157,6 +166,8 @@ CRG_SIGNATURES = [
     ("crg_film_device_ptrs", C.c_int, [vp, P(vp), P(vp), P(vp)]),
     ("crg_film_display", C.c_int, [vp, vp, c_stream]),
     ("crg_render", C.c_int, [vp, P(Camera), P(Settings), vp, c_stream]),
+    ("crg_render_batch", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
+    ("crg_batch_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_scene_set_counting", C.c_int, [vp, C.c_int]),
 ]

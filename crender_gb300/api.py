@@ -244,3 +244,23 @@ class Film:
 def render(scene: Scene, camera: dict, settings: _abi.Settings, film: Film, stream=None):
     cam = make_camera(camera)
     scene.ctx.check(scene.ctx.lib.crg_render(scene.h, C.byref(cam), C.byref(settings), film.h, stream))
+
+
+def render_batch(scenes, views, films, opts=None, stream=None):
+    """crg_render_batch: views = [(scene_index, camera dict, Settings)], one film each."""
+    ctx = scenes[0].ctx
+    sc = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
+    fl = (C.c_void_p * len(films))(*[f.h.value for f in films])
+    vs = (_abi.View * len(views))()
+    for i, (si, cam, st) in enumerate(views):
+        vs[i].scene = si
+        vs[i].camera = make_camera(cam)
+        vs[i].settings = st
+    o = _abi.WavefrontOpts(**(opts or {}))
+    return ctx.lib.crg_render_batch(sc, len(scenes), vs, fl, len(views), C.byref(o), stream)
+
+
+def batch_stats(ctx) -> dict:
+    s = _abi.RenderStats()
+    ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))
+    return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays)

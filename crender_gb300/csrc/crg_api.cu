@@ -253,6 +253,7 @@ crg_status crg_context_create(int device, crg_context **out) {
 
 crg_status crg_context_destroy(crg_context *ctx) {
     if (!ctx) return CRG_ERR_INVALID_ARG;
+    dev_free(ctx->wf_ws);
     delete ctx;
     return CRG_OK;
 }
@@ -597,6 +598,51 @@ crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_sett
         scene->last_stats.nodes_visited = c[3];
         scene->last_stats.tris_tested = c[4];
     }
+    return CRG_OK;
+}
+
+crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, crg_film *const *films,
+                            uint32_t nviews, const crg_wavefront_opts *opts, crg_stream stream) {
+    if (!scenes || nscenes == 0 || !scenes[0]) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scenes[0]->ctx;
+    if (!views || !films || nviews == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty batch");
+    if (nviews > 65535) return set_error(ctx, CRG_ERR_INVALID_ARG, "at most 65535 views per batch");
+    for (uint32_t i = 0; i < nscenes; ++i) {
+        if (!scenes[i] || scenes[i]->ctx != ctx) return set_error(ctx, CRG_ERR_INVALID_ARG, "scenes must share one context");
+        if (!scenes[i]->built) return set_error(ctx, CRG_ERR_NOT_BUILT, "scene not built");
+        if (scenes[i]->width != scenes[0]->width) return set_error(ctx, CRG_ERR_INVALID_ARG, "scenes must share one BVH width");
+        if (scenes[i]->ntri == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "scene has no triangles");
+    }
+    for (uint32_t v = 0; v < nviews; ++v) {
+        const crg_settings &s = views[v].settings;
+        if (views[v].scene >= nscenes) return set_error(ctx, CRG_ERR_INVALID_ARG, "view scene index out of range");
+        if (!films[v] || films[v]->ctx != ctx) return set_error(ctx, CRG_ERR_INVALID_ARG, "null film or film of another context");
+        if (s.width != films[v]->width || s.height != films[v]->height)
+            return set_error(ctx, CRG_ERR_INVALID_ARG, "view resolution differs from its film");
+        if (s.mode > CRG_MODE_EXTENDED || views[v].camera.mode > CRG_CAMERA_ORTHOGRAPHIC)
+            return set_error(ctx, CRG_ERR_INVALID_ARG, "bad estimator or camera mode");
+        if (s.max_bounces > 1023) return set_error(ctx, CRG_ERR_INVALID_ARG, "max_bounces above 1023");
+        if (films[v]->spp + s.spp > 0xFFFFFFFFull) return set_error(ctx, CRG_ERR_INVALID_ARG, "sample index would exceed 2^32");
+        for (uint32_t u = 0; u < v; ++u)
+            if (films[u] == films[v]) return set_error(ctx, CRG_ERR_INVALID_ARG, "films must be distinct");
+    }
+    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0};
+    if (opts) {
+        if (opts->path_pool) o.path_pool = opts->path_pool;
+        if (opts->chunk_samples) o.chunk_samples = opts->chunk_samples;
+        if (opts->block_size) o.block_size = opts->block_size;
+        if (opts->fetch) o.fetch = opts->fetch;
+        o.max_iterations = opts->max_iterations;
+    }
+    if ((o.block_size != 64 && o.block_size != 128 && o.block_size != 256) || o.fetch % 32 || o.fetch > 4096 ||
+        o.path_pool > (1u << 28))
+        return set_error(ctx, CRG_ERR_INVALID_ARG, "wavefront options: block_size 64/128/256, fetch a multiple of 32");
+    return render_batch(ctx, scenes, nscenes, views, films, nviews, o, (cudaStream_t)stream, &ctx->batch_stats);
+}
+
+crg_status crg_batch_stats_get(const crg_context *ctx, crg_render_stats *stats) {
+    if (!ctx || !stats) return CRG_ERR_INVALID_ARG;
+    *stats = ctx->batch_stats;
     return CRG_OK;
 }
 

@@ -8,16 +8,18 @@
 
 #include "../../include/crg.h"
 
+// Device buffer owned by a scene, film or context.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
 struct crg_context {
     int device = 0;
     std::string last_error;
     int sm_count = 0;
-};
-
-// Device buffer owned by a scene or film.
-struct DevBuf {
-    void *ptr = nullptr;
-    size_t bytes = 0;
+    DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
+    crg_render_stats batch_stats{};
 };
 
 struct crg_scene {
@@ -91,6 +93,11 @@ struct CamDev {
 CamDev camera_params(const crg_camera &c);
 crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film,
                          cudaStream_t stream);
+
+// wavefront.cu
+crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
+                        crg_film *const *films, uint32_t nviews, const crg_wavefront_opts &o, cudaStream_t stream,
+                        crg_render_stats *stats);
 
 } // namespace crg
 

@@ -151,7 +151,8 @@ void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, con
 
 } // namespace
 
-crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film, cudaStream_t st) {
+namespace rc {
+SceneDev scene_dev(const crg_scene *s) {
     SceneDev S{};
     S.nodes = (const uint4 *)s->wide.ptr;
     S.tris = (const float4 *)s->tris.ptr;
@@ -179,6 +180,12 @@ crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &se
     }
     S.err = (uint32_t *)s->err.ptr;
     S.counters = s->counting ? (unsigned long long *)s->counters.ptr : nullptr;
+    return S;
+}
+} // namespace rc
+
+crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film, cudaStream_t st) {
+    const SceneDev S = scene_dev(s);
     FilmDev F{(float *)film->sum.ptr,
               (double *)film->sum64.ptr,
               (double *)film->sumsq64.ptr,

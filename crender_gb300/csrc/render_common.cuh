@@ -39,6 +39,9 @@ struct SceneDev {
     unsigned long long *counters;
 };
 
+// Device view of a built scene (defined in render.cu).
+SceneDev scene_dev(const crg_scene *s);
+
 struct FilmDev {
     float *sum;
     double *sum64, *sumsq64;

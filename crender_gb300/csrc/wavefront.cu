@@ -1,0 +1,624 @@
+// wavefront.cu — batched wavefront path tracer (sm_103a).
+//
+// Many views (cameras over one or more scenes, each with its own resolution
+// and spp) are rendered in one CUDA-graph launch.  Paths live in a pool of P
+// slots (structure of arrays in HBM) and move through queues:
+//
+//   extend   closest hit for every path in the input queue
+//   shade    one bounce of the shared shading code (render_common.cuh): a path
+//            that continues goes to the output queue, an NEE shadow request
+//            to the shadow queue; a finished path writes its sample and the
+//            slot immediately takes the next sample of the batch
+//   shadow   the shadow tests; a visible contribution is added to the path
+//   control  swaps the queues, detects a drained chunk, and sets the graph's
+//            WHILE condition (bounded by an iteration cap that raises
+//            CRG_ERR_TIMEOUT instead of looping forever)
+//   resolve  adds a drained chunk's per-sample radiance to the films in sample
+//            order, so films are bit-identical to the megakernel's
+//   generate seeds the pool with the next chunk's first samples
+//
+// extend / shade / shadow are persistent kernels: a fixed grid whose warps
+// take `fetch` queue entries at a time with one atomic.  The order in which L
+// receives contributions (emission of bounce i, then NEE of bounce i, then
+// bounce i + 1) is the megakernel's, because the shadow kernel of bounce i
+// runs before the shade kernel of bounce i + 1.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "render_common.cuh"
+
+namespace crg {
+using namespace rc;
+namespace {
+
+struct ViewDev {
+    CamDev cam;
+    crg_settings set;
+    uint32_t scene;
+    uint32_t npix;
+    uint64_t spp0; // film sample count before this batch (sample index offset)
+    float *sum;
+    double *sum64, *sumsq64;
+};
+
+struct Segment {            // samples [s0, s1) of one view, contiguous in gid order
+    unsigned long long gid; // first gid of the segment
+    uint32_t view, s0, s1;
+    uint32_t pix_base;      // prefix of npix over the chunk's segments (resolve work index)
+};
+
+struct Chunk {
+    unsigned long long gid_begin, gid_end;
+    uint32_t seg_begin, seg_end;
+    uint32_t resolve_items; // sum of npix over the chunk's segments
+    uint32_t pad_;
+};
+
+struct Ctrl {
+    unsigned int in_count, out_count, sh_count;
+    unsigned int head_ext, head_shade, head_sh;
+    unsigned int parity;
+    unsigned int chunk;          // chunk being rendered
+    unsigned int resolve_chunk;  // chunk to resolve this iteration, or ~0u
+    unsigned int generate;       // 1: seed the pool with `chunk`
+    unsigned int done;
+    unsigned int error;
+    unsigned int iterations, max_iterations;
+    unsigned long long issued;   // next gid to issue in `chunk`
+    unsigned long long segments, shadow;
+};
+
+constexpr uint32_t kFinish = 1u << 31;    // meta.x flag: finish after the shadow test
+constexpr uint32_t kPrevDelta = 1u << 30; // meta.x flag: previous bounce was a delta lobe
+
+struct Wf {
+    Ctrl *ctrl;
+    const SceneDev *scenes;
+    const ViewDev *views;
+    const Segment *segs;
+    const Chunk *chunks;
+    uint32_t nchunks, P, fetch, pad_;
+    float4 *o, *d, *T, *L; // T.w = prev_pdf
+    uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
+    float4 *hit;           // t, prim bits, triangle slot bits, found
+    float4 *sh_o, *sh_d, *sh_c;
+    uint32_t *qa, *qb, *qsh;
+    float4 *slots;         // radiance per sample of the current chunk
+};
+
+__device__ __forceinline__ uint32_t *q_in(const Wf &w, const Ctrl &c) { return c.parity ? w.qb : w.qa; }
+__device__ __forceinline__ uint32_t *q_out(const Wf &w, const Ctrl &c) { return c.parity ? w.qa : w.qb; }
+
+// Warp-cooperative fetch of `fetch` entries; returns the first index (all
+// lanes of the active mask agree).
+__device__ __forceinline__ unsigned int warp_fetch(unsigned int *head, uint32_t fetch) {
+    unsigned int b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(head, fetch);
+    return __shfl_sync(0xFFFFFFFFu, b, 0);
+}
+
+// Warp-aggregated append of flagged lanes to a queue.
+__device__ __forceinline__ void warp_push(bool want, uint32_t value, uint32_t *queue, unsigned int *count) {
+    const uint32_t active = __activemask();
+    const uint32_t m = __ballot_sync(active, want);
+    if (!m) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(active, base, leader);
+    if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// Starts sample `gid` of the batch in path slot `slot` (camera ray, empty
+// throughput and radiance), exactly as the megakernel starts a sample.
+__device__ void start_sample(const Wf &w, uint32_t slot, unsigned long long gid, const Chunk &ch) {
+    uint32_t lo = ch.seg_begin, hi = ch.seg_end - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (w.segs[mid].gid <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    const Segment sg = w.segs[lo];
+    const ViewDev &V = w.views[sg.view];
+    const unsigned long long rel = gid - sg.gid;
+    const uint32_t s = sg.s0 + (uint32_t)(rel / V.npix);
+    const uint32_t pix = (uint32_t)(rel % V.npix);
+    const uint32_t sample = (uint32_t)(V.spp0 + s);
+    const uint32_t Wd = V.set.width, Hd = V.set.height;
+    const uint32_t px = pix % Wd, py = pix / Wd;
+    const f4 g0 = rand4(pix, sample, 0, V.set.seed);
+    const float x = ((float)px + g0.x) / (float)Wd;
+    const float y = ((float)py + g0.y) / (float)Hd;
+    v3 o, d;
+    camera_ray(V.cam, x, y, V.set.aspect, o, d);
+    w.o[slot] = make_float4(o.x, o.y, o.z, 0.0f);
+    w.d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
+    w.T[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.L[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.meta[slot] = make_uint4(sg.view | kPrevDelta, pix, sample, (uint32_t)(gid - ch.gid_begin));
+}
+
+// Writes a finished sample and, if the chunk has more, starts the next one
+// in the same slot (pushed to the output queue).
+__device__ __forceinline__ void finish_and_refill(const Wf &w, Ctrl *c, bool finishing, uint32_t slot, float4 Lv,
+                                                  uint32_t off) {
+    if (finishing) w.slots[off] = Lv;
+    const uint32_t active = __activemask();
+    const uint32_t m = __ballot_sync(active, finishing);
+    bool refill = false;
+    unsigned long long gid = 0;
+    const Chunk ch = w.chunks[c->chunk];
+    if (m) {
+        const uint32_t lane = threadIdx.x & 31;
+        const int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if ((int)lane == leader) base = atomicAdd(&c->issued, (unsigned long long)__popc(m));
+        base = __shfl_sync(active, base, leader);
+        gid = base + __popc(m & ((1u << lane) - 1u));
+        refill = finishing && gid < ch.gid_end;
+    }
+    if (refill) start_sample(w, slot, gid, ch);
+    warp_push(refill, slot, q_out(w, *c), &c->out_count);
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
+    Ctrl *c = w.ctrl;
+    const unsigned int n = c->in_count;
+    const uint32_t *in = q_in(w, *c);
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        const unsigned int base = warp_fetch(&c->head_ext, w.fetch);
+        if (base >= n) break;
+        for (uint32_t k = lane; k < w.fetch; k += 32) {
+            const unsigned int qi = base + k;
+            if (qi >= n) break;
+            const uint32_t slot = in[qi];
+            const uint32_t view = w.meta[slot].x & 0xFFFFu;
+            const SceneDev &S = w.scenes[w.views[view].scene];
+            const float4 o = w.o[slot], d = w.d[slot];
+            PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
+            Hit h;
+            const bool found = closest<W, false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
+            w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), found ? 1.0f : 0.0f);
+            if (C.err) atomicOr(&c->error, 1u);
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
+    Ctrl *c = w.ctrl;
+    const unsigned int n = c->in_count;
+    const uint32_t *in = q_in(w, *c);
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        const unsigned int base = warp_fetch(&c->head_shade, w.fetch);
+        if (base >= n) break;
+        for (uint32_t k0 = 0; k0 < w.fetch; k0 += 32) {
+            if (base + k0 >= n) break;
+            const unsigned int qi = base + k0 + lane;
+            const bool valid = qi < n && k0 + lane < w.fetch;
+            uint32_t slot = 0;
+            bool cont = false, finishing = false, shadow = false;
+            float4 Lv = make_float4(0, 0, 0, 0);
+            uint32_t off = 0;
+            if (valid) {
+                slot = in[qi];
+                uint4 m = w.meta[slot];
+                const uint32_t view = m.x & 0xFFFFu, depth = (m.x >> 16) & 0x3FFu;
+                const ViewDev &V = w.views[view];
+                const SceneDev &S = w.scenes[V.scene];
+                const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot], h4 = w.hit[slot];
+                PathState ps;
+                ps.o = mk(o.x, o.y, o.z);
+                ps.d = mk(d.x, d.y, d.z);
+                ps.T = mk(T.x, T.y, T.z);
+                ps.L = mk(L.x, L.y, L.z);
+                ps.prev_pdf = T.w;
+                ps.prev_delta = (m.x & kPrevDelta) ? 1u : 0u;
+                Hit h;
+                h.t = h4.x;
+                h.prim = __float_as_uint(h4.y);
+                h.slot = __float_as_uint(h4.z);
+                h.u = h.v = 0.0f;
+                PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
+                Aov aov;
+                NeeReq nr;
+                cont = V.set.mode == CRG_MODE_EXTENDED ? shade_extended(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr)
+                                                       : shade_faithful(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr);
+                if (cont && depth + 1 >= V.set.max_bounces) cont = false;
+                Lv = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
+                w.L[slot] = Lv;
+                off = m.w;
+                shadow = nr.kind != 0;
+                if (shadow) {
+                    w.sh_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.tmax);
+                    w.sh_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, __uint_as_float(nr.kind));
+                    w.sh_c[slot] = make_float4(nr.c.x, nr.c.y, nr.c.z, 0.0f);
+                }
+                uint32_t mx_ = (m.x & 0xFFFFu) | ((depth + 1) << 16) | (ps.prev_delta ? kPrevDelta : 0u);
+                if (!cont && shadow) mx_ |= kFinish;
+                m.x = mx_;
+                w.meta[slot] = m;
+                if (cont) {
+                    w.o[slot] = make_float4(ps.o.x, ps.o.y, ps.o.z, 0.0f);
+                    w.d[slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, 0.0f);
+                    w.T[slot] = make_float4(ps.T.x, ps.T.y, ps.T.z, ps.prev_pdf);
+                }
+                finishing = !cont && !shadow;
+            }
+            warp_push(valid && shadow, slot, w.qsh, &c->sh_count);
+            warp_push(valid && cont, slot, q_out(w, *c), &c->out_count);
+            finish_and_refill(w, c, valid && finishing, slot, Lv, off);
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
+    Ctrl *c = w.ctrl;
+    const unsigned int n = c->sh_count;
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        const unsigned int base = warp_fetch(&c->head_sh, w.fetch);
+        if (base >= n) break;
+        for (uint32_t k0 = 0; k0 < w.fetch; k0 += 32) {
+            if (base + k0 >= n) break;
+            const unsigned int qi = base + k0 + lane;
+            const bool valid = qi < n && k0 + lane < w.fetch;
+            uint32_t slot = 0, off = 0;
+            bool finishing = false;
+            float4 Lv = make_float4(0, 0, 0, 0);
+            if (valid) {
+                slot = w.qsh[qi];
+                uint4 m = w.meta[slot];
+                const ViewDev &V = w.views[m.x & 0xFFFFu];
+                const SceneDev &S = w.scenes[V.scene];
+                const float4 so = w.sh_o[slot], sd = w.sh_d[slot], sc = w.sh_c[slot];
+                NeeReq nr;
+                nr.o = mk(so.x, so.y, so.z);
+                nr.d = mk(sd.x, sd.y, sd.z);
+                nr.c = mk(sc.x, sc.y, sc.z);
+                nr.tmax = so.w;
+                nr.kind = __float_as_uint(sd.w);
+                PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
+                Lv = w.L[slot];
+                if (shadow_visible<W, false>(S, nr, C)) {
+                    const v3 L = add(mk(Lv.x, Lv.y, Lv.z), nr.c);
+                    Lv = make_float4(L.x, L.y, L.z, 0.0f);
+                    w.L[slot] = Lv;
+                }
+                if (C.err) atomicOr(&c->error, 1u);
+                finishing = (m.x & kFinish) != 0u;
+                off = m.w;
+            }
+            finish_and_refill(w, c, valid && finishing, slot, Lv, off);
+        }
+    }
+}
+
+__global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle) {
+    if (threadIdx.x != 0) return;
+    Ctrl *c = w.ctrl;
+    c->segments += c->in_count;
+    c->shadow += c->sh_count;
+    c->parity ^= 1u;
+    c->in_count = c->out_count;
+    c->out_count = 0;
+    c->sh_count = 0;
+    c->head_ext = c->head_shade = c->head_sh = 0;
+    c->resolve_chunk = 0xFFFFFFFFu;
+    c->generate = 0;
+    if (c->in_count == 0) {
+        // chunk drained: resolve it, then seed the next one or stop
+        c->resolve_chunk = c->chunk;
+        if (c->chunk + 1 < w.nchunks) {
+            c->chunk += 1;
+            c->generate = 1;
+        } else {
+            c->done = 1;
+        }
+    }
+    c->iterations += 1;
+    if (c->iterations >= c->max_iterations && !c->done) {
+        c->error |= 2u; // bounded loop ran out
+        c->done = 1;
+    }
+    cudaGraphSetConditional(handle, c->done ? 0u : 1u);
+}
+
+__global__ void k_wf_resolve(Wf w) {
+    const Ctrl *c = w.ctrl;
+    const uint32_t k = c->resolve_chunk;
+    if (k == 0xFFFFFFFFu) return;
+    const Chunk ch = w.chunks[k];
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < ch.resolve_items; item += gridDim.x * blockDim.x) {
+        uint32_t lo = ch.seg_begin, hi = ch.seg_end - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (w.segs[mid].pix_base <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const Segment sg = w.segs[lo];
+        const ViewDev &V = w.views[sg.view];
+        const uint32_t pix = item - sg.pix_base;
+        const uint32_t px = pix % V.set.width, py = pix / V.set.width;
+        const size_t fidx = (size_t)(V.set.width - 1 - px) + (size_t)(V.set.height - 1 - py) * V.set.width;
+        float acc[3] = {V.sum[fidx * 3], V.sum[fidx * 3 + 1], V.sum[fidx * 3 + 2]};
+        double a64[3] = {0, 0, 0}, q64[3] = {0, 0, 0};
+        if (V.sum64) {
+            for (int k3 = 0; k3 < 3; ++k3) {
+                a64[k3] = V.sum64[fidx * 3 + k3];
+                q64[k3] = V.sumsq64[fidx * 3 + k3];
+            }
+        }
+        const unsigned long long first = sg.gid - ch.gid_begin + pix;
+        for (uint32_t s = sg.s0; s < sg.s1; ++s) {
+            const float4 L = w.slots[first + (unsigned long long)(s - sg.s0) * V.npix];
+            acc[0] += L.x;
+            acc[1] += L.y;
+            acc[2] += L.z;
+            if (V.sum64) {
+                a64[0] += (double)L.x; a64[1] += (double)L.y; a64[2] += (double)L.z;
+                q64[0] += (double)L.x * (double)L.x;
+                q64[1] += (double)L.y * (double)L.y;
+                q64[2] += (double)L.z * (double)L.z;
+            }
+        }
+        V.sum[fidx * 3] = acc[0];
+        V.sum[fidx * 3 + 1] = acc[1];
+        V.sum[fidx * 3 + 2] = acc[2];
+        if (V.sum64) {
+            for (int k3 = 0; k3 < 3; ++k3) {
+                V.sum64[fidx * 3 + k3] = a64[k3];
+                V.sumsq64[fidx * 3 + k3] = q64[k3];
+            }
+        }
+    }
+}
+
+// Seeds the pool with the first min(P, chunk size) samples of the chunk.
+__global__ void k_wf_generate(Wf w, int first) {
+    Ctrl *c = w.ctrl;
+    if (!first && !c->generate) return;
+    const Chunk ch = w.chunks[c->chunk];
+    const unsigned long long total = ch.gid_end - ch.gid_begin;
+    const uint32_t count = (uint32_t)(total < w.P ? total : w.P);
+    uint32_t *in = q_in(w, *c);
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < count; slot += gridDim.x * blockDim.x) {
+        start_sample(w, slot, ch.gid_begin + slot, ch);
+        in[slot] = slot;
+    }
+}
+
+// Sets the counts after a generate (one thread; runs after k_wf_generate).
+__global__ void k_wf_generated(Wf w, int first) {
+    if (threadIdx.x != 0) return;
+    Ctrl *c = w.ctrl;
+    if (!first && !c->generate) return;
+    const Chunk ch = w.chunks[c->chunk];
+    const unsigned long long total = ch.gid_end - ch.gid_begin;
+    const uint32_t count = (uint32_t)(total < w.P ? total : w.P);
+    c->in_count = count;
+    c->issued = ch.gid_begin + count;
+    c->generate = 0;
+}
+
+__global__ void k_wf_start(Ctrl *c, unsigned int max_iterations) {
+    if (threadIdx.x != 0) return;
+    Ctrl z{};
+    z.resolve_chunk = 0xFFFFFFFFu;
+    z.max_iterations = max_iterations;
+    *c = z;
+}
+
+struct Workspace {
+    DevBuf buf;
+};
+
+size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
+
+template <int W>
+crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
+    // prologue on the caller's stream
+    k_wf_start<<<1, 32, 0, st>>>(wf.ctrl, max_iters);
+    k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
+    k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
+    CRG_CUDA(ctx, cudaGetLastError());
+    // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+    crg_status rc = CRG_OK;
+    do {
+        cudaError_t e;
+        if ((e = cudaGraphCreate(&graph, 0)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphCreate"); break; }
+        cudaGraphConditionalHandle handle;
+        if ((e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) {
+            rc = cuda_error(ctx, e, "cudaGraphConditionalHandleCreate");
+            break;
+        }
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp)) != cudaSuccess) {
+            rc = cuda_error(ctx, e, "cudaGraphAddNode(while)");
+            break;
+        }
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) {
+            rc = cuda_error(ctx, e, "cudaStreamCreate");
+            break;
+        }
+        if ((e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess) {
+            rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
+            break;
+        }
+        k_wf_extend<W><<<grid, block, 0, cap>>>(wf);
+        k_wf_shade<W><<<grid, block, 0, cap>>>(wf);
+        k_wf_shadow<W><<<grid, block, 0, cap>>>(wf);
+        k_wf_control<<<1, 32, 0, cap>>>(wf, handle);
+        k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
+        k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
+        k_wf_generated<<<1, 32, 0, cap>>>(wf, 0);
+        e = cudaStreamEndCapture(cap, &body);
+        if (e != cudaSuccess) { rc = cuda_error(ctx, e, "cudaStreamEndCapture"); break; }
+        if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphInstantiate"); break; }
+        if ((e = cudaGraphLaunch(exec, st)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphLaunch"); break; }
+        // the executable graph is destroyed below: wait for it first
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) { rc = cuda_error(ctx, e, "wavefront frame"); break; }
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (cap) cudaStreamDestroy(cap);
+    return rc;
+}
+
+} // namespace
+
+crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
+                        crg_film *const *films, uint32_t nviews, const crg_wavefront_opts &o, cudaStream_t st,
+                        crg_render_stats *stats) {
+    // ---- host-side plan: views, segments, chunks
+    const uint32_t width = scenes[0]->width;
+    std::vector<SceneDev> sdev(nscenes);
+    for (uint32_t i = 0; i < nscenes; ++i) sdev[i] = scene_dev(scenes[i]);
+    std::vector<ViewDev> vdev(nviews);
+    unsigned long long total = 0;
+    for (uint32_t v = 0; v < nviews; ++v) {
+        ViewDev &V = vdev[v];
+        V.cam = camera_params(views[v].camera);
+        V.set = views[v].settings;
+        V.scene = views[v].scene;
+        V.npix = V.set.width * V.set.height;
+        V.spp0 = films[v]->spp;
+        V.sum = (float *)films[v]->sum.ptr;
+        V.sum64 = (double *)films[v]->sum64.ptr;
+        V.sumsq64 = (double *)films[v]->sumsq64.ptr;
+        total += (unsigned long long)V.npix * V.set.spp;
+    }
+    if (total == 0) return CRG_OK;
+    const unsigned long long C = o.chunk_samples;
+    std::vector<Segment> segs;
+    std::vector<Chunk> chunks;
+    {
+        unsigned long long gid = 0, chunk_fill = 0;
+        Chunk cur{0, 0, 0, 0, 0, 0};
+        for (uint32_t v = 0; v < nviews; ++v) {
+            const uint32_t npix = vdev[v].npix;
+            uint32_t s = 0;
+            while (s < vdev[v].set.spp) {
+                if (chunk_fill + npix > C && chunk_fill > 0) { // close the chunk
+                    cur.gid_end = gid;
+                    cur.seg_end = (uint32_t)segs.size();
+                    chunks.push_back(cur);
+                    cur = Chunk{gid, 0, (uint32_t)segs.size(), 0, 0, 0};
+                    chunk_fill = 0;
+                }
+                const unsigned long long room = C > chunk_fill ? (C - chunk_fill) / npix : 0;
+                uint32_t take = (uint32_t)std::min<unsigned long long>(vdev[v].set.spp - s, std::max<unsigned long long>(room, 1));
+                Segment sg{gid, v, s, s + take, cur.resolve_items};
+                segs.push_back(sg);
+                cur.resolve_items += npix;
+                gid += (unsigned long long)take * npix;
+                chunk_fill += (unsigned long long)take * npix;
+                s += take;
+            }
+        }
+        cur.gid_end = gid;
+        cur.seg_end = (uint32_t)segs.size();
+        if (cur.seg_end > cur.seg_begin) chunks.push_back(cur);
+    }
+    unsigned long long max_chunk = 0;
+    for (const Chunk &ch : chunks) max_chunk = std::max(max_chunk, ch.gid_end - ch.gid_begin);
+    const uint32_t P = (uint32_t)std::min<unsigned long long>(o.path_pool, max_chunk);
+    // ---- device workspace (grow-only, owned by the context)
+    const size_t n_sc = align_up(sizeof(SceneDev) * nscenes), n_vd = align_up(sizeof(ViewDev) * nviews);
+    const size_t n_sg = align_up(sizeof(Segment) * segs.size()), n_ch = align_up(sizeof(Chunk) * chunks.size());
+    const size_t n_ctrl = align_up(sizeof(Ctrl));
+    const size_t n_f4 = align_up(sizeof(float4) * (size_t)P), n_u4 = align_up(sizeof(uint4) * (size_t)P);
+    const size_t n_q = align_up(sizeof(uint32_t) * (size_t)P);
+    const size_t n_slots = align_up(sizeof(float4) * (size_t)max_chunk);
+    const size_t bytes = n_sc + n_vd + n_sg + n_ch + n_ctrl + 8 * n_f4 + n_u4 + 3 * n_q + n_slots;
+    crg_status rc = dev_alloc(ctx, ctx->wf_ws, bytes);
+    if (rc != CRG_OK) return rc;
+    char *p = (char *)ctx->wf_ws.ptr;
+    auto take = [&](size_t b) {
+        char *r = p;
+        p += b;
+        return r;
+    };
+    Wf wf{};
+    SceneDev *d_sc = (SceneDev *)take(n_sc);
+    ViewDev *d_vd = (ViewDev *)take(n_vd);
+    Segment *d_sg = (Segment *)take(n_sg);
+    Chunk *d_ch = (Chunk *)take(n_ch);
+    wf.ctrl = (Ctrl *)take(n_ctrl);
+    wf.scenes = d_sc;
+    wf.views = d_vd;
+    wf.segs = d_sg;
+    wf.chunks = d_ch;
+    wf.nchunks = (uint32_t)chunks.size();
+    wf.P = P;
+    wf.fetch = o.fetch;
+    wf.o = (float4 *)take(n_f4);
+    wf.d = (float4 *)take(n_f4);
+    wf.T = (float4 *)take(n_f4);
+    wf.L = (float4 *)take(n_f4);
+    wf.hit = (float4 *)take(n_f4);
+    wf.sh_o = (float4 *)take(n_f4);
+    wf.sh_d = (float4 *)take(n_f4);
+    wf.sh_c = (float4 *)take(n_f4);
+    wf.meta = (uint4 *)take(n_u4);
+    wf.qa = (uint32_t *)take(n_q);
+    wf.qb = (uint32_t *)take(n_q);
+    wf.qsh = (uint32_t *)take(n_q);
+    wf.slots = (float4 *)take(n_slots);
+    CRG_CUDA(ctx, cudaMemcpyAsync(d_sc, sdev.data(), sizeof(SceneDev) * nscenes, cudaMemcpyHostToDevice, st));
+    CRG_CUDA(ctx, cudaMemcpyAsync(d_vd, vdev.data(), sizeof(ViewDev) * nviews, cudaMemcpyHostToDevice, st));
+    CRG_CUDA(ctx, cudaMemcpyAsync(d_sg, segs.data(), sizeof(Segment) * segs.size(), cudaMemcpyHostToDevice, st));
+    CRG_CUDA(ctx, cudaMemcpyAsync(d_ch, chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, st));
+    // persistent grid: resident blocks of the heaviest kernel on every SM
+    int per_sm = 0;
+    cudaError_t e;
+    if (width == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<2>, (int)o.block_size, 0);
+    else if (width == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<4>, (int)o.block_size, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<8>, (int)o.block_size, 0);
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    const uint32_t grid = (uint32_t)(std::max(ctx->sm_count, 1) * per_sm);
+    // every chunk needs at most (samples / P + 1) refills of max_bounces + 1 iterations
+    unsigned long long iters = 16;
+    uint32_t maxb = 1;
+    for (uint32_t v = 0; v < nviews; ++v) maxb = std::max(maxb, vdev[v].set.max_bounces);
+    for (const Chunk &ch : chunks) iters += ((ch.gid_end - ch.gid_begin) / std::max<uint32_t>(P, 1) + 2) * (maxb + 2) * 4;
+    uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
+    if (o.max_iterations) max_iters = o.max_iterations;
+    switch (width) {
+    case 2: rc = run<2>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    case 4: rc = run<4>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    default: rc = run<8>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    }
+    if (rc != CRG_OK) return rc;
+    Ctrl host{};
+    CRG_CUDA(ctx, cudaMemcpyAsync(&host, wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
+    CRG_CUDA(ctx, cudaStreamSynchronize(st));
+    if (host.error & 2u) return set_error(ctx, CRG_ERR_TIMEOUT, "wavefront: iteration cap reached before the batch drained");
+    if (host.error & 1u) return set_error(ctx, CRG_ERR_DEVICE, "wavefront: traversal stack overflow");
+    for (uint32_t v = 0; v < nviews; ++v) films[v]->spp += vdev[v].set.spp;
+    if (stats) {
+        stats->samples = total;
+        stats->segments = host.segments;
+        stats->shadow_rays = host.shadow;
+        stats->nodes_visited = 0;
+        stats->tris_tested = 0;
+    }
+    return CRG_OK;
+}
+
+} // namespace crg

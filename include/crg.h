@@ -307,6 +307,41 @@ crg_status crg_film_display(crg_film *film, float *d_rgba, crg_stream stream);
 crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_settings *settings,
                       crg_film *film, crg_stream stream);
 
+/* ------------------------------------------------------------------ batched wavefront */
+
+/* One view of a batch: a camera over scenes[scene] with its own resolution,
+ * spp, depth, estimator and seed (settings), rendered into its own film. */
+typedef struct crg_view {
+    uint32_t scene;
+    uint32_t pad_;
+    crg_camera camera;
+    crg_settings settings;
+} crg_view;
+
+/* Wavefront knobs (the autotuner's search space besides the BVH width).
+ * Zero fields take the defaults. */
+typedef struct crg_wavefront_opts {
+    uint32_t path_pool;     /* paths in flight (default 4,194,304) */
+    uint32_t chunk_samples; /* samples resolved into the films per chunk (default 33,554,432) */
+    uint32_t block_size;    /* threads per block of the persistent kernels: 64, 128 or 256 (default 128) */
+    uint32_t fetch;         /* queue entries a warp takes per atomic, multiple of 32 (default 64) */
+    uint32_t max_iterations;/* cap on the device-side loop (0 = a bound derived from the batch);
+                               reaching it ends the frame with CRG_ERR_TIMEOUT */
+} crg_wavefront_opts;
+
+/* Renders every view of a batch in one launch of the wavefront form (one CUDA
+ * graph per frame with a device-side loop): generate / extend / shade / shadow
+ * queues driven by persistent kernels with atomic work fetch.  Films receive
+ * exactly the samples crg_render would add (same random numbers, same order):
+ * with the same settings the FP32 and FP64 sums are bit-identical to the
+ * megakernel's.  AOV planes are not written.  All scenes must be built with the
+ * same width and context; films must be distinct.  Replaces the per-pass loop
+ * of the renderer (src/render/renderer.cpp:116-144) for many cameras at once.
+ * Calls on one context must not overlap (they share its workspace). */
+crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
+                            crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
+                            crg_stream stream);
+
 /* Statistics of the last render on this scene (renderer::current_stats,
  * renderer.cpp:396-404): segments traced (the reference's ray count,
  * renderer.cpp:271-272/356) and shadow rays traced. */
@@ -318,6 +353,8 @@ typedef struct crg_render_stats {
     uint64_t tris_tested;   /* triangles tested by all traversals (counting mode) */
 } crg_render_stats;
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats);
+/* Statistics of the last crg_render_batch on this context. */
+crg_status crg_batch_stats_get(const crg_context *ctx, crg_render_stats *stats);
 /* Turn on per-launch counting of segments, shadow rays, nodes visited and
  * triangles tested for crg_render (runs an instrumented kernel variant). */
 crg_status crg_scene_set_counting(crg_scene *scene, int enabled);

@@ -1,0 +1,132 @@
+"""Wavefront form (crg_render_batch) versus the megakernel (crg_render).
+
+Both run the same per-bounce shading code with the same random numbers, and
+the wavefront resolves each sample into the film in sample order, so the FP32
+and FP64 film sums must be bit-identical — for one view, for batches of views
+over several scenes with uneven resolution and spp, and with a path pool and
+chunks small enough to force regeneration and several resolves.  The device
+loop is bounded: a tiny iteration cap must end the frame with TIMEOUT and
+leave the context usable."""
+import numpy as np
+import pytest
+
+from crender_gb300 import api, scenes
+from test_gpu_c_render import _box_variant
+
+pytestmark = pytest.mark.gpu
+
+
+def _mega(ctx, scene, cam, st, passes=1):
+    f = api.Film(ctx, st.width, st.height, f64=True)
+    for _ in range(passes):
+        api.render(scene, cam, st, f)
+    out = f.download(f64=True)
+    f.close()
+    return out
+
+
+def _same(a, b):
+    for k in ("sum", "sum64", "sumsq64"):
+        bad = int((a[k].view(np.uint8).reshape(a[k].size, -1) != b[k].view(np.uint8).reshape(b[k].size, -1)).any(1).sum())
+        assert bad == 0, f"{k}: {bad} values differ"
+
+
+@pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
+@pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64)])
+def test_single_view_matches_megakernel(ctx, mode, rr, opts):
+    sc = _box_variant("materials")
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    st = api.make_settings(40, 30, 6, max_bounces=8, rr_depth=rr, mode=mode, seed=21, aspect=40 / 30)
+    try:
+        ref = _mega(ctx, s, sc["camera"], st)
+        f = api.Film(ctx, 40, 30, f64=True)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], opts))
+        assert f.spp == 6
+        _same(f.download(f64=True), ref)
+        f.close()
+    finally:
+        s.close()
+
+
+def test_batch_of_uneven_views_and_scenes(ctx):
+    a = _box_variant("plain")
+    b = _box_variant("materials")
+    sa = api.Scene(ctx, a["verts"], a["mat_idx"], a["mats"]).build()
+    sb = api.Scene(ctx, b["verts"], b["mat_idx"], b["mats"]).build()
+    sb.set_skybox(np.array([[[0.3, 0.4, 0.5, 1.0]]], np.float32))
+    views = [
+        (0, a["camera"], api.make_settings(32, 32, 4, 8, 3, 1, 1)),
+        (1, dict(position=(0.5, 0.6, -1.2), rotation=(6.0, -4.0, 0.0), fov=50.0), api.make_settings(48, 20, 9, 10, 3, 1, 2, 48 / 20)),
+        (0, a["camera"], api.make_settings(16, 24, 16, 6, 0, 0, 3)),
+        (1, b["camera"], api.make_settings(8, 8, 33, 12, 4, 1, 4)),
+    ]
+    try:
+        refs = [_mega(ctx, (sa, sb)[si], cam, st) for si, cam, st in views]
+        films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
+        ctx.check(api.render_batch([sa, sb], views, films, dict(path_pool=2048, chunk_samples=4096)))
+        for f, r in zip(films, refs):
+            _same(f.download(f64=True), r)
+            f.close()
+        stats = api.batch_stats(ctx)
+        assert stats["samples"] == sum(st.width * st.height * st.spp for _, _, st in views)
+        assert stats["segments"] >= stats["samples"]
+    finally:
+        sa.close()
+        sb.close()
+
+
+def test_accumulates_after_megakernel_passes(ctx):
+    """A film that already holds megakernel samples continues with the next
+    sample indices, exactly like a further megakernel pass."""
+    sc = _box_variant("plain")
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    st = api.make_settings(24, 24, 3, 8, 3, 1, 5)
+    try:
+        ref = _mega(ctx, s, sc["camera"], st, passes=2)
+        f = api.Film(ctx, 24, 24, f64=True)
+        api.render(s, sc["camera"], st, f)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f]))
+        assert f.spp == 6
+        _same(f.download(f64=True), ref)
+        f.close()
+    finally:
+        s.close()
+
+
+def test_iteration_cap_times_out_and_context_survives(ctx):
+    sc = _box_variant("plain")
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    st = api.make_settings(32, 32, 8, 8, 3, 1, 6)
+    try:
+        f = api.Film(ctx, 32, 32)
+        rc = api.render_batch([s], [(0, sc["camera"], st)], [f], dict(max_iterations=3))
+        assert rc == 4  # CRG_ERR_TIMEOUT
+        f.close()
+        # the context still renders
+        ref = _mega(ctx, s, sc["camera"], st)
+        g = api.Film(ctx, 32, 32, f64=True)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [g]))
+        _same(g.download(f64=True), ref)
+        g.close()
+    finally:
+        s.close()
+
+
+def test_displaced_scene_small(ctx, orc):
+    """The displaced-icosphere scene (4,195,280 + 1,282 triangles): megakernel
+    bit-identical to the oracle and to the wavefront at a small resolution."""
+    sc = scenes.displaced_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    s.set_skybox(sc["skybox"])
+    st = api.make_settings(24, 14, 2, 16, 3, 1, 7, 24 / 14)
+    try:
+        ref = _mega(ctx, s, sc["camera"], st)
+        f = api.Film(ctx, 24, 14, f64=True)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f]))
+        _same(f.download(f64=True), ref)
+        f.close()
+    finally:
+        s.close()
+    o = orc.render(sc, sc["camera"], st, skybox=sc["skybox"])
+    _same(ref, o)
+    assert np.isfinite(ref["sum"]).all() and ref["sum"].mean() > 0
