@@ -227,8 +227,14 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                 PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
                 Aov aov;
                 NeeReq nr;
-                cont = V.set.mode == CRG_MODE_EXTENDED ? shade_extended(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr)
-                                                       : shade_faithful(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr);
+                nr.kind = 0;
+                if (depth >= V.set.max_bounces) {
+                    cont = false; // max_bounces == 0: the megakernel traces nothing for this sample
+                } else {
+                    cont = V.set.mode == CRG_MODE_EXTENDED
+                               ? shade_extended(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr)
+                               : shade_faithful(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr);
+                }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
                 Lv = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
                 w.L[slot] = Lv;
