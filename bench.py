@@ -2,23 +2,29 @@
 """Benchmark of the render hot path through the C ABI (libcrg.so).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl crg|reference]
-                    [--workload box|soup]
+                    [--workload batch|box|displaced|soup]
 
 Workloads (seeded synthetic inputs; no external data):
-  box   the 36-triangle box scene, 512x512, 64 spp, 8 segments, Russian
-        roulette from segment 3, extended estimator (NEE + MIS), one frame
-        per step rendered by the one-thread-per-pixel megakernel.
-        Metric: Msamples/s (pixel samples).
-  soup  1,048,576-triangle soup, 16,777,216 closest-hit rays per step.
-        Metric: Mrays/s.
+  batch      (default) 64 views drawn from the box and displaced scenes with
+             resolutions in {128^2 .. 1920x1080} and spp in {16, 64, 256}
+             (4.73G samples): the wavefront form renders the whole batch in one
+             graph launch per step; the megakernel renders the same views one
+             crg_render call each.  Both produce bit-identical films, so equal
+             RMSE holds by construction.  Metric: Msamples/s (wavefront).
+  box        the 36-triangle box scene, 512x512, 64 spp, 8 segments, RR from 3,
+             extended estimator, megakernel.  Metric: Msamples/s.
+  displaced  the displaced icosphere (4,196,562 triangles), 1920x1080, 16 of the
+             256 spp per step (a frame is 16 steps), depth 16, megakernel.
+  soup       1,048,576-triangle soup, 16,777,216 closest-hit rays.  Mrays/s.
 
-`value` is device-timed (CUDA events on the launching stream, inputs resident,
-L2 flushed by a 256 MiB write between steps, outside the events).  `e2e` times
-the same step through the public C ABI from pinned host buffers: scene upload,
-BVH build, render, film download.  --impl reference times the CPU oracle (the
-C++ restatement of the reference integrator, all host cores) on a bounded
-sample of the same workload.  Multi-GPU runs are independent replicas (weak
-scaling, no collective on the data path).
+`value` is device-timed (CUDA events on the launching stream; inputs resident;
+L2 flushed by a 256 MiB write between steps, outside the events).  `e2e` runs
+the same step through the public C ABI from pinned host buffers (scene upload,
+BVH build, render, film download).  `time_to_rmse` (batch and box workloads):
+time for the box configuration to reach RMSE <= 1e-2 against an FP64
+16384-spp image.  --impl reference times the CPU oracle (the C++ restatement
+of the reference integrator; Embree cannot be built here) on all host cores on
+a bounded sample.  Multi-GPU runs are independent replicas (weak scaling).
 """
 from __future__ import annotations
 
@@ -37,6 +43,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BOX = dict(width=512, height=512, spp=64, max_bounces=8, rr_depth=3, mode=1, seed=1)
+L2_NOTE = "flushed between steps (256 MiB write, outside the timed events)"
 
 
 def env_rank():
@@ -76,8 +83,14 @@ class ClockSampler:
         self.th.join(timeout=10)
 
     def summary(self):
-        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in self.rows if r and num(r[0]) is not None]
+        mx = [num(r[1]) for r in self.rows if len(r) > 1 and num(r[1]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
@@ -93,33 +106,55 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def workload_config(w):
+    if w == "batch":
+        return {"workload": "64 uneven views of the box (36 tris) and displaced (4,196,562 tris) scenes, "
+                            "resolutions 128^2..1920x1080, spp 16/64/256, depth 8/16, RR from 3, extended estimator; "
+                            "wavefront form, one graph launch per batch; BVH width 8 with treelets",
+                "views": 64, "samples_per_step": 4728979456, "l2": L2_NOTE}
+    if w == "box":
+        return {"workload": "box scene (36 tris) 512x512, 64 spp, 8 segments, RR from 3, extended estimator, megakernel",
+                "resolution": [512, 512], "spp": 64, "max_bounces": 8, "rr_depth": 3, "l2": L2_NOTE}
+    if w == "displaced":
+        return {"workload": "displaced icosphere (4,196,562 tris) 1920x1080, 16 spp per step, depth 16, RR from 3, "
+                            "extended estimator, megakernel", "l2": L2_NOTE}
+    return {"workload": "soup 1,048,576 tris, 16,777,216 closest-hit rays per step, BVH width 8", "l2": L2_NOTE}
+
+
 # ---------------------------------------------------------------- CPU oracle leg
-def cpu_box(sample_rows: int, nthreads: int = 0):
-    """Times the oracle (C++ restatement of the reference estimator) on rows
-    [0, sample_rows) of the box frame.  Returns (Msamples/s, seconds, samples)."""
+def cpu_render(scene, camera, st, rows, skybox=None):
+    from oracle import orc
+
+    f = orc.render(scene, camera, st, rows=rows, skybox=skybox)
+    return (rows[1] - rows[0]) * st.width * st.spp, f["render_seconds"]
+
+
+def cpu_leg(workload):
+    """Bounded CPU sample of the workload on all host cores (the oracle)."""
     from crender_gb300 import api, scenes
     from oracle import orc
 
-    sc = scenes.box_scene()
-    st = api.make_settings(**BOX)
-    t0 = time.perf_counter()
-    orc.render(sc, sc["camera"], st, nthreads=nthreads, rows=(0, sample_rows))
-    dt = time.perf_counter() - t0
-    n = sample_rows * BOX["width"] * BOX["spp"]
-    return n / dt / 1e6, dt, n
-
-
-def cpu_soup(nrays: int, nthreads: int = 0):
-    from crender_gb300 import scenes
-    from oracle import orc
-
-    v = scenes.soup(1 << 20, 1)
-    rays = scenes.soup_rays(nrays, 2)
-    b = orc.Bvh(v)
-    t0 = time.perf_counter()
-    b.closest(rays, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    return nrays / dt / 1e6, dt, nrays
+    if workload == "soup":
+        v = scenes.soup(1 << 20, 1)
+        rays = scenes.soup_rays(1 << 18, 2)
+        b = orc.Bvh(v)
+        t0 = time.perf_counter()
+        b.closest(rays)
+        dt = time.perf_counter() - t0
+        return (1 << 18) / dt / 1e6, f"262,144 of the 16,777,216 primary rays on the soup ({dt:.1f} s)"
+    n_tot, t_tot, parts = 0, 0.0, []
+    if workload in ("box", "batch"):
+        sc = scenes.box_scene()
+        n, dt = cpu_render(sc, sc["camera"], api.make_settings(**BOX), (0, 64))
+        n_tot, t_tot = n_tot + n, t_tot + dt
+        parts.append(f"box rows 0-63 at 512x512x64 ({n} samples, {dt:.1f} s)")
+    if workload in ("displaced", "batch"):
+        sc = scenes.displaced_scene()
+        st = api.make_settings(1920, 1080, 4, 16, 3, 1, 1, 1920 / 1080)
+        n, dt = cpu_render(sc, sc["camera"], st, (500, 564), skybox=sc["skybox"])
+        n_tot, t_tot = n_tot + n, t_tot + dt
+        parts.append(f"displaced rows 500-563 at 1920x1080x4 ({n} samples, {dt:.1f} s)")
+    return n_tot / t_tot / 1e6, "; ".join(parts)
 
 
 def run_reference(args):
@@ -128,60 +163,84 @@ def run_reference(args):
         return 0
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     cores = os.cpu_count() or 1
-    vals = []
+    vals, sample = [], ""
     for i in range(args.warmup + args.steps):
-        if args.workload == "box":
-            v, dt, n = cpu_box(64)
-            sample = "rows 0-63 of the 512x512 64-spp box frame (2,097,152 samples)"
-        else:
-            v, dt, n = cpu_soup(1 << 18)
-            sample = "262,144 of the 16,777,216 primary rays on the 1,048,576-triangle soup"
+        v, sample = cpu_leg(args.workload)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
-    unit = "Msamples/s" if args.workload == "box" else "Mrays/s"
-    line = {
-        "impl": "reference",
-        "metric": unit,
-        "value": value,
-        "unit": unit,
-        "n_gpus": args.gpus,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic",
-        "config": workload_config(args.workload),
+    unit = "Mrays/s" if args.workload == "soup" else "Msamples/s"
+    print(json.dumps({
+        "impl": "reference", "metric": unit, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(args.workload),
         "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "CPU oracle (C++ restatement of CRender's estimator and an LBVH + watertight traversal "
-                "standing in for Embree 3, which cannot be built here); std::thread over all host cores",
-    }
-    print(json.dumps(line))
+        "note": "CPU oracle: C++ restatement of CRender's estimator with an LBVH + watertight traversal standing in "
+                "for Embree 3, which cannot be built here; std::thread over all host cores",
+    }))
     return 0
 
 
-def workload_config(w):
-    if w == "box":
-        return {"workload": "box scene (36 tris) 512x512, 64 spp, 8 segments, RR from segment 3, extended estimator, "
-                            "megakernel, BVH width 8",
-                "resolution": [512, 512], "spp": 64, "max_bounces": 8, "rr_depth": 3,
-                "l2": "flushed between steps (256 MiB write, outside the timed events)"}
-    return {"workload": "soup 1,048,576 tris, 16,777,216 closest-hit rays per step, BVH width 8",
-            "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+# ---------------------------------------------------------------- GPU helpers
+class Timer:
+    def __init__(self, torch, stream, flush):
+        self.torch, self.stream, self.flush = torch, stream, flush
+
+    def steps(self, fn, steps, warmup):
+        """Sum of per-step CUDA-event times (ms) with an L2 flush between steps."""
+        for _ in range(warmup):
+            fn()
+        self.torch.cuda.synchronize()
+        evs = [(self.torch.cuda.Event(enable_timing=True), self.torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for e0, e1 in evs:
+            self.flush()
+            e0.record(self.stream)
+            fn()
+            e1.record(self.stream)
+        self.torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+
+def time_to_rmse(ctx, api, scenes, timer, stream, target=1e-2):
+    """Box configuration: spp needed to reach RMSE <= target against an FP64
+    16384-spp reference, and the device time of that many spp for each form."""
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    ref = api.Film(ctx, 512, 512, f64=True)
+    ctx.check(api.render_batch([s], [(0, sc["camera"], api.make_settings(512, 512, 16384, 8, 3, 1, 9001))], [ref]))
+    r = ref.download(f64=True)["sum64"] / 16384.0
+    ref.close()
+    film = api.Film(ctx, 512, 512)
+    spp, rmse, total = 0, float("inf"), 0
+    step = 64
+    while rmse > target and total < 16384:
+        api.render(s, sc["camera"], api.make_settings(512, 512, step, 8, 3, 1, 1), film, stream)
+        total += step
+        img = film.download()["sum"].astype(np.float64) / total
+        rmse = float(np.sqrt(np.mean((img - r) ** 2)))
+        spp = total
+    film.close()
+    st = api.make_settings(512, 512, spp, 8, 3, 1, 1)
+    f = api.Film(ctx, 512, 512)
+    t_mega = timer.steps(lambda: (f.reset(stream), api.render(s, sc["camera"], st, f, stream)), 1, 1)[0]
+    t_wave = timer.steps(lambda: (f.reset(stream), ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], None, stream))), 1, 1)[0]
+    f.close()
+    s.close()
+    return {"target_rmse": target, "spp": spp, "rmse": rmse, "reference": "FP64 16384-spp box image, independent seed",
+            "megakernel_s": t_mega / 1e3, "wavefront_s": t_wave / 1e3}
 
 
 # ---------------------------------------------------------------- GPU leg
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="crg", choices=["crg", "reference"])
-    ap.add_argument("--workload", default="box", choices=["box", "soup"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -199,179 +258,210 @@ def main():
 
     ctx = api.Context(local)
     stream = torch.cuda.current_stream()
-    sh = C_stream = stream.cuda_stream
+    S = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def flush_l2():
-        flush.fill_(rank & 0xFF)
-
+    timer = Timer(torch, stream, lambda: flush.fill_(rank & 0xFF))
     peak, peak_kind = measured_peaks()
-    extra = {}
-    if args.workload == "box":
-        sc = scenes.box_scene()
-        scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
-        st = api.make_settings(**BOX)
-        film = api.Film(ctx, 512, 512)
-        units_per_step = 512 * 512 * BOX["spp"]
-        unit = "Msamples/s"
+    out = {}
+    unit = "Mrays/s" if args.workload == "soup" else "Msamples/s"
+
+    if args.workload == "batch":
+        box, disp = scenes.box_scene(), scenes.displaced_scene()
+        sb = api.Scene(ctx, box["verts"], box["mat_idx"], box["mats"]).build(8, 1)
+        sd = api.Scene(ctx, disp["verts"], disp["mat_idx"], disp["mats"]).build(8, 1)
+        sd.set_skybox(disp["skybox"])
+        vdefs = scenes.batch_views()
+        views = [(si, cam, api.make_settings(v["width"], v["height"], v["spp"], v["max_bounces"], 3, 1, 1 + i,
+                                             v["width"] / v["height"])) for i, (si, cam, v) in enumerate(vdefs)]
+        films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
+        units = sum(st.width * st.height * st.spp for _, _, st in views)
+
+        def wave():
+            for f in films:
+                f.reset(S)
+            ctx.check(api.render_batch([sb, sd], views, films, None, S))
+
+        def mega():
+            for (si, cam, st), f in zip(views, films):
+                f.reset(S)
+                api.render((sb, sd)[si], cam, st, f, S)
+
+        # instrumented wavefront pass (untimed): traversal work for the byte count
+        for f in films:
+            f.reset(S)
+        ctx.check(api.render_batch([sb, sd], views, films, dict(count_work=1), S))
+        torch.cuda.synchronize()
+        work = api.batch_stats(ctx)
+        rays = work["segments"] + work["shadow_rays"]
+        algo = rays * 48 + work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
+        with ClockSampler(local) as clk:
+            ms = timer.steps(wave, args.steps, args.warmup)
+        mega_ms = timer.steps(mega, 2, 1)
+        out["megakernel"] = {"value": units / (sum(mega_ms) / len(mega_ms) / 1e3) / 1e6, "unit": unit,
+                             "ms_per_step": sum(mega_ms) / len(mega_ms),
+                             "how": "same 64 views, one crg_render call per view (the drop-in), 1 warm-up + 2 steps"}
+        out["work"] = {**work, "mrays_per_step": rays / 1e6}
+        kernel = "wavefront frame: one graph launch (k_wf_extend / k_wf_shade / k_wf_shadow / control / resolve)"
+        launches = None  # counted below from the iteration count
+
+        # e2e: both scenes from pinned host memory, build, batch render, all films back to pinned memory
+        pins = {}
+        for name, sc in (("box", box), ("disp", disp)):
+            pins[name] = [api.PinnedArray(ctx, sc[k].shape, sc[k].dtype) for k in ("verts", "mat_idx", "mats")]
+            for p, k in zip(pins[name], ("verts", "mat_idx", "mats")):
+                p.array[...] = sc[k]
+        outs = [api.PinnedArray(ctx, (st.width * st.height * 3,), np.float32) for _, _, st in views]
+        h2d = sum(p.array.nbytes for v in pins.values() for p in v) + 16
+        d2h = sum(o.array.nbytes for o in outs)
+
+        def e2e_step():
+            a = api.Scene(ctx, *[p.array for p in pins["box"]]).build(8, 1, stream=S)
+            b = api.Scene(ctx, *[p.array for p in pins["disp"]]).build(8, 1, stream=S)
+            b.set_skybox(disp["skybox"])
+            for f in films:
+                f.reset(S)
+            ctx.check(api.render_batch([a, b], views, films, None, S))
+            for f, o in zip(films, outs):
+                ctx.check(ctx.lib.crg_film_download(f.h, o.ptr, None, None, None, None, None, S))
+            a.close()
+            b.close()
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / 2
+        out["e2e"] = {"value": units * world / e2e_s / 1e6, "unit": unit, "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                      "path": "crg_scene_create x2 (pinned host geometry) + crg_scene_build x2 + crg_render_batch + "
+                              "64 x crg_film_download (pinned)"}
+        if not args.no_rmse:
+            out["time_to_rmse"] = time_to_rmse(ctx, api, scenes, timer, S)
+    elif args.workload in ("box", "displaced"):
+        if args.workload == "box":
+            sc = scenes.box_scene()
+            st = api.make_settings(**BOX)
+        else:
+            sc = scenes.displaced_scene()
+            st = api.make_settings(1920, 1080, 16, 16, 3, 1, 1, 1920 / 1080)
+        scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+        if "skybox" in sc:
+            scene.set_skybox(sc["skybox"])
+        film = api.Film(ctx, st.width, st.height)
+        units = st.width * st.height * st.spp
 
         def step():
-            film.reset(C_stream)
-            api.render(scene, sc["camera"], st, film, C_stream)
+            film.reset(S)
+            api.render(scene, sc["camera"], st, film, S)
 
-        # instrumented run (untimed): traversal work for the algorithmic-byte count
         scene.set_counting(True)
-        film.reset(C_stream)
-        api.render(scene, sc["camera"], st, film, C_stream)
-        torch.cuda.synchronize()
-        stats = scene.stats()
-        scene.set_counting(False)
-        node_bytes = scene.info()["node_bytes"]
-        rays = stats["segments"] + stats["shadow_rays"]
-        # layout-counted bytes: node loads + triangle loads (48 B) + 12 B film RGB per sample
-        algo_bytes = stats["nodes_visited"] * node_bytes + stats["tris_tested"] * 48 + units_per_step * 12
-        extra["work"] = {"segments": stats["segments"], "shadow_rays": stats["shadow_rays"],
-                         "nodes_visited": stats["nodes_visited"], "tris_tested": stats["tris_tested"],
-                         "mrays_per_frame": rays / 1e6}
-        launches_per_step = 1
-        kernel = "k_render (megakernel)"
-    else:
-        v = scenes.soup(1 << 20, 1)
-        scene = api.Scene(ctx, v, np.zeros(len(v), np.uint32), scenes.material_table([{}])).build()
-        rays_h = scenes.soup_rays(1 << 24, 2)
-        rb = api.DeviceBuffer.from_array(ctx, rays_h)
-        hb = api.DeviceBuffer(ctx, 16 << 24)
-        units_per_step = 1 << 24
-        unit = "Mrays/s"
-        lib = ctx.lib
-
-        def step():
-            ctx.check(lib.crg_intersect_closest(scene.h, rb.ptr, hb.ptr, units_per_step, C_stream))
-
-        nb = api.DeviceBuffer(ctx, 4 << 24)
-        tb = api.DeviceBuffer(ctx, 4 << 24)
-        ctx.check(lib.crg_intersect_closest_counted(scene.h, rb.ptr, hb.ptr, nb.ptr, tb.ptr, units_per_step, C_stream))
-        nodes = nb.download(np.zeros(1 << 24, np.uint32)).astype(np.int64).sum()
-        tris = tb.download(np.zeros(1 << 24, np.uint32)).astype(np.int64).sum()
-        node_bytes = scene.info()["node_bytes"]
-        algo_bytes = units_per_step * (32 + 16) + nodes * node_bytes + tris * 48
-        extra["work"] = {"nodes_visited": int(nodes), "tris_tested": int(tris)}
-        launches_per_step = 1
-        kernel = "k_intersect<8> (closest hit)"
-
-    for _ in range(args.warmup):
         step()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
         torch.cuda.synchronize()
-        for e0, e1 in evs:
-            flush_l2()
-            e0.record(stream)
-            step()
-            e1.record(stream)
-        torch.cuda.synchronize()
-    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_s = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-        torch.distributed.barrier()
-    value = units_per_step * args.steps * world / total_s / 1e6
-    mean_launch_s = total_s / args.steps
-    achieved = algo_bytes / mean_launch_s / 1e9
-
-    # ---- end to end through the C ABI from pinned host buffers
-    e2e = None
-    if args.workload == "box":
+        work = scene.stats()
+        scene.set_counting(False)
+        rays = work["segments"] + work["shadow_rays"]
+        algo = work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
+        out["work"] = {**work, "mrays_per_step": rays / 1e6}
+        with ClockSampler(local) as clk:
+            ms = timer.steps(step, args.steps, args.warmup)
+        kernel = "k_render (megakernel)"
+        launches = args.steps
         pv = api.PinnedArray(ctx, sc["verts"].shape, np.float32)
         pm = api.PinnedArray(ctx, sc["mat_idx"].shape, np.uint32)
         pmat = api.PinnedArray(ctx, sc["mats"].shape, sc["mats"].dtype)
-        pout = api.PinnedArray(ctx, (512 * 512 * 3,), np.float32)
-        pv.array[...] = sc["verts"]
-        pm.array[...] = sc["mat_idx"]
-        pmat.array[...] = sc["mats"]
-        e2e_film = api.Film(ctx, 512, 512)
-        h2d = pv.array.nbytes + pm.array.nbytes + pmat.array.nbytes
-        d2h = pout.array.nbytes
+        pout = api.PinnedArray(ctx, (st.width * st.height * 3,), np.float32)
+        pv.array[...], pm.array[...], pmat.array[...] = sc["verts"], sc["mat_idx"], sc["mats"]
 
         def e2e_step():
-            s2 = api.Scene(ctx, pv.array, pm.array, pmat.array).build(stream=C_stream)
-            e2e_film.reset(C_stream)
-            api.render(s2, sc["camera"], st, e2e_film, C_stream)
-            ctx.check(ctx.lib.crg_film_download(e2e_film.h, pout.ptr, None, None, None, None, None, C_stream))
+            s2 = api.Scene(ctx, pv.array, pm.array, pmat.array).build(8, 1, stream=S)
+            if "skybox" in sc:
+                s2.set_skybox(sc["skybox"])
+            film.reset(S)
+            api.render(s2, sc["camera"], st, film, S)
+            ctx.check(ctx.lib.crg_film_download(film.h, pout.ptr, None, None, None, None, None, S))
             s2.close()
 
-        for _ in range(2):
-            e2e_step()
+        e2e_step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             e2e_step()
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
-        e2e = {"value": units_per_step * world / e2e_s / 1e6, "unit": unit, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
-               "path": "crg_scene_create (pinned host geometry) + crg_scene_build + crg_film_reset + crg_render + "
-                       "crg_film_download (pinned)"}
+        out["e2e"] = {"value": units * world / e2e_s / 1e6, "unit": unit,
+                      "h2d_bytes_per_step": int(pv.array.nbytes + pm.array.nbytes + pmat.array.nbytes),
+                      "d2h_bytes_per_step": int(pout.array.nbytes), "ms_per_step": e2e_s * 1e3,
+                      "path": "crg_scene_create (pinned host geometry) + crg_scene_build + crg_render + crg_film_download"}
+        if args.workload == "box" and not args.no_rmse:
+            out["time_to_rmse"] = time_to_rmse(ctx, api, scenes, timer, S)
     else:
-        pr = api.PinnedArray(ctx, rays_h.shape, rays_h.dtype)
-        pr.array[...] = rays_h
-        ph = api.PinnedArray(ctx, (units_per_step * 16,), np.uint8)
+        v = scenes.soup(1 << 20, 1)
+        scene = api.Scene(ctx, v, np.zeros(len(v), np.uint32), scenes.material_table([{}])).build()
+        n = 1 << 24
+        rays_h = scenes.soup_rays(n, 2)
+        rb = api.DeviceBuffer.from_array(ctx, rays_h)
+        hb = api.DeviceBuffer(ctx, 16 * n)
+        units = n
         lib = ctx.lib
 
+        def step():
+            ctx.check(lib.crg_intersect_closest(scene.h, rb.ptr, hb.ptr, n, S))
+
+        nb, tb = api.DeviceBuffer(ctx, 4 * n), api.DeviceBuffer(ctx, 4 * n)
+        ctx.check(lib.crg_intersect_closest_counted(scene.h, rb.ptr, hb.ptr, nb.ptr, tb.ptr, n, S))
+        nodes = int(nb.download(np.zeros(n, np.uint32)).astype(np.int64).sum())
+        tris = int(tb.download(np.zeros(n, np.uint32)).astype(np.int64).sum())
+        algo = n * 48 + nodes * 80 + tris * 48
+        out["work"] = {"nodes_visited": nodes, "tris_tested": tris}
+        with ClockSampler(local) as clk:
+            ms = timer.steps(step, args.steps, args.warmup)
+        kernel = "k_intersect<8> (closest hit)"
+        launches = args.steps
+        pr = api.PinnedArray(ctx, rays_h.shape, rays_h.dtype)
+        pr.array[...] = rays_h
+        ph = api.PinnedArray(ctx, (n * 16,), np.uint8)
+
         def e2e_step():
-            ctx.check(lib.crg_memcpy_h2d(ctx.h, rb.ptr, pr.ptr, pr.array.nbytes, C_stream))
-            ctx.check(lib.crg_intersect_closest(scene.h, rb.ptr, hb.ptr, units_per_step, C_stream))
-            ctx.check(lib.crg_memcpy_d2h(ctx.h, ph.ptr, hb.ptr, units_per_step * 16, C_stream))
-            ctx.check(lib.crg_stream_sync(ctx.h, C_stream))
+            ctx.check(lib.crg_memcpy_h2d(ctx.h, rb.ptr, pr.ptr, pr.array.nbytes, S))
+            ctx.check(lib.crg_intersect_closest(scene.h, rb.ptr, hb.ptr, n, S))
+            ctx.check(lib.crg_memcpy_d2h(ctx.h, ph.ptr, hb.ptr, n * 16, S))
+            ctx.check(lib.crg_stream_sync(ctx.h, S))
 
         e2e_step()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             e2e_step()
         e2e_s = (time.perf_counter() - t0) / args.steps
-        e2e = {"value": units_per_step * world / e2e_s / 1e6, "unit": unit, "h2d_bytes_per_step": int(pr.array.nbytes),
-               "d2h_bytes_per_step": int(units_per_step * 16), "ms_per_step": e2e_s * 1e3,
-               "path": "crg_memcpy_h2d (pinned rays) + crg_intersect_closest + crg_memcpy_d2h (pinned hits)"}
+        out["e2e"] = {"value": units * world / e2e_s / 1e6, "unit": unit, "h2d_bytes_per_step": int(pr.array.nbytes),
+                      "d2h_bytes_per_step": int(n * 16), "ms_per_step": e2e_s * 1e3,
+                      "path": "crg_memcpy_h2d (pinned rays) + crg_intersect_closest + crg_memcpy_d2h (pinned hits)"}
 
+    total_s = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+        torch.distributed.barrier()
+    value = units * args.steps * world / total_s / 1e6
+    achieved = algo / (total_s / args.steps) / 1e9
+    if launches is None:
+        # per frame: 3 prologue kernels + 7 graph kernels per device-loop iteration
+        launches = args.steps * (3 + 7 * int(api.batch_stats(ctx)["iterations"]))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        if args.workload == "box":
-            cv, cdt, cn = cpu_box(64)
-            cpu = {"value": cv, "unit": unit, "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"rows 0-63 of the 512x512 64-spp box frame ({cn} samples, {cdt:.1f} s)"}
-        else:
-            cv, cdt, cn = cpu_soup(1 << 18)
-            cpu = {"value": cv, "unit": unit, "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"{cn} of the 16,777,216 primary rays ({cdt:.1f} s)"}
-
+        cv, sample = cpu_leg(args.workload)
+        cpu = {"value": cv, "unit": unit, "cores": os.cpu_count(), "kind": "port", "sample": sample}
     if rank == 0:
         line = {
-            "metric": unit,
-            "value": value,
-            "unit": unit,
-            "n_gpus": world,
-            "steps": args.steps,
-            "warmup": args.warmup,
-            "ms_per_step": total_s / args.steps * 1e3,
-            "higher_is_better": True,
-            "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "f32",
-            "data": "synthetic",
-            "config": workload_config(args.workload),
+            "metric": unit, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args.workload),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "kernel": kernel, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": int(algo_bytes)},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "clocks": clk.summary(),
-            "gpu_launches": launches_per_step * args.steps,
-            **extra,
+                         "algorithmic_bytes_per_launch": int(algo)},
+            "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches, **out,
         }
         print(json.dumps(line))
     if world > 1:

@@ -84,12 +84,12 @@ class View(C.Structure):
 
 class WavefrontOpts(C.Structure):
     _fields_ = [("path_pool", C.c_uint32), ("chunk_samples", C.c_uint32), ("block_size", C.c_uint32),
-                ("fetch", C.c_uint32), ("max_iterations", C.c_uint32)]
+                ("fetch", C.c_uint32), ("max_iterations", C.c_uint32), ("count_work", C.c_uint32)]
 
 
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("segments", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64)]
+                ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("iterations", C.c_uint64)]
 
 
 # numpy views of the same layouts
@@ -204,6 +204,7 @@ class OrcFilm(C.Structure):
         ("spp", C.c_uint64),
         ("segments", C.c_uint64),
         ("shadow_rays", C.c_uint64),
+        ("render_seconds", C.c_double),
     ]
 
 

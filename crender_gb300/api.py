@@ -263,4 +263,5 @@ def render_batch(scenes, views, films, opts=None, stream=None):
 def batch_stats(ctx) -> dict:
     s = _abi.RenderStats()
     ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))
-    return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays)
+    return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays, nodes_visited=s.nodes_visited,
+                tris_tested=s.tris_tested, iterations=s.iterations)

@@ -67,6 +67,7 @@ struct Ctrl {
     unsigned int iterations, max_iterations;
     unsigned long long issued;   // next gid to issue in `chunk`
     unsigned long long segments, shadow;
+    unsigned long long nodes, tris; // traversal work (instrumented variant only)
 };
 
 constexpr uint32_t kFinish = 1u << 31;    // meta.x flag: finish after the shadow test
@@ -163,8 +164,9 @@ __device__ __forceinline__ void finish_and_refill(const Wf &w, Ctrl *c, bool fin
     warp_push(refill, slot, q_out(w, *c), &c->out_count);
 }
 
-template <int W>
+template <int W, bool CNT>
 __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
+    unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
     const uint32_t *in = q_in(w, *c);
@@ -181,10 +183,18 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             const float4 o = w.o[slot], d = w.d[slot];
             PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
             Hit h;
-            const bool found = closest<W, false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
+            const bool found = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
             w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), found ? 1.0f : 0.0f);
             if (C.err) atomicOr(&c->error, 1u);
+            if (CNT) {
+                nodes += C.nodes;
+                tris += C.tris;
+            }
         }
+    }
+    if (CNT) {
+        atomicAdd(&c->nodes, nodes);
+        atomicAdd(&c->tris, tris);
     }
 }
 
@@ -263,8 +273,9 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
     }
 }
 
-template <int W>
+template <int W, bool CNT>
 __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
+    unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
     const unsigned int n = c->sh_count;
     const uint32_t lane = threadIdx.x & 31;
@@ -292,17 +303,25 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
                 nr.kind = __float_as_uint(sd.w);
                 PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
                 Lv = w.L[slot];
-                if (shadow_visible<W, false>(S, nr, C)) {
+                if (shadow_visible<W, CNT>(S, nr, C)) {
                     const v3 L = add(mk(Lv.x, Lv.y, Lv.z), nr.c);
                     Lv = make_float4(L.x, L.y, L.z, 0.0f);
                     w.L[slot] = Lv;
                 }
                 if (C.err) atomicOr(&c->error, 1u);
+                if (CNT) {
+                    nodes += C.nodes;
+                    tris += C.tris;
+                }
                 finishing = (m.x & kFinish) != 0u;
                 off = m.w;
             }
             finish_and_refill(w, c, valid && finishing, slot, Lv, off);
         }
+    }
+    if (CNT) {
+        atomicAdd(&c->nodes, nodes);
+        atomicAdd(&c->tris, tris);
     }
 }
 
@@ -427,7 +446,7 @@ struct Workspace {
 
 size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 
-template <int W>
+template <int W, bool CNT>
 crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
     // prologue on the caller's stream
     k_wf_start<<<1, 32, 0, st>>>(wf.ctrl, max_iters);
@@ -466,9 +485,9 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
             rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
             break;
         }
-        k_wf_extend<W><<<grid, block, 0, cap>>>(wf);
+        k_wf_extend<W, CNT><<<grid, block, 0, cap>>>(wf);
         k_wf_shade<W><<<grid, block, 0, cap>>>(wf);
-        k_wf_shadow<W><<<grid, block, 0, cap>>>(wf);
+        k_wf_shadow<W, CNT><<<grid, block, 0, cap>>>(wf);
         k_wf_control<<<1, 32, 0, cap>>>(wf, handle);
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
@@ -605,10 +624,11 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     for (const Chunk &ch : chunks) iters += ((ch.gid_end - ch.gid_begin) / std::max<uint32_t>(P, 1) + 2) * (maxb + 2) * 4;
     uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
     if (o.max_iterations) max_iters = o.max_iterations;
+    const bool cnt = o.count_work != 0;
     switch (width) {
-    case 2: rc = run<2>(ctx, wf, grid, o.block_size, max_iters, st); break;
-    case 4: rc = run<4>(ctx, wf, grid, o.block_size, max_iters, st); break;
-    default: rc = run<8>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    case 2: rc = cnt ? run<2, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<2, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    case 4: rc = cnt ? run<4, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<4, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    default: rc = cnt ? run<8, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<8, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
     }
     if (rc != CRG_OK) return rc;
     Ctrl host{};
@@ -621,8 +641,9 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
         stats->samples = total;
         stats->segments = host.segments;
         stats->shadow_rays = host.shadow;
-        stats->nodes_visited = 0;
-        stats->tris_tested = 0;
+        stats->nodes_visited = host.nodes;
+        stats->tris_tested = host.tris;
+        stats->iterations = host.iterations;
     }
     return CRG_OK;
 }

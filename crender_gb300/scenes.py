@@ -323,3 +323,34 @@ def _cache_path(*key):
     if not root:
         return None
     return os.path.join(root, "_".join(str(k) for k in key) + ".npz")
+
+
+def batch_views(n=64, seed=3):
+    """The batched-render workload: n views, each drawing its scene from
+    {box, displaced}, its resolution from {128^2, 256^2, 512^2, 1024x768,
+    1920x1080} and its spp from {16, 64, 256}, with the camera on a seeded orbit
+    (box: an arc in front of the open face; displaced: around the sphere).
+    Returns [(scene_index, camera dict, dict(width, height, spp, max_bounces))];
+    scene 0 = box_scene(), 1 = displaced_scene()."""
+    rng = np.random.default_rng(seed)
+    res = [(128, 128), (256, 256), (512, 512), (1024, 768), (1920, 1080)]
+    spps = [16, 64, 256]
+    out = []
+    for _ in range(n):
+        scene = int(rng.integers(2))
+        w, h = res[int(rng.integers(len(res)))]
+        spp = spps[int(rng.integers(len(spps)))]
+        a = float(rng.uniform(-25.0, 25.0)) if scene == 0 else float(rng.uniform(-180.0, 180.0))
+        b = float(rng.uniform(-6.0, 6.0)) if scene == 0 else float(rng.uniform(-20.0, 10.0))
+        ra, rb = math.radians(a), math.radians(b)
+        fwd = np.array([math.sin(ra) * math.cos(rb), -math.sin(rb), math.cos(ra) * math.cos(rb)])
+        if scene == 0:
+            pos = np.array([0.5, 0.5, 0.5]) - 1.9 * fwd
+            cam = dict(position=tuple(pos), rotation=(a, b, 0.0), fov=40.0)
+            mb = 8
+        else:
+            pos = -3.4 * fwd
+            cam = dict(position=tuple(pos), rotation=(a, b, 0.0), fov=45.0)
+            mb = 16
+        out.append((scene, cam, dict(width=w, height=h, spp=spp, max_bounces=mb)))
+    return out

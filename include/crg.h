@@ -327,6 +327,8 @@ typedef struct crg_wavefront_opts {
     uint32_t fetch;         /* queue entries a warp takes per atomic, multiple of 32 (default 64) */
     uint32_t max_iterations;/* cap on the device-side loop (0 = a bound derived from the batch);
                                reaching it ends the frame with CRG_ERR_TIMEOUT */
+    uint32_t count_work;    /* 1 = instrumented kernels: crg_batch_stats_get also reports
+                               nodes visited and triangles tested */
 } crg_wavefront_opts;
 
 /* Renders every view of a batch in one launch of the wavefront form (one CUDA
@@ -351,6 +353,7 @@ typedef struct crg_render_stats {
     uint64_t shadow_rays;
     uint64_t nodes_visited; /* wide nodes loaded by all traversals (counting mode) */
     uint64_t tris_tested;   /* triangles tested by all traversals (counting mode) */
+    uint64_t iterations;    /* device-loop iterations of the last batch (wavefront only) */
 } crg_render_stats;
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats);
 /* Statistics of the last crg_render_batch on this context. */

@@ -79,6 +79,7 @@ typedef struct orc_film {
     uint64_t spp;       /* in: samples already accumulated (sample index offset); out: += spp */
     uint64_t segments;  /* out: segments traced (reference ray count) */
     uint64_t shadow_rays;
+    double render_seconds; /* out: wall time of the pixel loop (BVH build excluded) */
 } orc_film;
 
 int orc_render(const orc_scene_desc *scene, const crg_camera *cam, const crg_settings *set, orc_film *film,

@@ -137,4 +137,5 @@ def render(scene: dict, camera: dict, settings: _abi.Settings, film: dict | None
     film["spp"] = f.spp
     film["segments"] = film.get("segments", 0) + f.segments
     film["shadow_rays"] = film.get("shadow_rays", 0) + f.shadow_rays
+    film["render_seconds"] = f.render_seconds
     return film

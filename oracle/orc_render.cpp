@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <limits>
@@ -671,9 +672,11 @@ int orc_render_rows(const orc_scene_desc *desc, const crg_camera *cam, const crg
         seg += my_seg;
         shad += my_sh;
     };
+    const auto t0 = std::chrono::steady_clock::now();
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; ++t) th.emplace_back(work);
     for (auto &t : th) t.join();
+    film->render_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     film->segments += seg.load();
     film->shadow_rays += shad.load();
     orc_bvh_free(bvh);
