@@ -241,6 +241,8 @@ def main():
     ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE leg")
+    ap.add_argument("--form", default="megakernel", choices=["megakernel", "wavefront"],
+                    help="renderer for the box / displaced workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -352,22 +354,35 @@ def main():
         film = api.Film(ctx, st.width, st.height)
         units = st.width * st.height * st.spp
 
-        def step():
-            film.reset(S)
-            api.render(scene, sc["camera"], st, film, S)
+        if args.form == "megakernel":
+            def step():
+                film.reset(S)
+                api.render(scene, sc["camera"], st, film, S)
 
-        scene.set_counting(True)
-        step()
-        torch.cuda.synchronize()
-        work = scene.stats()
-        scene.set_counting(False)
+            scene.set_counting(True)
+            step()
+            torch.cuda.synchronize()
+            work = scene.stats()
+            scene.set_counting(False)
+            kernel = "k_render (megakernel)"
+            launches = args.steps
+        else:
+            def step():
+                film.reset(S)
+                ctx.check(api.render_batch([scene], [(0, sc["camera"], st)], [film], None, S))
+
+            film.reset(S)
+            ctx.check(api.render_batch([scene], [(0, sc["camera"], st)], [film], dict(count_work=1), S))
+            torch.cuda.synchronize()
+            work = api.batch_stats(ctx)
+            kernel = "wavefront frame: one graph launch"
+            launches = args.steps * (3 + 7 * int(work["iterations"]))
         rays = work["segments"] + work["shadow_rays"]
         algo = work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
         out["work"] = {**work, "mrays_per_step": rays / 1e6}
+        out["form"] = args.form
         with ClockSampler(local) as clk:
             ms = timer.steps(step, args.steps, args.warmup)
-        kernel = "k_render (megakernel)"
-        launches = args.steps
         pv = api.PinnedArray(ctx, sc["verts"].shape, np.float32)
         pm = api.PinnedArray(ctx, sc["mat_idx"].shape, np.uint32)
         pmat = api.PinnedArray(ctx, sc["mats"].shape, sc["mats"].dtype)
@@ -448,7 +463,7 @@ def main():
     achieved = algo / (total_s / args.steps) / 1e9
     if launches is None:
         # per frame: 3 prologue kernels + 7 graph kernels per device-loop iteration
-        launches = args.steps * (3 + 7 * int(api.batch_stats(ctx)["iterations"]))
+        launches = args.steps * (3 + 7 * int(out["work"]["iterations"]))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
