@@ -243,6 +243,9 @@ def main():
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE leg")
     ap.add_argument("--form", default="megakernel", choices=["megakernel", "wavefront"],
                     help="renderer for the box / displaced workloads")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="wavefront: drive the loop from the host (profilers cannot see kernels inside "
+                         "graphs with conditional nodes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -367,9 +370,11 @@ def main():
             kernel = "k_render (megakernel)"
             launches = args.steps
         else:
+            wopts = dict(host_loop=1) if args.host_loop else None
+
             def step():
                 film.reset(S)
-                ctx.check(api.render_batch([scene], [(0, sc["camera"], st)], [film], None, S))
+                ctx.check(api.render_batch([scene], [(0, sc["camera"], st)], [film], wopts, S))
 
             film.reset(S)
             ctx.check(api.render_batch([scene], [(0, sc["camera"], st)], [film], dict(count_work=1), S))
@@ -394,7 +399,10 @@ def main():
             if "skybox" in sc:
                 s2.set_skybox(sc["skybox"])
             film.reset(S)
-            api.render(s2, sc["camera"], st, film, S)
+            if args.form == "megakernel":
+                api.render(s2, sc["camera"], st, film, S)
+            else:
+                ctx.check(api.render_batch([s2], [(0, sc["camera"], st)], [film], None, S))
             ctx.check(ctx.lib.crg_film_download(film.h, pout.ptr, None, None, None, None, None, S))
             s2.close()
 
@@ -408,7 +416,8 @@ def main():
         out["e2e"] = {"value": units * world / e2e_s / 1e6, "unit": unit,
                       "h2d_bytes_per_step": int(pv.array.nbytes + pm.array.nbytes + pmat.array.nbytes),
                       "d2h_bytes_per_step": int(pout.array.nbytes), "ms_per_step": e2e_s * 1e3,
-                      "path": "crg_scene_create (pinned host geometry) + crg_scene_build + crg_render + crg_film_download"}
+                      "path": "crg_scene_create (pinned host geometry) + crg_scene_build + "
+                              + ("crg_render" if args.form == "megakernel" else "crg_render_batch") + " + crg_film_download"}
         if args.workload == "box" and not args.no_rmse:
             out["time_to_rmse"] = time_to_rmse(ctx, api, scenes, timer, S)
     else:

@@ -626,7 +626,7 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         for (uint32_t u = 0; u < v; ++u)
             if (films[u] == films[v]) return set_error(ctx, CRG_ERR_INVALID_ARG, "films must be distinct");
     }
-    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0, 0};
+    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0, 0, 0};
     if (opts) {
         if (opts->path_pool) o.path_pool = opts->path_pool;
         if (opts->chunk_samples) o.chunk_samples = opts->chunk_samples;
@@ -634,6 +634,7 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         if (opts->fetch) o.fetch = opts->fetch;
         o.max_iterations = opts->max_iterations;
         o.count_work = opts->count_work;
+        o.host_loop = opts->host_loop;
     }
     if ((o.block_size != 64 && o.block_size != 128 && o.block_size != 256) || o.fetch % 32 || o.fetch > 4096 ||
         o.path_pool > (1u << 28))

@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
     }
 }
 
-__global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle) {
+__global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle, int in_graph) {
     if (threadIdx.x != 0) return;
     Ctrl *c = w.ctrl;
     c->segments += c->in_count;
@@ -352,7 +352,7 @@ __global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle) {
         c->error |= 2u; // bounded loop ran out
         c->done = 1;
     }
-    cudaGraphSetConditional(handle, c->done ? 0u : 1u);
+    if (in_graph) cudaGraphSetConditional(handle, c->done ? 0u : 1u);
 }
 
 __global__ void k_wf_resolve(Wf w) {
@@ -446,13 +446,45 @@ struct Workspace {
 
 size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 
+// Host-driven loop: the same kernels launched from the host, which polls the
+// done flag every 8 iterations (for profilers that cannot see into graphs
+// with conditional nodes, and for runtimes without them).
 template <int W, bool CNT>
-crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
+crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
+    unsigned int *done_h = nullptr;
+    CRG_CUDA(ctx, cudaHostAlloc(&done_h, sizeof(unsigned int), cudaHostAllocDefault));
+    crg_status rc = CRG_OK;
+    for (uint32_t it = 0; it < max_iters + 8; ++it) {
+        k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
+        k_wf_shade<W><<<grid, block, 0, st>>>(wf);
+        k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+        k_wf_control<<<1, 32, 0, st>>>(wf, 0, 0);
+        k_wf_resolve<<<grid, 256, 0, st>>>(wf);
+        k_wf_generate<<<grid, 256, 0, st>>>(wf, 0);
+        k_wf_generated<<<1, 32, 0, st>>>(wf, 0);
+        if ((it & 7) == 7) {
+            cudaError_t e = cudaMemcpyAsync(done_h, &wf.ctrl->done, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                rc = cuda_error(ctx, e, "wavefront host loop");
+                break;
+            }
+            if (*done_h) break;
+        }
+    }
+    cudaFreeHost(done_h);
+    return rc;
+}
+
+template <int W, bool CNT>
+crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st,
+               bool host_loop) {
     // prologue on the caller's stream
     k_wf_start<<<1, 32, 0, st>>>(wf.ctrl, max_iters);
     k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
     k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
     CRG_CUDA(ctx, cudaGetLastError());
+    if (host_loop) return run_host<W, CNT>(ctx, wf, grid, block, max_iters, st);
     // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -488,7 +520,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
         k_wf_extend<W, CNT><<<grid, block, 0, cap>>>(wf);
         k_wf_shade<W><<<grid, block, 0, cap>>>(wf);
         k_wf_shadow<W, CNT><<<grid, block, 0, cap>>>(wf);
-        k_wf_control<<<1, 32, 0, cap>>>(wf, handle);
+        k_wf_control<<<1, 32, 0, cap>>>(wf, handle, 1);
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
         k_wf_generated<<<1, 32, 0, cap>>>(wf, 0);
@@ -624,11 +656,11 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     for (const Chunk &ch : chunks) iters += ((ch.gid_end - ch.gid_begin) / std::max<uint32_t>(P, 1) + 2) * (maxb + 2) * 4;
     uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
     if (o.max_iterations) max_iters = o.max_iterations;
-    const bool cnt = o.count_work != 0;
+    const bool cnt = o.count_work != 0, hl = o.host_loop != 0;
     switch (width) {
-    case 2: rc = cnt ? run<2, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<2, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
-    case 4: rc = cnt ? run<4, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<4, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
-    default: rc = cnt ? run<8, true>(ctx, wf, grid, o.block_size, max_iters, st) : run<8, false>(ctx, wf, grid, o.block_size, max_iters, st); break;
+    case 2: rc = cnt ? run<2, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<2, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
+    case 4: rc = cnt ? run<4, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<4, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
+    default: rc = cnt ? run<8, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<8, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
     }
     if (rc != CRG_OK) return rc;
     Ctrl host{};

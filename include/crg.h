@@ -329,6 +329,8 @@ typedef struct crg_wavefront_opts {
                                reaching it ends the frame with CRG_ERR_TIMEOUT */
     uint32_t count_work;    /* 1 = instrumented kernels: crg_batch_stats_get also reports
                                nodes visited and triangles tested */
+    uint32_t host_loop;     /* 1 = drive the loop from the host instead of one graph with a
+                               device-side condition (same kernels; for profilers) */
 } crg_wavefront_opts;
 
 /* Renders every view of a batch in one launch of the wavefront form (one CUDA

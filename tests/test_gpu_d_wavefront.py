@@ -32,7 +32,8 @@ def _same(a, b):
 
 
 @pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
-@pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64)])
+@pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64),
+                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1)])
 def test_single_view_matches_megakernel(ctx, mode, rr, opts):
     sc = _box_variant("materials")
     s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
