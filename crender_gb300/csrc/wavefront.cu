@@ -328,6 +328,12 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
 __global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle, int in_graph) {
     if (threadIdx.x != 0) return;
     Ctrl *c = w.ctrl;
+    if (c->done) { // iterations after the end (host-driven loop) change nothing
+        c->resolve_chunk = 0xFFFFFFFFu;
+        c->generate = 0;
+        if (in_graph) cudaGraphSetConditional(handle, 0u);
+        return;
+    }
     c->segments += c->in_count;
     c->shadow += c->sh_count;
     c->parity ^= 1u;
