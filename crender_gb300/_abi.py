@@ -167,6 +167,8 @@ CRG_SIGNATURES = [
     ("crg_film_device_ptrs", C.c_int, [vp, P(vp), P(vp), P(vp)]),
     ("crg_film_display", C.c_int, [vp, vp, c_stream]),
     ("crg_render", C.c_int, [vp, P(Camera), P(Settings), vp, c_stream]),
+    ("crg_scene_set_materials", C.c_int, [vp, vp, C.c_uint32]),
+    ("crg_backward", C.c_int, [vp, P(Camera), P(Settings), vp, vp, vp, c_stream]),
     ("crg_render_batch", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
     ("crg_batch_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),
@@ -220,6 +222,7 @@ ORC_SIGNATURES = [
     ("orc_intersect_closest_f64", None, [vp, C.c_uint32, vp, vp, vp, vp, C.c_uint64]),
     ("orc_render", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), P(OrcFilm), C.c_int]),
     ("orc_render_rows", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), P(OrcFilm), C.c_uint32, C.c_uint32, C.c_int]),
+    ("orc_adjoint", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), vp, vp, vp, C.c_int]),
     ("orc_camera_ray", None, [P(Camera), P(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_float, vp, vp]),
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),

@@ -105,9 +105,25 @@ __global__ void k_display(const float *__restrict__ sum, float4 *__restrict__ ou
     }
 }
 
+// Per-triangle areas in double from the float vertices (kept on the host so
+// the emitter table can be rebuilt when materials change).
+void compute_areas(crg_scene *s, const float *verts) {
+    s->tri_area.assign(s->ntri, 0.0);
+    for (uint32_t p = 0; p < s->ntri; ++p) {
+        const float *v = verts + (size_t)p * 9;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = (double)v[3 + a] - (double)v[a];
+            e2[a] = (double)v[6 + a] - (double)v[a];
+        }
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        s->tri_area[p] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+}
+
 // Emissive triangles weighted by area x luminance of colour*emission (double
 // sums in primitive order; CDF and pdfs rounded to float once).
-crg_status prepare_lights(crg_scene *s, const float *verts) {
+crg_status prepare_lights(crg_scene *s) {
     const uint32_t nmat = s->nmat;
     std::vector<double> lum(nmat, 0.0);
     for (uint32_t m = 0; m < nmat; ++m) {
@@ -117,26 +133,14 @@ crg_status prepare_lights(crg_scene *s, const float *verts) {
             lum[m] = 0.2126 * (double)r + 0.7152 * (double)g + 0.0722 * (double)b;
         }
     }
-    std::vector<uint32_t> mat_idx(s->ntri);
-    if (s->ntri) {
-        const cudaError_t e = cudaMemcpy(mat_idx.data(), s->mat_idx.ptr, sizeof(uint32_t) * s->ntri, cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return cuda_error(s->ctx, e, "cudaMemcpy(mat_idx)");
-    }
+    std::vector<uint32_t> &mat_idx = s->host_mat_idx;
     std::vector<uint32_t> prim;
     std::vector<double> w;
     double total = 0.0;
     for (uint32_t p = 0; p < s->ntri; ++p) {
         const uint32_t m = mat_idx[p];
         if (!(lum[m] > 0.0)) continue;
-        const float *v = verts + (size_t)p * 9;
-        double e1[3], e2[3];
-        for (int a = 0; a < 3; ++a) {
-            e1[a] = (double)v[3 + a] - (double)v[a];
-            e2[a] = (double)v[6 + a] - (double)v[a];
-        }
-        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
-        const double ar = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-        const double wt = ar * lum[m];
+        const double wt = s->tri_area[p] * lum[m];
         prim.push_back(p);
         w.push_back(wt);
         total += wt;
@@ -184,6 +188,7 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
     s->ntri = ntri;
     s->nmat = nmat;
     s->host_mats.assign(mats, mats + nmat);
+    s->host_mat_idx.assign(mat_idx, mat_idx + ntri);
     apply_sun(s, default_sun());
     s->sun_enabled = 0;
     crg_status rc;
@@ -318,7 +323,10 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
         const cudaError_t e = cudaMemcpy(s->verts.ptr, verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts)");
     }
-    if (rc == CRG_OK) rc = prepare_lights(s, verts);
+    if (rc == CRG_OK) {
+        compute_areas(s, verts);
+        rc = prepare_lights(s);
+    }
     if (rc != CRG_OK) {
         scene_free(s);
         return rc;
@@ -346,7 +354,10 @@ crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint3
             if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts to host)");
         }
     }
-    if (rc == CRG_OK) rc = prepare_lights(s, hv.data());
+    if (rc == CRG_OK) {
+        compute_areas(s, hv.data());
+        rc = prepare_lights(s);
+    }
     if (rc != CRG_OK) {
         scene_free(s);
         return rc;
@@ -646,6 +657,33 @@ crg_status crg_batch_stats_get(const crg_context *ctx, crg_render_stats *stats) 
     if (!ctx || !stats) return CRG_ERR_INVALID_ARG;
     *stats = ctx->batch_stats;
     return CRG_OK;
+}
+
+crg_status crg_scene_set_materials(crg_scene *scene, const crg_material *mats, uint32_t nmat) {
+    if (!scene || !mats) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scene->ctx;
+    if (nmat != scene->nmat) return set_error(ctx, CRG_ERR_INVALID_ARG, "material count differs from the scene's");
+    for (uint32_t m = 0; m < nmat; ++m)
+        if (mats[m].shade_type > CRG_SHADE_GLASS) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad shade_type");
+    scene->host_mats.assign(mats, mats + nmat);
+    CRG_CUDA(ctx, cudaMemcpy(scene->mats.ptr, mats, sizeof(crg_material) * nmat, cudaMemcpyHostToDevice));
+    return prepare_lights(scene);
+}
+
+crg_status crg_backward(crg_scene *scene, const crg_camera *camera, const crg_settings *settings, const float *d_adjoint,
+                        double *d_grad_colour, double *d_grad_emission, crg_stream stream) {
+    if (!scene || !camera || !settings || !d_adjoint || !d_grad_colour || !d_grad_emission)
+        return set_error(scene ? scene->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
+    crg_context *ctx = scene->ctx;
+    if (!scene->built) return set_error(ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (scene->ntri == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "scene has no triangles");
+    const crg_settings &s = *settings;
+    if (s.mode != CRG_MODE_EXTENDED) return set_error(ctx, CRG_ERR_UNSUPPORTED, "the adjoint differentiates the extended estimator");
+    if (s.max_bounces > 32) return set_error(ctx, CRG_ERR_INVALID_ARG, "adjoint: max_bounces above 32");
+    if (s.width == 0 || s.height == 0 || s.spp == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty adjoint pass");
+    if (camera->mode > CRG_CAMERA_ORTHOGRAPHIC) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad camera mode");
+    if (scene->sun_enabled) return set_error(ctx, CRG_ERR_UNSUPPORTED, "adjoint: the sun belongs to the faithful estimator");
+    return launch_backward(scene, camera_params(*camera), s, d_adjoint, d_grad_colour, d_grad_emission, (cudaStream_t)stream);
 }
 
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats) {

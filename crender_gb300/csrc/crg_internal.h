@@ -31,8 +31,10 @@ struct crg_scene {
     DevBuf mat_idx; // uint32[ntri]
     DevBuf mats;    // crg_material[nmat]
     std::vector<crg_material> host_mats;
+    std::vector<uint32_t> host_mat_idx;
     // emissive triangles (power-weighted CDF)
     uint32_t nlights = 0;
+    std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table
     DevBuf light_prim, light_cdf, light_pdf, mat_light_pdf;
     // environment / sun
     DevBuf sky;
@@ -93,6 +95,10 @@ struct CamDev {
 CamDev camera_params(const crg_camera &c);
 crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film,
                          cudaStream_t stream);
+
+// adjoint.cu
+crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &set, const float *adj, double *g_col,
+                           double *g_em, cudaStream_t stream);
 
 // wavefront.cu
 crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,

@@ -158,7 +158,24 @@ struct NeeReq {
     v3 o, d, c;
     float tmax;
     uint32_t kind; // 0 none, 1 emitter (any hit below tmax), 2 sun (closest hit with alpha pass-through)
+    // parameter factors of c beyond the path throughput (for the adjoint)
+    uint32_t bsdf_mat, light_mat;
+    v3 bsdf_dlog; // d log(BSDF factor) / d colour, per channel
 };
+
+// Records how a path's radiance depends on material parameters (adjoint).
+// Every contribution to L is the throughput (a product of per-bounce factors,
+// each depending on one material's colour) times emitter terms; the tape sees
+// each factor and each contribution.  NullTape compiles to nothing.
+struct NullTape {
+    __device__ __forceinline__ void mult(uint32_t, v3) {}
+    __device__ __forceinline__ void emit(v3, uint32_t) {}
+    __device__ __forceinline__ void env(v3) {}
+};
+
+__device__ __forceinline__ v3 inv_or_zero(v3 c) {
+    return mk(c.x > 0.0f ? 1.0f / c.x : 0.0f, c.y > 0.0f ? 1.0f / c.y : 0.0f, c.z > 0.0f ? 1.0f / c.z : 0.0f);
+}
 
 __device__ __forceinline__ void path_start(PathState &ps, v3 o, v3 d) {
     ps.o = o;
@@ -271,11 +288,17 @@ __device__ __forceinline__ float ggx_lambda(v3 w, float a) {
     const float z2 = w.z * w.z;
     return (sqrtf(1.0f + ((a * a) * s2) / z2) - 1.0f) * 0.5f;
 }
-__device__ __forceinline__ v3 schlick(v3 f0, float c) {
+__device__ __forceinline__ v3 schlick(v3 f0, float c, float *m5_out = nullptr) {
     const float m = 1.0f - clampf(c, 0.0f, 1.0f);
     const float m2 = m * m;
     const float m5 = (m2 * m2) * m;
+    if (m5_out) *m5_out = m5;
     return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+// d log(Schlick F) / d colour for F0 = colour * reflectiveness
+__device__ __forceinline__ v3 schlick_dlog(v3 Fr, float m5, float refl) {
+    const float k = refl * (1.0f - m5);
+    return mk(Fr.x > 0.0f ? k / Fr.x : 0.0f, Fr.y > 0.0f ? k / Fr.y : 0.0f, Fr.z > 0.0f ? k / Fr.z : 0.0f);
 }
 __device__ __forceinline__ v3 sample_vndf(v3 ve, float a, float u1, float u2) {
     const v3 vh = normalize(mk(a * ve.x, a * ve.y, ve.z));
@@ -318,7 +341,7 @@ __device__ __forceinline__ uint32_t pick_light(const SceneDev &S, float u) {
 // Emissive-triangle NEE at p: fills nr (kind 1) with the shadow ray and the
 // contribution it carries if unoccluded; bsdf 0 = Lambert (albedo), 1 = GGX.
 __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo,
-                            const onb &F, v3 wol, float alpha, NeeReq &nr) {
+                            const onb &F, v3 wol, float alpha, NeeReq &nr, uint32_t mat = 0, float refl = 1.0f) {
     nr.kind = 0;
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
     const uint32_t j = pick_light(S, g.x);
@@ -348,6 +371,7 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
         f = mul(albedo, kInvPi);
         p_bsdf = cos_s * kInvPi;
         cos_i = cos_s;
+        nr.bsdf_dlog = inv_or_zero(albedo);
     } else {
         const v3 wil = to_local(F, wi);
         if (!(wil.z > 0.0f)) return;
@@ -357,12 +381,16 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
         const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
         const float G2 = 1.0f / ((1.0f + lo_) + li);
         const float G1 = 1.0f / (1.0f + lo_);
-        const v3 Fr = schlick(albedo, woh);
+        float m5;
+        const v3 Fr = schlick(albedo, woh, &m5);
         f = mul(Fr, (D * G2) / ((4.0f * wol.z) * wil.z));
         p_bsdf = (G1 * D) / (4.0f * wol.z);
         cos_i = wil.z;
+        nr.bsdf_dlog = schlick_dlog(Fr, m5, refl);
     }
     const float w_mis = (p_light * p_light) / (p_light * p_light + p_bsdf * p_bsdf);
+    nr.bsdf_mat = mat;
+    nr.light_mat = __ldg(&S.mat_idx[prim]);
     nr.kind = 1;
     nr.o = po;
     nr.d = wi;
@@ -372,13 +400,16 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
 
 // Extended estimator bounce: MIS-weighted emission, emissive-triangle NEE,
 // Lambert (geometric-normal hemisphere) / GGX VNDF / Fresnel dielectric, RR.
+template <class Tape = NullTape>
 __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set, const PathCtx &C, uint32_t i, PathState &ps,
-                               bool found, const Hit &h, Aov &aov, NeeReq &nr) {
+                                      bool found, const Hit &h, Aov &aov, NeeReq &nr, Tape *tape = nullptr) {
     nr.kind = 0;
     if (!found) {
         const v3 env = sample_sky(S, ps.d);
         if (i == 0) aov.albedo = env;
-        ps.L = add(ps.L, mulv(ps.T, env));
+        const v3 contrib = mulv(ps.T, env);
+        ps.L = add(ps.L, contrib);
+        if (tape) tape->env(contrib);
         return false;
     }
     const v3 p = add(ps.o, mul(ps.d, h.t));
@@ -404,13 +435,17 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
     if (emission > 0.0f) {
         const v3 Le = mk(c0 * emission, c1 * emission, c2 * emission);
         if (ps.prev_delta) {
-            ps.L = add(ps.L, mulv(ps.T, Le));
+            const v3 contrib = mulv(ps.T, Le);
+            ps.L = add(ps.L, contrib);
+            if (tape) tape->emit(contrib, mi);
         } else {
             const float cos_l = absf(cos_nd);
             if (cos_l > 0.0f) {
                 const float pl = (__ldg(&S.mat_light_pdf[mi]) * (h.t * h.t)) / cos_l;
                 const float w = (ps.prev_pdf * ps.prev_pdf) / (ps.prev_pdf * ps.prev_pdf + pl * pl);
-                ps.L = add(ps.L, mul(mulv(ps.T, Le), w));
+                const v3 contrib = mul(mulv(ps.T, Le), w);
+                ps.L = add(ps.L, contrib);
+                if (tape) tape->emit(contrib, mi);
             }
         }
     }
@@ -420,7 +455,7 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
     const uint32_t shade = m.shade_type;
     if (shade == CRG_SHADE_SMOOTH) {
         const onb F = build_local(Ng);
-        if (have_lights) nee_prepare(S, C, i, p, Ng, ps.T, 0, rgb, F, mk(0, 0, 0), 0.0f, nr);
+        if (have_lights) nee_prepare(S, C, i, p, Ng, ps.T, 0, rgb, F, mk(0, 0, 0), 0.0f, nr, mi);
         float sp, cp;
         sincos2pi(g.y, &sp, &cp);
         const float r = sqrtf(g.x);
@@ -430,6 +465,7 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
         ps.prev_pdf = l.z * kInvPi;
         ps.prev_delta = 0u;
         ps.T = mulv(ps.T, rgb);
+        if (tape) tape->mult(mi, inv_or_zero(rgb));
     } else if (shade == CRG_SHADE_METAL) {
         const v3 f0 = mul(rgb, m.reflectiveness);
         const float alpha = m.roughness;
@@ -438,11 +474,12 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
             ps.o = add(p, mul(n, 1e-4f));
             ps.T = mulv(ps.T, f0);
             ps.prev_delta = 1u;
+            if (tape) tape->mult(mi, inv_or_zero(rgb));
         } else {
             const onb F = build_local(n);
             const v3 wol = to_local(F, wo);
             if (!(wol.z > 0.0f)) return false;
-            if (have_lights) nee_prepare(S, C, i, p, n, ps.T, 1, f0, F, wol, alpha, nr);
+            if (have_lights) nee_prepare(S, C, i, p, n, ps.T, 1, f0, F, wol, alpha, nr, mi, m.reflectiveness);
             const v3 hh = sample_vndf(wol, alpha, g.x, g.y);
             const float woh = dot(wol, hh);
             const float k2 = 2.0f * woh;
@@ -451,8 +488,10 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
             const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
             const float G1 = 1.0f / (1.0f + lo_);
             const float G2 = 1.0f / ((1.0f + lo_) + li);
-            const v3 Fr = schlick(f0, woh);
+            float m5;
+            const v3 Fr = schlick(f0, woh, &m5);
             ps.T = mulv(ps.T, mul(Fr, G2 / G1));
+            if (tape) tape->mult(mi, schlick_dlog(Fr, m5, m.reflectiveness));
             ps.prev_pdf = (G1 * ggx_D(hh.z, alpha)) / (4.0f * wol.z);
             ps.prev_delta = 0u;
             ps.d = from_local(F, wil);
@@ -474,6 +513,7 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
         }
         ps.T = mulv(ps.T, rgb);
         ps.prev_delta = 1u;
+        if (tape) tape->mult(mi, inv_or_zero(rgb));
     }
     if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
         const float q = mn(mx(mx(ps.T.x, ps.T.y), ps.T.z), 0.95f);

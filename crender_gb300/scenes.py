@@ -354,3 +354,22 @@ def batch_views(n=64, seed=3):
             mb = 16
         out.append((scene, cam, dict(width=w, height=h, spp=spp, max_bounces=mb)))
     return out
+
+
+def inverse_box(albedo=None, light_colour=None):
+    """Inverse-rendering scene: the box scene with one material per
+    non-emitting triangle (34 albedos, RGB) and one light material of emission
+    17 whose colour sets the radiance (17 x colour; the emitter's colour is
+    also its albedo, as in the reference).  With no arguments the parameters
+    are the box scene's true ones; `albedo` [34, 3] and `light_colour` [3]
+    override them (the optimisation starts from albedo 0.5 and radiance 10,
+    i.e. light colour 10/17)."""
+    base = box_scene()
+    true_alb = base["mats"]["colour"][base["mat_idx"][:34], :3].astype(np.float64)
+    alb = true_alb if albedo is None else np.asarray(albedo, np.float64).reshape(34, 3)
+    lc = np.ones(3) if light_colour is None else np.asarray(light_colour, np.float64).reshape(3)
+    rows = [{"colour": tuple(alb[i]) + (1.0,)} for i in range(34)]
+    rows.append({"colour": tuple(lc) + (1.0,), "emission": 17.0})
+    mat_idx = np.concatenate([np.arange(34, dtype=np.uint32), np.full(2, 34, np.uint32)])
+    return dict(verts=base["verts"], mat_idx=mat_idx, mats=material_table(rows), camera=base["camera"],
+                true_albedo=true_alb, true_light=np.ones(3))

@@ -346,6 +346,30 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
                             crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
                             crg_stream stream);
 
+/* ------------------------------------------------------------------ differentiation */
+
+/* Replaces the material table (same count, e.g. after an optimiser step)
+ * without rebuilding the BVH; the emitter table is rebuilt. */
+crg_status crg_scene_set_materials(crg_scene *scene, const crg_material *mats, uint32_t nmat);
+
+/* Backward half of a forward/backward pair whose forward half is crg_render
+ * (extended estimator): the path-replay adjoint (Vicini, Speierer & Jakob,
+ * SIGGRAPH 2021).  Re-traces settings->spp fresh samples per pixel (sample
+ * indices 0..spp-1 under settings->seed; use a seed different from the
+ * forward pass for an unbiased gradient) and ADDS to
+ *   d_grad_colour   device double[nmat*3]: d/d colour of every material
+ *   d_grad_emission device double[nmat]  : d/d emission of every material
+ * the gradient of sum_p <d_adjoint[p], I[p]>, where I[p] is the pixel's mean
+ * radiance over these samples and d_adjoint is a device float[W*H*3] image in
+ * film layout (typically dLoss/dI of the forward image).  Random decisions
+ * (Russian roulette included) are held fixed, so the result is the exact
+ * derivative of the estimator for those samples: it matches central finite
+ * differences with common random numbers when roulette is off.  No path is
+ * stored.  Requires mode EXTENDED, max_bounces <= 32, sun off. */
+crg_status crg_backward(crg_scene *scene, const crg_camera *camera, const crg_settings *settings,
+                        const float *d_adjoint, double *d_grad_colour, double *d_grad_emission,
+                        crg_stream stream);
+
 /* Statistics of the last render on this scene (renderer::current_stats,
  * renderer.cpp:396-404): segments traced (the reference's ray count,
  * renderer.cpp:271-272/356) and shadow rays traced. */

@@ -88,6 +88,12 @@ int orc_render(const orc_scene_desc *scene, const crg_camera *cam, const crg_set
 int orc_render_rows(const orc_scene_desc *scene, const crg_camera *cam, const crg_settings *set,
                     orc_film *film, uint32_t y0, uint32_t y1, int nthreads);
 
+/* FP64 gradient of sum_p <adj[p], mean of spp samples> (extended estimator,
+ * samples 0..spp-1 under set->seed) w.r.t. every material's colour and
+ * emission, accumulated into grad_colour[nmat*3] and grad_emission[nmat]. */
+int orc_adjoint(const orc_scene_desc *scene, const crg_camera *cam, const crg_settings *set, const float *adj,
+                double *grad_colour, double *grad_emission, int nthreads);
+
 /* Camera ray of pixel (px, py) with jitter (jx, jy) (for unit tests). */
 void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx,
                     float jy, float *org, float *dir);

@@ -139,3 +139,18 @@ def render(scene: dict, camera: dict, settings: _abi.Settings, film: dict | None
     film["shadow_rays"] = film.get("shadow_rays", 0) + f.shadow_rays
     film["render_seconds"] = f.render_seconds
     return film
+
+
+def adjoint(scene: dict, camera: dict, settings: _abi.Settings, adj: np.ndarray, nthreads=0, **kw):
+    """FP64 CPU gradient (colour [nmat, 3], emission [nmat]) of <adj, pixel means>."""
+    from crender_gb300.api import make_camera
+
+    d, keep = scene_desc(scene, **kw)
+    nmat = d.nmat
+    gc = np.zeros(3 * nmat)
+    ge = np.zeros(nmat)
+    adj = np.ascontiguousarray(adj, np.float32)
+    cam = make_camera(camera)
+    rc = lib().orc_adjoint(C.byref(d), C.byref(cam), C.byref(settings), ptr(adj), ptr(gc), ptr(ge), nthreads)
+    assert rc == 0, rc
+    return gc.reshape(nmat, 3), ge

@@ -276,6 +276,61 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
     return L;
 }
 
+/* ------------------------------------------------------------ adjoint tape
+ * Records the parameter factors of a path (path-replay adjoint): every
+ * contribution to L is the throughput (a product of per-bounce factors, each
+ * depending on one material's colour) times emitter terms.  On each
+ * contribution the gradient of <delta, L> is added for every factor:
+ * delta * contribution * d log(factor) / d parameter, in double. */
+struct Tape {
+    std::vector<uint32_t> mat;
+    std::vector<v3> dlog;
+    double dx = 0, dy = 0, dz = 0;
+    const crg_material *mats = nullptr;
+    double *g_col = nullptr, *g_em = nullptr;
+    void add_factor(uint32_t m, v3 d, double wx, double wy, double wz) {
+        if (wx != 0.0 && d.x != 0.0f) g_col[3 * m + 0] += wx * (double)d.x;
+        if (wy != 0.0 && d.y != 0.0f) g_col[3 * m + 1] += wy * (double)d.y;
+        if (wz != 0.0 && d.z != 0.0f) g_col[3 * m + 2] += wz * (double)d.z;
+    }
+    void emitter(uint32_t m, double wx, double wy, double wz);
+    void path(v3 C, double &wx, double &wy, double &wz) {
+        wx = dx * (double)C.x;
+        wy = dy * (double)C.y;
+        wz = dz * (double)C.z;
+        for (size_t k = 0; k < mat.size(); ++k) add_factor(mat[k], dlog[k], wx, wy, wz);
+    }
+    void mult(uint32_t m, v3 d) {
+        mat.push_back(m);
+        dlog.push_back(d);
+    }
+    void env(v3 C) {
+        double wx, wy, wz;
+        path(C, wx, wy, wz);
+    }
+    void emit(v3 C, uint32_t m) {
+        double wx, wy, wz;
+        path(C, wx, wy, wz);
+        emitter(m, wx, wy, wz);
+    }
+    void nee(v3 C, uint32_t bsdf_mat, v3 bsdf_dlog, uint32_t light_mat) {
+        double wx, wy, wz;
+        path(C, wx, wy, wz);
+        add_factor(bsdf_mat, bsdf_dlog, wx, wy, wz);
+        emitter(light_mat, wx, wy, wz);
+    }
+};
+
+v3 inv_or_zero(v3 c) {
+    return mk(c.x > 0.0f ? 1.0f / c.x : 0.0f, c.y > 0.0f ? 1.0f / c.y : 0.0f, c.z > 0.0f ? 1.0f / c.z : 0.0f);
+}
+
+void Tape::emitter(uint32_t m, double wx, double wy, double wz) {
+    const crg_material &em = mats[m];
+    add_factor(m, inv_or_zero(mk(em.colour[0], em.colour[1], em.colour[2])), wx, wy, wz);
+    if (em.emission > 0.0f) g_em[m] += (wx + wy + wz) / (double)em.emission;
+}
+
 /* ------------------------------------------------------------ extended */
 
 float ggx_D(float nh, float a) { /* sampling.h:93-106 */
@@ -288,11 +343,17 @@ float ggx_lambda(v3 w, float a) {
     const float z2 = w.z * w.z;
     return (std::sqrt(1.0f + ((a * a) * s2) / z2) - 1.0f) * 0.5f;
 }
-v3 schlick(v3 f0, float c) {
+v3 schlick(v3 f0, float c, float *m5_out = nullptr) {
     const float m = 1.0f - clampf(c, 0.0f, 1.0f);
     const float m2 = m * m;
     const float m5 = (m2 * m2) * m;
+    if (m5_out) *m5_out = m5;
     return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+/* d log(Schlick F) / d colour for F0 = colour * reflectiveness */
+v3 schlick_dlog(v3 Fr, float m5, float refl) {
+    const float k = refl * (1.0f - m5);
+    return mk(Fr.x > 0.0f ? k / Fr.x : 0.0f, Fr.y > 0.0f ? k / Fr.y : 0.0f, Fr.z > 0.0f ? k / Fr.z : 0.0f);
 }
 v3 sample_vndf(v3 ve, float a, float u1, float u2) {
     const v3 vh = normalize(mk(a * ve.x, a * ve.y, ve.z));
@@ -333,7 +394,8 @@ uint32_t pick_light(const Scene &S, float u) {
 }
 
 /* Emissive-triangle NEE; bsdf 0 = Lambert (albedo), 1 = GGX (F0, alpha, frame, wol). */
-v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, v3 wol, float alpha) {
+v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, v3 wol, float alpha,
+       Tape *tape = nullptr, uint32_t bsdf_mat = 0, float refl = 1.0f) {
     const Scene &S = *C.S;
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.set->seed);
     const uint32_t j = pick_light(S, g.x);
@@ -360,12 +422,13 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
     const crg_material &lm = S.mats[S.mat_idx[prim]];
     const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
     const float p_light = (S.light_pdf[j] * d2) / cos_l;
-    v3 f;
+    v3 f, bsdf_dlog;
     float p_bsdf, cos_i;
     if (bsdf == 0) {
         f = mul(albedo, kInvPi);
         p_bsdf = cos_s * kInvPi;
         cos_i = cos_s;
+        bsdf_dlog = inv_or_zero(albedo);
     } else {
         const v3 wil = to_local(F, wi);
         if (!(wil.z > 0.0f)) return mk(0, 0, 0);
@@ -375,16 +438,20 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
         const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
         const float G2 = 1.0f / ((1.0f + lo_) + li);
         const float G1 = 1.0f / (1.0f + lo_);
-        const v3 Fr = schlick(albedo, woh);
+        float m5;
+        const v3 Fr = schlick(albedo, woh, &m5);
         f = mul(Fr, (D * G2) / ((4.0f * wol.z) * wil.z));
         p_bsdf = (G1 * D) / (4.0f * wol.z);
         cos_i = wil.z;
+        bsdf_dlog = schlick_dlog(Fr, m5, refl);
     }
     const float w_mis = (p_light * p_light) / (p_light * p_light + p_bsdf * p_bsdf);
-    return mul(mulv(mulv(T, f), Le), (cos_i * w_mis) / p_light);
+    const v3 c_out = mul(mulv(mulv(T, f), Le), (cos_i * w_mis) / p_light);
+    if (tape) tape->nee(c_out, bsdf_mat, bsdf_dlog, S.mat_idx[prim]);
+    return c_out;
 }
 
-v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
+v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
     const Scene &S = *C.S;
     const crg_settings &set = *C.set;
     v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
@@ -397,6 +464,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
             const v3 env = sample_sky(S, d);
             if (i == 0) aov.albedo = env;
             L = add(L, mulv(T, env));
+            if (tape) tape->env(mulv(T, env));
             break;
         }
         const v3 p = add(o, mul(d, h.t));
@@ -422,12 +490,14 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
             const v3 Le = mk(col[0] * m.emission, col[1] * m.emission, col[2] * m.emission);
             if (prev_delta) {
                 L = add(L, mulv(T, Le));
+                if (tape) tape->emit(mulv(T, Le), mi);
             } else {
                 const float cos_l = absf(cos_nd);
                 if (cos_l > 0.0f) {
                     const float pl = (S.mat_light_pdf[mi] * (h.t * h.t)) / cos_l;
                     const float w = (prev_pdf * prev_pdf) / (prev_pdf * prev_pdf + pl * pl);
                     L = add(L, mul(mulv(T, Le), w));
+                    if (tape) tape->emit(mul(mulv(T, Le), w), mi);
                 }
             }
         }
@@ -441,7 +511,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
              * whichever side was hit, as the reference does
              * (renderer.cpp:93-97): the same integral, estimated better. */
             const onb F = build_local(Ng);
-            if (have_lights) L = add(L, nee(C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f));
+            if (have_lights) L = add(L, nee(C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f, tape, mi));
             float sp, cp;
             sincos2pi(g.y, &sp, &cp);
             const float r = std::sqrt(g.x);
@@ -451,6 +521,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
             prev_pdf = l.z * kInvPi;
             prev_delta = false;
             T = mulv(T, rgb);
+            if (tape) tape->mult(mi, inv_or_zero(rgb));
         } else if (m.shade_type == CRG_SHADE_METAL) {
             const v3 f0 = mul(rgb, m.reflectiveness);
             const float alpha = m.roughness;
@@ -459,11 +530,12 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
                 o = add(p, mul(n, 1e-4f));
                 T = mulv(T, f0);
                 prev_delta = true;
+                if (tape) tape->mult(mi, inv_or_zero(rgb));
             } else {
                 const onb F = build_local(n);
                 const v3 wol = to_local(F, wo);
                 if (!(wol.z > 0.0f)) break;
-                if (have_lights) L = add(L, nee(C, i, p, n, T, 1, f0, F, wol, alpha));
+                if (have_lights) L = add(L, nee(C, i, p, n, T, 1, f0, F, wol, alpha, tape, mi, m.reflectiveness));
                 const v3 hh = sample_vndf(wol, alpha, g.x, g.y);
                 const float woh = dot(wol, hh);
                 const float k2 = 2.0f * woh;
@@ -472,8 +544,10 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
                 const float lo_ = ggx_lambda(wol, alpha), li = ggx_lambda(wil, alpha);
                 const float G1 = 1.0f / (1.0f + lo_);
                 const float G2 = 1.0f / ((1.0f + lo_) + li);
-                const v3 Fr = schlick(f0, woh);
+                float m5;
+                const v3 Fr = schlick(f0, woh, &m5);
                 T = mulv(T, mul(Fr, G2 / G1));
+                if (tape) tape->mult(mi, schlick_dlog(Fr, m5, m.reflectiveness));
                 prev_pdf = (G1 * ggx_D(hh.z, alpha)) / (4.0f * wol.z);
                 prev_delta = false;
                 d = from_local(F, wil);
@@ -495,6 +569,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov) {
             }
             T = mulv(T, rgb);
             prev_delta = true;
+            if (tape) tape->mult(mi, inv_or_zero(rgb));
         }
         if (set.rr_depth > 0 && i + 1 >= set.rr_depth) {
             const float q = minf(maxf(maxf(T.x, T.y), T.z), 0.95f);
@@ -679,6 +754,61 @@ int orc_render_rows(const orc_scene_desc *desc, const crg_camera *cam, const crg
     film->render_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     film->segments += seg.load();
     film->shadow_rays += shad.load();
+    orc_bvh_free(bvh);
+    return CRG_OK;
+}
+
+int orc_adjoint(const orc_scene_desc *desc, const crg_camera *cam, const crg_settings *set, const float *adj,
+                double *grad_colour, double *grad_emission, int nthreads) {
+    if (!desc || !cam || !set || !adj || !grad_colour || !grad_emission) return CRG_ERR_INVALID_ARG;
+    if (set->mode != CRG_MODE_EXTENDED) return CRG_ERR_UNSUPPORTED;
+    Scene S;
+    orc_bvh *bvh = nullptr;
+    prepare(*desc, S, &bvh);
+    const CamParams cp = camera_params(*cam);
+    const uint32_t W = set->width, H = set->height, nmat = desc->nmat;
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::vector<std::vector<double>> gc(nthreads, std::vector<double>(3 * (size_t)nmat, 0.0)),
+        ge(nthreads, std::vector<double>(nmat, 0.0));
+    std::atomic<uint64_t> next{0};
+    const uint64_t npix = (uint64_t)W * H;
+    auto work = [&](int tid) {
+        Tape tape;
+        tape.mats = desc->mats;
+        tape.g_col = gc[tid].data();
+        tape.g_em = ge[tid].data();
+        for (;;) {
+            const uint64_t q = next.fetch_add(1);
+            if (q >= npix) break;
+            const uint32_t px = (uint32_t)(q % W), py = (uint32_t)(q / W);
+            const uint32_t pix = py * W + px;
+            const uint64_t fidx = (uint64_t)(W - 1 - px) + (uint64_t)(H - 1 - py) * W;
+            const double inv = 1.0 / (double)set->spp;
+            tape.dx = (double)adj[fidx * 3] * inv;
+            tape.dy = (double)adj[fidx * 3 + 1] * inv;
+            tape.dz = (double)adj[fidx * 3 + 2] * inv;
+            if (tape.dx == 0.0 && tape.dy == 0.0 && tape.dz == 0.0) continue;
+            for (uint32_t s = 0; s < set->spp; ++s) {
+                Ctx C{&S, set, pix, s};
+                const f4 g0 = rand4(pix, s, 0, set->seed);
+                const float x = ((float)px + g0.x) / (float)W;
+                const float y = ((float)py + g0.y) / (float)H;
+                v3 o, d;
+                camera_ray(cp, x, y, set->aspect, o, d);
+                Aov aov;
+                tape.mat.clear();
+                tape.dlog.clear();
+                trace_extended(C, o, d, aov, &tape);
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+    for (auto &t : th) t.join();
+    for (int t = 0; t < nthreads; ++t) {
+        for (size_t k = 0; k < 3 * (size_t)nmat; ++k) grad_colour[k] += gc[t][k];
+        for (size_t k = 0; k < nmat; ++k) grad_emission[k] += ge[t][k];
+    }
     orc_bvh_free(bvh);
     return CRG_OK;
 }
