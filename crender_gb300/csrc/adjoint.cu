@@ -9,13 +9,22 @@
 // one material's colour, times the emitter's colour and emission.  The
 // gradient of <adjoint, pixel mean> with respect to a factor's parameter is
 // therefore the contribution times d log(factor) / d parameter, summed over
-// the factors the contribution carries.  A thread keeps its path's factor list
-// (at most one per bounce) and, at every contribution, adds
-// delta_pixel * contribution * d log(factor) to the gradient of each factor's
-// material: Lambert and glass colour (1 / colour), GGX F0 through Schlick's
+// the factors the contribution carries: every contribution adds
+// delta_pixel * contribution * d log(factor) to the gradient of the material
+// of each factor it carries (at most one factor per bounce): Lambert and glass colour (1 / colour), GGX F0 through Schlick's
 // Fresnel, emitter colour (1 / colour) and emission (1 / emission).
-// Gradients accumulate in FP64: per block in shared memory, then once per
-// block into the caller's arrays.
+// Instead of adding to every factor at every contribution (quadratic in the
+// path length), a thread keeps the running sum Wc of its path's contribution
+// weights (delta_pixel * contribution) and, per factor, the value of Wc when
+// the factor was pushed: the factor's gradient is d log(factor) times the
+// weight that arrived after it (Wc at path end minus that value), added once
+// when the path ends.  A light sample taken at a vertex is shaded after that
+// vertex's factor was pushed but does not carry it (it carries the BSDF
+// evaluated towards the light instead), so its weight is also added to the
+// pushed factor's start value; when both factors are the same (Lambert) the
+// two cancel and nothing is done.  Emitter terms go to a one-entry per-thread
+// cache keyed by the emitter's material.  Gradients accumulate in FP64: per
+// warp in shared memory, then once per block into the caller's arrays.
 #include "render_common.cuh"
 
 namespace crg {
@@ -28,62 +37,105 @@ struct GradTape {
     uint32_t n;
     uint32_t mat[kMaxFactors];
     v3 dlog[kMaxFactors];
-    double dx, dy, dz; // adjoint of the pixel mean / spp, per channel
+    double pre[kMaxFactors][3]; // Wc when the factor was pushed
+    double wc[3];               // weight of the path's contributions so far
+    double dx, dy, dz;          // adjoint of the pixel mean / spp, per channel
+    uint32_t em_mat;            // emitter cache (0xffffffff = empty)
+    double ew[3];
     const crg_material *mats;
     double *g_col, *g_em;
 
-    __device__ __forceinline__ void add_factor(uint32_t m, v3 d, double wx, double wy, double wz) {
+    __device__ __forceinline__ void add3(uint32_t m, v3 d, double wx, double wy, double wz) {
         if (wx != 0.0 && d.x != 0.0f) atomicAdd(&g_col[3 * m + 0], wx * (double)d.x);
         if (wy != 0.0 && d.y != 0.0f) atomicAdd(&g_col[3 * m + 1], wy * (double)d.y);
         if (wz != 0.0 && d.z != 0.0f) atomicAdd(&g_col[3 * m + 2], wz * (double)d.z);
     }
-    __device__ __forceinline__ void emitter(uint32_t m, double wx, double wy, double wz) {
-        const crg_material &em = mats[m];
-        const v3 col = mk(em.colour[0], em.colour[1], em.colour[2]);
-        add_factor(m, inv_or_zero(col), wx, wy, wz);
-        if (em.emission > 0.0f) atomicAdd(&g_em[m], (wx + wy + wz) / (double)em.emission);
+    __device__ __forceinline__ void flush_emitter() {
+        if (em_mat == 0xffffffffu) return;
+        const crg_material &em = mats[em_mat];
+        add3(em_mat, inv_or_zero(mk(em.colour[0], em.colour[1], em.colour[2])), ew[0], ew[1], ew[2]);
+        if (em.emission > 0.0f) atomicAdd(&g_em[em_mat], (ew[0] + ew[1] + ew[2]) / (double)em.emission);
+        em_mat = 0xffffffffu;
     }
-    __device__ __forceinline__ void path(v3 C, double &wx, double &wy, double &wz) {
+    __device__ __forceinline__ void emitter(uint32_t m, double wx, double wy, double wz) {
+        if (m != em_mat) {
+            flush_emitter();
+            em_mat = m;
+            ew[0] = ew[1] = ew[2] = 0.0;
+        }
+        ew[0] += wx;
+        ew[1] += wy;
+        ew[2] += wz;
+    }
+    __device__ __forceinline__ void begin() {
+        n = 0;
+        wc[0] = wc[1] = wc[2] = 0.0;
+    }
+    // Weight of contribution C, added to the running sum.
+    __device__ __forceinline__ void weigh(v3 C, double &wx, double &wy, double &wz) {
         wx = dx * (double)C.x;
         wy = dy * (double)C.y;
         wz = dz * (double)C.z;
-        for (uint32_t k = 0; k < n; ++k) add_factor(mat[k], dlog[k], wx, wy, wz);
+        wc[0] += wx;
+        wc[1] += wy;
+        wc[2] += wz;
     }
     __device__ __forceinline__ void mult(uint32_t m, v3 d) {
         if (n < kMaxFactors) {
             mat[n] = m;
             dlog[n] = d;
+            pre[n][0] = wc[0];
+            pre[n][1] = wc[1];
+            pre[n][2] = wc[2];
             ++n;
         }
     }
     __device__ __forceinline__ void env(v3 C) {
         double wx, wy, wz;
-        path(C, wx, wy, wz);
+        weigh(C, wx, wy, wz);
     }
     __device__ __forceinline__ void emit(v3 C, uint32_t m) {
         double wx, wy, wz;
-        path(C, wx, wy, wz);
+        weigh(C, wx, wy, wz);
         emitter(m, wx, wy, wz);
     }
-    __device__ __forceinline__ void nee(const NeeReq &nr) {
+    // Light sample at the vertex whose factor (if any) has index nf.
+    __device__ __forceinline__ void nee(const NeeReq &nr, uint32_t nf) {
         double wx, wy, wz;
-        path(nr.c, wx, wy, wz);
-        add_factor(nr.bsdf_mat, nr.bsdf_dlog, wx, wy, wz);
+        weigh(nr.c, wx, wy, wz);
         emitter(nr.light_mat, wx, wy, wz);
+        const bool pushed = n > nf;
+        if (pushed && mat[nf] == nr.bsdf_mat && __float_as_uint(dlog[nf].x) == __float_as_uint(nr.bsdf_dlog.x) &&
+            __float_as_uint(dlog[nf].y) == __float_as_uint(nr.bsdf_dlog.y) &&
+            __float_as_uint(dlog[nf].z) == __float_as_uint(nr.bsdf_dlog.z))
+            return;
+        if (pushed) {
+            pre[nf][0] += wx;
+            pre[nf][1] += wy;
+            pre[nf][2] += wz;
+        }
+        add3(nr.bsdf_mat, nr.bsdf_dlog, wx, wy, wz);
+    }
+    // Path end: every factor gets the weight that arrived after it.
+    __device__ __forceinline__ void end() {
+        for (uint32_t k = 0; k < n; ++k)
+            add3(mat[k], dlog[k], wc[0] - pre[k][0], wc[1] - pre[k][1], wc[2] - pre[k][2]);
     }
 };
 
 template <int W>
 __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_settings set, const float *__restrict__ adj,
                                                  double *__restrict__ g_col, double *__restrict__ g_em, uint32_t nmat,
-                                                 int use_shared) {
+                                                 uint32_t copies) {
     extern __shared__ double sh[];
     double *col = g_col, *em = g_em;
-    if (use_shared) {
-        for (uint32_t k = threadIdx.x; k < 4 * nmat; k += blockDim.x) sh[k] = 0.0;
+    const uint32_t nacc = 4 * nmat;
+    if (copies) {
+        for (uint32_t k = threadIdx.x; k < copies * nacc; k += blockDim.x) sh[k] = 0.0;
         __syncthreads();
-        col = sh;
-        em = sh + 3 * nmat;
+        double *mine = sh + (size_t)((threadIdx.x >> 5) % copies) * nacc;
+        col = mine;
+        em = mine + 3 * nmat;
     }
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
@@ -96,6 +148,7 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
         tape.mats = S.mats;
         tape.g_col = col;
         tape.g_em = em;
+        tape.em_mat = 0xffffffffu;
         tape.dx = (double)adj[fidx * 3] * inv;
         tape.dy = (double)adj[fidx * 3 + 1] * inv;
         tape.dz = (double)adj[fidx * 3 + 2] * inv;
@@ -110,27 +163,31 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
             PathState ps;
             path_start(ps, o, d);
             Aov aov;
-            tape.n = 0;
+            tape.begin();
             for (uint32_t i = 0; i < set.max_bounces; ++i) {
                 Hit h;
                 const bool found = closest<W, false>(S, ps.o, ps.d, INFINITY, h, C);
                 NeeReq nr;
+                const uint32_t nf = tape.n;
                 const bool cont = shade_extended(S, set, C, i, ps, found, h, aov, nr, &tape);
                 if (nr.kind != 0 && shadow_visible<W, false>(S, nr, C)) {
                     ps.L = add(ps.L, nr.c);
-                    tape.nee(nr);
+                    tape.nee(nr, nf);
                 }
                 if (!cont) break;
             }
+            tape.end();
         }
+        tape.flush_emitter();
     }
     if (C.err) atomicOr(S.err, C.err);
-    if (use_shared) {
+    if (copies) {
         __syncthreads();
-        for (uint32_t k = threadIdx.x; k < 3 * nmat; k += blockDim.x)
-            if (sh[k] != 0.0) atomicAdd(&g_col[k], sh[k]);
-        for (uint32_t k = threadIdx.x; k < nmat; k += blockDim.x)
-            if (sh[3 * nmat + k] != 0.0) atomicAdd(&g_em[k], sh[3 * nmat + k]);
+        for (uint32_t k = threadIdx.x; k < nacc; k += blockDim.x) {
+            double v = 0.0;
+            for (uint32_t c = 0; c < copies; ++c) v += sh[(size_t)c * nacc + k];
+            if (v != 0.0) atomicAdd(k < 3 * nmat ? &g_col[k] : &g_em[k - 3 * nmat], v);
+        }
     }
 }
 
@@ -142,13 +199,14 @@ crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &
     const uint32_t T = 128;
     const uint64_t npix = (uint64_t)set.width * set.height;
     const uint32_t blocks = (uint32_t)((npix + T - 1) / T);
-    const size_t shmem = sizeof(double) * 4 * (size_t)s->nmat;
-    const int use_shared = shmem <= 48 * 1024 ? 1 : 0;
-    const size_t dyn = use_shared ? shmem : 0;
+    // one FP64 accumulator copy per warp when it fits in 48 KB, else one per block, else global atomics
+    const size_t per_copy = sizeof(double) * 4 * (size_t)s->nmat;
+    const uint32_t copies = per_copy * (T / 32) <= 48 * 1024 ? T / 32 : (per_copy <= 48 * 1024 ? 1 : 0);
+    const size_t dyn = per_copy * copies;
     switch (s->width) {
-    case 2: k_adjoint<2><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, use_shared); break;
-    case 4: k_adjoint<4><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, use_shared); break;
-    default: k_adjoint<8><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, use_shared); break;
+    case 2: k_adjoint<2><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
+    case 4: k_adjoint<4><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
+    default: k_adjoint<8><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(s->ctx, e, "k_adjoint launch");

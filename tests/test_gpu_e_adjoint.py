@@ -99,7 +99,8 @@ def test_matches_finite_differences_and_cost(ctx):
             fm = float(np.dot(adj.astype(np.float64), P.render(P.bwd, f64=True)))
             P.set_mats(sc["mats"])
             fd = (fp - fm) / (2 * h)
-            assert abs(gc[m, c] - fd) <= 1e-3 * abs(gc[m, c]) + 1e-3 * np.abs(gc).max() * 1e-3, (m, c, gc[m, c], fd)
+            assert abs(gc[m, c]) > 1e-6 * np.abs(gc).max()
+            assert abs(gc[m, c] - fd) <= 1e-3 * abs(gc[m, c]), (m, c, gc[m, c], fd)
             checked += 1
         assert checked == 8
         # cost: backward / forward at the same spp
@@ -124,13 +125,17 @@ def test_adam_recovers_parameters(ctx):
     true_sc = scenes.inverse_box()
     T = Problem(ctx, true_sc, spp=1024, seed_fwd=77)
     tgt = T.render(T.fwd, f64=True)
+    T.fwd.spp, T.fwd.seed = 32, 5
+    img = T.render(T.fwd)
+    floor = float(np.mean((img - tgt) ** 2))  # 32-spp noise at the true parameters
     T.close()
     sc = _init_scene()
     P = Problem(ctx, sc, rr=3)
     theta = np.concatenate([np.full(34 * 3, 0.5), np.full(3, 10 / 17)])
+    hi = np.concatenate([np.ones(102), np.full(3, 4.0)])
     m1, m2 = np.zeros_like(theta), np.zeros_like(theta)
     lr, b1, b2 = 0.02, 0.9, 0.999
-    losses = []
+    losses, seen = [], None
     try:
         for it in range(200):
             mats = scenes.inverse_box(albedo=theta[:102].reshape(34, 3), light_colour=theta[102:])["mats"]
@@ -139,16 +144,20 @@ def test_adam_recovers_parameters(ctx):
             img = P.render(P.fwd)
             diff = img - tgt
             losses.append(float(np.mean(diff * diff)))
-            gc, ge = P.backward((2.0 * diff / img.size).astype(np.float32))
+            gc, _ = P.backward((2.0 * diff / img.size).astype(np.float32))
             g = np.concatenate([gc[:34].ravel(), gc[34]])
+            if seen is None:
+                seen = np.abs(g[:102]) > 1e-3 * np.abs(g[:102]).max()
             m1 = b1 * m1 + (1 - b1) * g
             m2 = b2 * m2 + (1 - b2) * g * g
-            step = lr * (m1 / (1 - b1 ** (it + 1))) / (np.sqrt(m2 / (1 - b2 ** (it + 1))) + 1e-8)
-            theta = np.clip(theta - step, 1e-3, np.concatenate([np.ones(102), np.full(3, 4.0)]))
-        assert np.mean(losses[-10:]) < 0.2 * losses[0], (losses[0], losses[-10:])
-        err0 = np.abs(0.5 - true_sc["true_albedo"]).mean()
-        err1 = np.abs(theta[:102].reshape(34, 3) - true_sc["true_albedo"]).mean()
-        assert err1 < 0.6 * err0, (err0, err1)
-        assert np.abs(theta[102:] - 1.0).max() < np.abs(10 / 17 - 1.0)
+            step = lr * (m1 / (1 - b1 ** (it + 1))) / (np.sqrt(m2 / (1 - b2 ** (it + 1))) + 1e-12)
+            theta = np.clip(theta - step, 1e-3, hi)
+        final = float(np.mean(losses[-10:]))
+        assert final - floor < 0.1 * (losses[0] - floor), (losses[0], final, floor)
+        truth = true_sc["true_albedo"].ravel()
+        err0 = np.abs(0.5 - truth)[seen].mean()
+        err1 = np.abs(theta[:102] - truth)[seen].mean()
+        assert err1 < 0.5 * err0, (err0, err1)
+        assert np.abs(theta[102:] - 1.0).max() < 0.5 * abs(10 / 17 - 1.0), theta[102:]
     finally:
         P.close()
