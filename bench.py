@@ -2,7 +2,7 @@
 """Benchmark of the render hot path through the C ABI (libcrg.so).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl crg|reference]
-                    [--workload batch|box|displaced|soup]
+                    [--workload batch|box|displaced|soup|inverse]
 
 Workloads (seeded synthetic inputs; no external data):
   batch      (default) 64 views drawn from the box and displaced scenes with
@@ -16,6 +16,12 @@ Workloads (seeded synthetic inputs; no external data):
   displaced  the displaced icosphere (4,196,562 triangles), 1920x1080, 16 of the
              256 spp per step (a frame is 16 steps), depth 16, megakernel.
   soup       1,048,576-triangle soup, 16,777,216 closest-hit rays.  Mrays/s.
+  inverse    inverse rendering of the box scene (34 per-triangle albedos + light
+             radiance), 256x256: a step is one forward (32 spp), the L2 loss
+             against a 4096-spp target and one path-replay backward (32 spp).
+             Msamples/s over forward + backward samples; also reports the
+             backward/forward time ratio, central-FD agreement (h = 1e-3,
+             common random numbers) and a 200-step Adam run (lr 0.02).
 
 `value` is device-timed (CUDA events on the launching stream; inputs resident;
 L2 flushed by a 256 MiB write between steps, outside the events).  `e2e` runs
@@ -118,6 +124,10 @@ def workload_config(w):
     if w == "displaced":
         return {"workload": "displaced icosphere (4,196,562 tris) 1920x1080, 16 spp per step, depth 16, RR from 3, "
                             "extended estimator, megakernel", "l2": L2_NOTE}
+    if w == "inverse":
+        return {"workload": "inverse rendering, box scene with 34 per-triangle albedos + light radiance, 256x256, "
+                            "32 spp forward + L2 loss vs a 4096-spp target + 32 spp path-replay backward, depth 8, "
+                            "RR from 3", "resolution": [256, 256], "spp_forward": 32, "spp_backward": 32, "l2": L2_NOTE}
     return {"workload": "soup 1,048,576 tris, 16,777,216 closest-hit rays per step, BVH width 8", "l2": L2_NOTE}
 
 
@@ -142,6 +152,16 @@ def cpu_leg(workload):
         b.closest(rays)
         dt = time.perf_counter() - t0
         return (1 << 18) / dt / 1e6, f"262,144 of the 16,777,216 primary rays on the soup ({dt:.1f} s)"
+    if workload == "inverse":
+        sc = scenes.inverse_box(albedo=np.full((34, 3), 0.5), light_colour=np.full(3, 10 / 17))
+        st = api.make_settings(64, 64, 32, 8, 3, 1, 1)
+        f = orc.render(sc, sc["camera"], st)
+        adj = np.random.default_rng(0).uniform(-1, 1, 64 * 64 * 3).astype(np.float32)
+        t0 = time.perf_counter()
+        orc.adjoint(sc, sc["camera"], st, adj)
+        dt = f["render_seconds"] + time.perf_counter() - t0
+        n = 2 * 64 * 64 * 32
+        return n / dt / 1e6, f"forward + adjoint of the inverse box at 64x64x32 spp ({n} samples, {dt:.1f} s)"
     n_tot, t_tot, parts = 0, 0.0, []
     if workload in ("box", "batch"):
         sc = scenes.box_scene()
@@ -231,6 +251,131 @@ def time_to_rmse(ctx, api, scenes, timer, stream, target=1e-2):
             "megakernel_s": t_mega / 1e3, "wavefront_s": t_wave / 1e3}
 
 
+def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
+    """Forward / loss / backward step of the inverse-rendering problem, plus FD
+    agreement and an Adam run through the public calls."""
+    W, SPP = 256, 32
+    true_sc = scenes.inverse_box()
+    init = scenes.inverse_box(albedo=np.full((34, 3), 0.5), light_colour=np.full(3, 10 / 17))
+    scene = api.Scene(ctx, init["verts"], init["mat_idx"], init["mats"]).build(8, 1)
+    cam = init["camera"]
+    nmat, npx = len(init["mats"]), W * W * 3
+    # target: 4096 spp of the true parameters, FP64 film
+    api.set_materials(scene, true_sc["mats"])
+    tf = api.Film(ctx, W, W, f64=True)
+    api.render(scene, cam, api.make_settings(W, W, 4096, 8, 3, 1, 4242), tf, S)
+    target = (tf.download(f64=True)["sum64"] / 4096).astype(np.float32)
+    tf.close()
+    api.set_materials(scene, init["mats"])
+    tb = api.DeviceBuffer.from_array(ctx, target)
+    ab, lb = api.DeviceBuffer(ctx, npx * 4), api.DeviceBuffer(ctx, 8)
+    gc, ge = api.DeviceBuffer(ctx, nmat * 24), api.DeviceBuffer(ctx, nmat * 8)
+    film = api.Film(ctx, W, W)
+    fwd = api.make_settings(W, W, SPP, 8, 3, 1, 1)
+    bwd = api.make_settings(W, W, SPP, 8, 3, 1, 2)
+
+    def forward():
+        film.reset(S)
+        api.render(scene, cam, fwd, film, S)
+        api.loss_l2(film, tb, ab, lb, S)
+
+    def backward():
+        api.backward(scene, cam, bwd, ab, gc, ge, S)
+
+    def step():
+        forward()
+        backward()
+
+    # traversal work of the backward pass (the forward with the backward's random numbers traces the same paths)
+    scene.set_counting(True)
+    film.reset(S)
+    api.render(scene, cam, bwd, film, S)
+    torch.cuda.synchronize()
+    work = scene.stats()
+    scene.set_counting(False)
+    units = 2 * W * W * SPP
+    algo = 2 * (work["nodes_visited"] * 80 + work["tris_tested"] * 48) + W * W * 12 * 4
+    with ClockSampler(env_rank()[2]) as clk:
+        ms = timer.steps(step, args.steps, args.warmup)
+    f_ms = timer.steps(forward, 3, 1)
+    b_ms = timer.steps(backward, 3, 1)
+    out["work"] = {**work, "note": "counted on the forward with the backward's random numbers (same paths)"}
+    out["forward_ms"] = statistics.median(f_ms)
+    out["backward_ms"] = statistics.median(b_ms)
+    out["backward_over_forward"] = out["backward_ms"] / out["forward_ms"]
+
+    # central differences with common random numbers (roulette off) against the adjoint
+    f64film = api.Film(ctx, W, W, f64=True)
+    st0 = api.make_settings(W, W, SPP, 8, 0, 1, 7)
+    f64film.reset(S)
+    api.render(scene, cam, st0, f64film, S)
+    img = f64film.download(f64=True)["sum64"] / SPP
+    adj = (2.0 * (img - target) / npx).astype(np.float32)
+    ab.upload(adj)
+    gc.upload(np.zeros(nmat * 3))
+    ge.upload(np.zeros(nmat))
+    api.backward(scene, cam, st0, ab, gc, ge, S)
+    g = gc.download(np.zeros(nmat * 3)).reshape(nmat, 3)
+    h, rel = 1e-3, []
+    for m, c in [(0, 0), (6, 1), (14, 2), (26, 0), (34, 1)]:
+        vals = []
+        for sgn in (1, -1):
+            mats = init["mats"].copy()
+            mats[m]["colour"][c] += sgn * h
+            api.set_materials(scene, mats)
+            f64film.reset(S)
+            api.render(scene, cam, st0, f64film, S)
+            vals.append(float(np.dot(adj.astype(np.float64), f64film.download(f64=True)["sum64"] / SPP)))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        rel.append(abs(g[m, c] - fd) / max(abs(fd), 1e-30))
+    api.set_materials(scene, init["mats"])
+    f64film.close()
+    out["fd_check"] = {"params": 5, "h": h, "max_rel_err": max(rel), "spp": SPP, "resolution": [W, W],
+                       "rr": "off", "random_numbers": "common (same seed for +h, -h and the adjoint)"}
+
+    # e2e: Adam through the public calls, host parameters, per-step uploads and gradient downloads
+    theta = np.concatenate([np.full(102, 0.5), np.full(3, 10 / 17)])
+    hi = np.concatenate([np.ones(102), np.full(3, 4.0)])
+    m1, m2 = np.zeros_like(theta), np.zeros_like(theta)
+    zc, ze, lh = np.zeros(nmat * 3), np.zeros(nmat), np.zeros(1)
+    losses = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(200):
+        mats = scenes.inverse_box(albedo=theta[:102].reshape(34, 3), light_colour=theta[102:])["mats"]
+        api.set_materials(scene, mats)
+        fwd.seed, bwd.seed = 1000 + 2 * it, 1001 + 2 * it
+        gc.upload(zc, S)
+        ge.upload(ze, S)
+        forward()
+        backward()
+        lb.download(lh, S)
+        grad = gc.download(zc.copy(), S)[:105]  # 34 albedos (RGB) then the light colour
+        losses.append(float(lh[0]))
+        m1 = 0.9 * m1 + 0.1 * grad
+        m2 = 0.999 * m2 + 0.001 * grad * grad
+        theta = np.clip(theta - 0.02 * (m1 / (1 - 0.9 ** (it + 1))) / (np.sqrt(m2 / (1 - 0.999 ** (it + 1))) + 1e-12),
+                        1e-3, hi)
+    torch.cuda.synchronize()
+    adam_s = time.perf_counter() - t0
+    truth = true_sc["true_albedo"].ravel()
+    out["adam"] = {"steps": 200, "lr": 0.02, "seconds": adam_s, "loss_first": losses[0],
+                   "loss_last10_mean": float(np.mean(losses[-10:])),
+                   "albedo_mae_first": float(np.abs(0.5 - truth).mean()),
+                   "albedo_mae_last": float(np.abs(theta[:102] - truth).mean()),
+                   "light_radiance_last": (17 * theta[102:]).tolist(), "light_radiance_true": 17.0}
+    h2d = nmat * 48 + nmat * 24 + nmat * 8
+    out["e2e"] = {"value": units * world / (adam_s / 200) / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": 8 + nmat * 24, "ms_per_step": adam_s / 200 * 1e3,
+                  "path": "crg_scene_set_materials (host table) + crg_render + crg_film_loss_l2 + crg_backward + "
+                          "loss and gradient downloads + host Adam update, 200 iterations"}
+    for b in (tb, ab, lb, gc, ge):
+        b.free()
+    film.close()
+    scene.close()
+    return units, algo, "k_render + k_loss_l2 + k_adjoint (one forward/backward step)", 3 * args.steps, clk, ms
+
+
 # ---------------------------------------------------------------- GPU leg
 def main():
     ap = argparse.ArgumentParser()
@@ -238,7 +383,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="crg", choices=["crg", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup", "inverse"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE leg")
     ap.add_argument("--form", default="megakernel", choices=["megakernel", "wavefront"],
@@ -420,6 +565,8 @@ def main():
                               + ("crg_render" if args.form == "megakernel" else "crg_render_batch") + " + crg_film_download"}
         if args.workload == "box" and not args.no_rmse:
             out["time_to_rmse"] = time_to_rmse(ctx, api, scenes, timer, S)
+    elif args.workload == "inverse":
+        units, algo, kernel, launches, clk, ms = inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch)
     else:
         v = scenes.soup(1 << 20, 1)
         scene = api.Scene(ctx, v, np.zeros(len(v), np.uint32), scenes.material_table([{}])).build()

@@ -169,6 +169,7 @@ CRG_SIGNATURES = [
     ("crg_render", C.c_int, [vp, P(Camera), P(Settings), vp, c_stream]),
     ("crg_scene_set_materials", C.c_int, [vp, vp, C.c_uint32]),
     ("crg_backward", C.c_int, [vp, P(Camera), P(Settings), vp, vp, vp, c_stream]),
+    ("crg_film_loss_l2", C.c_int, [vp, vp, vp, vp, c_stream]),
     ("crg_render_batch", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
     ("crg_batch_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),

@@ -265,3 +265,24 @@ def batch_stats(ctx) -> dict:
     ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))
     return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays, nodes_visited=s.nodes_visited,
                 tris_tested=s.tris_tested, iterations=s.iterations)
+
+
+# ---------------------------------------------------------------- differentiation
+def set_materials(scene: Scene, mats: np.ndarray):
+    """crg_scene_set_materials: same count, BVH kept, emitter table rebuilt."""
+    mats = np.ascontiguousarray(mats)
+    scene.ctx.check(scene.ctx.lib.crg_scene_set_materials(scene.h, ptr(mats), len(mats)))
+    scene.mats = mats
+
+
+def loss_l2(film: Film, target: DeviceBuffer, adjoint: DeviceBuffer, loss: DeviceBuffer, stream=None):
+    """crg_film_loss_l2: loss = mean (I - T)^2 into `loss` (double), dLoss/dI into `adjoint` (float)."""
+    film.ctx.check(film.ctx.lib.crg_film_loss_l2(film.h, target.ptr, adjoint.ptr, loss.ptr, stream))
+
+
+def backward(scene: Scene, camera: dict, settings: _abi.Settings, adjoint: DeviceBuffer, grad_colour: DeviceBuffer,
+             grad_emission: DeviceBuffer, stream=None):
+    """crg_backward: adds d<adjoint, I>/d(colour, emission) into the two device double arrays."""
+    cam = make_camera(camera)
+    scene.ctx.check(scene.ctx.lib.crg_backward(scene.h, C.byref(cam), C.byref(settings), adjoint.ptr,
+                                               grad_colour.ptr, grad_emission.ptr, stream))

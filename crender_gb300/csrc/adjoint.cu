@@ -191,7 +191,41 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
     }
 }
 
+// Block sums of (I - T)^2 in FP64, one atomic per block; d_adjoint written alongside.
+__global__ void __launch_bounds__(256) k_loss_l2(const float *__restrict__ sum, float inv_spp, const float *__restrict__ tgt,
+                                                 float *__restrict__ adj, double *__restrict__ loss, uint64_t n, float scale,
+                                                 double inv_n) {
+    __shared__ double part[8];
+    double acc = 0.0;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const float d = sum[k] * inv_spp - tgt[k];
+        adj[k] = d * scale;
+        acc += (double)d * (double)d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        atomicAdd(loss, t * inv_n);
+    }
+}
+
 } // namespace
+
+crg_status launch_loss_l2(crg_film *f, const float *target, float *adj, double *loss, cudaStream_t st) {
+    const uint64_t n = (uint64_t)f->width * f->height * 3;
+    CRG_CUDA(f->ctx, cudaMemsetAsync(loss, 0, sizeof(double), st));
+    const uint32_t T = 256;
+    const uint64_t want = (n + T - 1) / T;
+    const uint32_t blocks = (uint32_t)(want < 4096 ? want : 4096);
+    k_loss_l2<<<blocks, T, 0, st>>>((const float *)f->sum.ptr, 1.0f / (float)f->spp, target, adj, loss, n,
+                                    2.0f / (float)n, 1.0 / (double)n);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(f->ctx, e, "k_loss_l2 launch");
+    return CRG_OK;
+}
 
 crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &set, const float *adj, double *g_col,
                            double *g_em, cudaStream_t st) {

@@ -686,6 +686,13 @@ crg_status crg_backward(crg_scene *scene, const crg_camera *camera, const crg_se
     return launch_backward(scene, camera_params(*camera), s, d_adjoint, d_grad_colour, d_grad_emission, (cudaStream_t)stream);
 }
 
+crg_status crg_film_loss_l2(crg_film *film, const float *d_target, float *d_adjoint, double *d_loss, crg_stream stream) {
+    if (!film || !d_target || !d_adjoint || !d_loss)
+        return set_error(film ? film->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
+    if (film->spp == 0) return set_error(film->ctx, CRG_ERR_INVALID_ARG, "film holds no samples");
+    return launch_loss_l2(film, d_target, d_adjoint, d_loss, (cudaStream_t)stream);
+}
+
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats) {
     if (!scene || !stats) return CRG_ERR_INVALID_ARG;
     *stats = scene->last_stats;

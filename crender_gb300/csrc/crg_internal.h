@@ -99,6 +99,7 @@ crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &se
 // adjoint.cu
 crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &set, const float *adj, double *g_col,
                            double *g_em, cudaStream_t stream);
+crg_status launch_loss_l2(crg_film *f, const float *target, float *adj, double *loss, cudaStream_t stream);
 
 // wavefront.cu
 crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,

@@ -370,6 +370,15 @@ crg_status crg_backward(crg_scene *scene, const crg_camera *camera, const crg_se
                         const float *d_adjoint, double *d_grad_colour, double *d_grad_emission,
                         crg_stream stream);
 
+/* Image loss of a forward pass, the link between crg_render and crg_backward:
+ * with I = film sum / film spp (FP32 sum plane) and T = d_target (device
+ * float[W*H*3], film layout),
+ *   *d_loss    = mean over the W*H*3 values of (I - T)^2       (device double, overwritten)
+ *   d_adjoint  = dLoss/dI = 2 (I - T) / (W*H*3)               (device float[W*H*3], overwritten)
+ * No reference counterpart (the reference renderer has no differentiation). */
+crg_status crg_film_loss_l2(crg_film *film, const float *d_target, float *d_adjoint, double *d_loss,
+                            crg_stream stream);
+
 /* Statistics of the last render on this scene (renderer::current_stats,
  * renderer.cpp:396-404): segments traced (the reference's ray count,
  * renderer.cpp:271-272/356) and shadow rays traced. */

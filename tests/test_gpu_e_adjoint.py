@@ -33,7 +33,7 @@ class Problem:
         self.cam = api.make_camera(sc["camera"])
 
     def set_mats(self, mats):
-        self.ctx.check(self.ctx.lib.crg_scene_set_materials(self.scene.h, _abi.ptr(mats), len(mats)))
+        api.set_materials(self.scene, mats)
 
     def render(self, st, f64=False):
         self.film.reset()
@@ -46,8 +46,7 @@ class Problem:
         zeros_c, zeros_e = np.zeros(self.nmat * 3), np.zeros(self.nmat)
         self.gc.upload(zeros_c)
         self.ge.upload(zeros_e)
-        self.ctx.check(self.ctx.lib.crg_backward(self.scene.h, C.byref(self.cam), C.byref(self.bwd), self.adj.ptr,
-                                                 self.gc.ptr, self.ge.ptr, None))
+        api.backward(self.scene, self.sc["camera"], self.bwd, self.adj, self.gc, self.ge)
         return self.gc.download(zeros_c).reshape(self.nmat, 3), self.ge.download(zeros_e)
 
     def close(self):
@@ -160,4 +159,26 @@ def test_adam_recovers_parameters(ctx):
         assert err1 < 0.5 * err0, (err0, err1)
         assert np.abs(theta[102:] - 1.0).max() < 0.5 * abs(10 / 17 - 1.0), theta[102:]
     finally:
+        P.close()
+
+
+def test_loss_l2_matches_numpy(ctx):
+    sc = scenes.box_scene()
+    P = Problem(ctx, dict(sc), W=64, spp=8)
+    tb, ab, lb = api.DeviceBuffer(ctx, 64 * 64 * 12), api.DeviceBuffer(ctx, 64 * 64 * 12), api.DeviceBuffer(ctx, 8)
+    try:
+        P.film.reset()
+        api.render(P.scene, sc["camera"], P.fwd, P.film)
+        tgt = np.random.default_rng(4).uniform(0, 1, 64 * 64 * 3).astype(np.float32)
+        tb.upload(tgt)
+        api.loss_l2(P.film, tb, ab, lb)
+        adj = ab.download(np.zeros(64 * 64 * 3, np.float32))
+        loss = lb.download(np.zeros(1))[0]
+        img = P.film.download()["sum"]
+        d = img * (np.float32(1) / np.float32(8)) - tgt
+        assert np.array_equal(adj, d * np.float32(2.0 / d.size))
+        assert loss == pytest.approx(float(np.mean(d.astype(np.float64) ** 2)), rel=1e-12)
+    finally:
+        for b in (tb, ab, lb):
+            b.free()
         P.close()
