@@ -154,14 +154,14 @@ def cpu_leg(workload):
         return (1 << 18) / dt / 1e6, f"262,144 of the 16,777,216 primary rays on the soup ({dt:.1f} s)"
     if workload == "inverse":
         sc = scenes.inverse_box(albedo=np.full((34, 3), 0.5), light_colour=np.full(3, 10 / 17))
-        st = api.make_settings(64, 64, 32, 8, 3, 1, 1)
+        st = api.make_settings(256, 256, 32, 8, 3, 1, 1)
         f = orc.render(sc, sc["camera"], st)
-        adj = np.random.default_rng(0).uniform(-1, 1, 64 * 64 * 3).astype(np.float32)
+        adj = np.random.default_rng(0).uniform(-1, 1, 256 * 256 * 3).astype(np.float32)
         t0 = time.perf_counter()
         orc.adjoint(sc, sc["camera"], st, adj)
         dt = f["render_seconds"] + time.perf_counter() - t0
-        n = 2 * 64 * 64 * 32
-        return n / dt / 1e6, f"forward + adjoint of the inverse box at 64x64x32 spp ({n} samples, {dt:.1f} s)"
+        n = 2 * 256 * 256 * 32
+        return n / dt / 1e6, f"one full forward + adjoint step of the inverse box, 256x256x32 spp ({n} samples, {dt:.2f} s)"
     n_tot, t_tot, parts = 0, 0.0, []
     if workload in ("box", "batch"):
         sc = scenes.box_scene()

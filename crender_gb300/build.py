@@ -30,6 +30,24 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+HOST = os.path.join(ROOT, "host")
+CXX = os.environ.get("CXX", "g++")
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "..", "include")]
+
+
+def build_host(libcrg: str) -> str:
+    """libcrg_host.so (the C++ adapter: crg::host::scene / camera / renderer)
+    and crg_host_selftest, linked against libcrg.so with an $ORIGIN rpath."""
+    so = os.path.join(OUT, "libcrg_host.so")
+    exe = os.path.join(OUT, "crg_host_selftest")
+    link = ["-L", OUT, "-lcrg", "-Wl,-rpath,$ORIGIN", "-pthread"]
+    log = _run([CXX, *CXXFLAGS, "-shared", os.path.join(HOST, "crg_host.cpp"), "-o", so + ".tmp", *link])
+    os.replace(so + ".tmp", so)
+    log += _run([CXX, *CXXFLAGS, os.path.join(HOST, "selftest.cpp"), "-o", exe + ".tmp", "-lcrg_host", *link])
+    os.replace(exe + ".tmp", exe)
+    return log
+
+
 def build(verbose: bool = False, ptxas_v: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_v else []
@@ -52,6 +70,7 @@ def build(verbose: bool = False, ptxas_v: bool = False) -> str:
     tmp = lib + ".tmp"
     _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
     os.replace(tmp, lib)
+    logs.append(build_host(lib))
     log = "".join(logs)
     if verbose:
         sys.stdout.write(log)

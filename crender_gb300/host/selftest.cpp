@@ -1,0 +1,137 @@
+// selftest.cpp — drives crg::host::scene / renderer the way the reference's
+// UI drives cr::scene / cr::renderer, on a scene read from a file, and writes
+// what it saw for the tests to compare with direct ABI calls.
+//
+//   crg_host_selftest <in> <out>
+// in : u32 magic 0x54475243, ntri, nmat, W, H, spp, bounces, mode, nrays, nsplit;
+//      float verts[ntri*9]; u32 mat_idx[ntri]; crg_material mats[nmat];
+//      crg_camera cam; crg_ray rays[nrays]
+//      (triangles [0, nsplit) and [nsplit, ntri) go in as two models, indexed)
+// out: u64 spp1; float sums1[W*H*3]; u64 spp2; float sums2[W*H*3];
+//      u64 total_rays; per ray: u32 prim, float distance, float normal[3]
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "crg_host.h"
+
+using namespace crg::host;
+
+namespace {
+
+template <class T> bool rd(FILE *f, T *p, size_t n) { return n == 0 || std::fread(p, sizeof(T), n, f) == n; }
+template <class T> void wr(FILE *f, const T *p, size_t n) { if (n) std::fwrite(p, sizeof(T), n, f); }
+
+model_data make_model(const std::vector<float> &v, const std::vector<uint32_t> &mi, const std::vector<crg_material> &mats,
+                      size_t t0, size_t t1) {
+    model_data m;
+    m.name = "part";
+    // indexed the way an OBJ loader produces it: vertices listed in reverse, indices pointing back
+    const size_t nt = t1 - t0;
+    m.vertices.resize(nt * 3);
+    for (size_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const float *p = &v[(t0 + t) * 9 + k * 3];
+            m.vertices[nt * 3 - 1 - (t * 3 + k)] = vec3{p[0], p[1], p[2]};
+            m.vertex_indices.push_back((uint32_t)(nt * 3 - 1 - (t * 3 + k)));
+        }
+    for (const crg_material &c : mats) {
+        material_information info;
+        info.shade_type = (material_information::type)c.shade_type;
+        info.ior = c.ior;
+        info.roughness = c.roughness;
+        info.reflectiveness = c.reflectiveness;
+        info.emission = c.emission;
+        std::memcpy(info.colour, c.colour, sizeof(info.colour));
+        m.materials.push_back(info);
+    }
+    for (size_t t = t0; t < t1; ++t) m.material_indices.push_back(mi[t]);
+    return m;
+}
+
+} // namespace
+
+int main(int argc, char **argv) {
+    if (argc != 3) {
+        std::fprintf(stderr, "usage: %s <in> <out>\n", argv[0]);
+        return 2;
+    }
+    FILE *f = std::fopen(argv[1], "rb");
+    if (!f) return 2;
+    uint32_t h[10];
+    if (!rd(f, h, 10) || h[0] != 0x54475243u) return 2;
+    const uint32_t ntri = h[1], nmat = h[2], W = h[3], H = h[4], spp = h[5], bounces = h[6], mode = h[7], nrays = h[8],
+                   nsplit = h[9];
+    std::vector<float> verts((size_t)ntri * 9);
+    std::vector<uint32_t> mat_idx(ntri);
+    std::vector<crg_material> mats(nmat);
+    crg_camera cam;
+    std::vector<crg_ray> rays(nrays);
+    if (!rd(f, verts.data(), verts.size()) || !rd(f, mat_idx.data(), ntri) || !rd(f, mats.data(), nmat) ||
+        !rd(f, &cam, 1) || !rd(f, rays.data(), nrays))
+        return 2;
+    std::fclose(f);
+    try {
+        scene sc(0);
+        // the second model's material indices are relative to its own table
+        std::vector<uint32_t> mi2(mat_idx);
+        sc.add_model(make_model(verts, mat_idx, mats, 0, nsplit));
+        if (nsplit < ntri) sc.add_model(make_model(verts, mi2, mats, nsplit, ntri));
+        sc.set_sun_enabled(false);
+        camera *c = sc.camera();
+        c->fov = cam.fov;
+        c->current_mode = cam.mode == CRG_CAMERA_PERSPECTIVE ? camera::mode::perspective : camera::mode::orthographic;
+        c->scale = cam.scale;
+        c->rotate(vec3{cam.rotation[0], cam.rotation[1], cam.rotation[2]});
+        c->position = vec3{cam.position[0], cam.position[1], cam.position[2]};
+
+        renderer::options o;
+        o.mode = mode;
+        o.target_spp = spp;
+        renderer r(W, H, bounces, &sc, o);
+        if (!r.wait_for_target(120.0)) {
+            std::fprintf(stderr, "target spp not reached\n");
+            return 1;
+        }
+        const uint64_t spp1 = r.current_sample_count();
+        const std::vector<float> s1 = r.current_sums();
+        const image *prog = r.current_progress();
+        if (!prog->valid()) {
+            std::fprintf(stderr, "no progress image\n");
+            return 1;
+        }
+        // update(): pause, change the depth, restart from an empty film
+        r.update([&] { r.set_max_bounces((int)bounces / 2); });
+        if (!r.wait_for_target(120.0)) {
+            std::fprintf(stderr, "target spp not reached after update()\n");
+            return 1;
+        }
+        const uint64_t spp2 = r.current_sample_count();
+        const std::vector<float> s2 = r.current_sums();
+        const uint64_t total_rays = r.current_stats().total_rays;
+
+        std::vector<ray> rr(nrays);
+        for (uint32_t i = 0; i < nrays; ++i)
+            rr[i] = ray{vec3{rays[i].org[0], rays[i].org[1], rays[i].org[2]},
+                        vec3{rays[i].dir[0], rays[i].dir[1], rays[i].dir[2]}};
+        const std::vector<intersection_record> recs = sc.cast_rays(rr);
+        FILE *g = std::fopen(argv[2], "wb");
+        if (!g) return 2;
+        wr(g, &spp1, 1);
+        wr(g, s1.data(), s1.size());
+        wr(g, &spp2, 1);
+        wr(g, s2.data(), s2.size());
+        wr(g, &total_rays, 1);
+        for (const intersection_record &rec : recs) {
+            const uint32_t prim = rec.material ? rec.prim_id : CRG_INVALID_PRIM;
+            const float row[4] = {rec.distance, rec.normal.x, rec.normal.y, rec.normal.z};
+            wr(g, &prim, 1);
+            wr(g, row, 4);
+        }
+        std::fclose(g);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "selftest: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

@@ -105,3 +105,17 @@ def test_null_arguments_are_rejected(lib):
     assert lib.crg_intersect_closest(None, None, None, 0, None) == 1
     lib.crg_film_spp.argtypes = [C.c_void_p, C.c_void_p]
     assert lib.crg_film_spp(None, None) == 1
+
+
+def test_host_adapter_built():
+    """The C++ adapter library and its self-test program are built and link;
+    the program rejects bad arguments before touching a device."""
+    import subprocess
+
+    root = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "crender_gb300", "_build")
+    assert os.path.exists(os.path.join(root, "libcrg_host.so"))
+    exe = os.path.join(root, "crg_host_selftest")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exe, "/nonexistent/in", "/nonexistent/out"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
