@@ -637,7 +637,7 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         for (uint32_t u = 0; u < v; ++u)
             if (films[u] == films[v]) return set_error(ctx, CRG_ERR_INVALID_ARG, "films must be distinct");
     }
-    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0, 0, 0};
+    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0, 0, 0, 1};
     if (opts) {
         if (opts->path_pool) o.path_pool = opts->path_pool;
         if (opts->chunk_samples) o.chunk_samples = opts->chunk_samples;
@@ -646,10 +646,12 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         o.max_iterations = opts->max_iterations;
         o.count_work = opts->count_work;
         o.host_loop = opts->host_loop;
+        if (opts->fuse) o.fuse = opts->fuse;
     }
     if ((o.block_size != 64 && o.block_size != 128 && o.block_size != 256) || o.fetch % 32 || o.fetch > 4096 ||
-        o.path_pool > (1u << 28))
-        return set_error(ctx, CRG_ERR_INVALID_ARG, "wavefront options: block_size 64/128/256, fetch a multiple of 32");
+        o.path_pool > (1u << 28) || o.fuse > 3)
+        return set_error(ctx, CRG_ERR_INVALID_ARG,
+                         "wavefront options: block_size 64/128/256, fetch a multiple of 32, path_pool <= 2^28, fuse <= 3");
     return render_batch(ctx, scenes, nscenes, views, films, nviews, o, (cudaStream_t)stream, &ctx->batch_stats);
 }
 

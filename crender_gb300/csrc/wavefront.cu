@@ -198,8 +198,21 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
     }
 }
 
-template <int W>
+// Warp-aggregated count of flagged lanes (shadow rays traced inside a fused shade kernel).
+__device__ __forceinline__ void warp_count(bool want, unsigned int *count) {
+    const uint32_t active = __activemask();
+    const uint32_t m = __ballot_sync(active, want);
+    if (m && (threadIdx.x & 31) == (uint32_t)(__ffs(m) - 1)) atomicAdd(count, (unsigned int)__popc(m));
+}
+
+// FUSE 0: shade only (hits from k_wf_extend, shadow rays to the shadow queue)
+// FUSE 1: shade + the NEE shadow test in the same thread (no shadow queue)
+// FUSE 2: closest hit + shade + shadow test (one kernel per bounce)
+// Contributions reach L in the same order in every form: emission of bounce
+// i, its NEE, then bounce i + 1.
+template <int W, int FUSE, bool CNT>
 __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
+    unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
     const uint32_t *in = q_in(w, *c);
@@ -221,7 +234,16 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                 const uint32_t view = m.x & 0xFFFFu, depth = (m.x >> 16) & 0x3FFu;
                 const ViewDev &V = w.views[view];
                 const SceneDev &S = w.scenes[V.scene];
-                const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot], h4 = w.hit[slot];
+                const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot];
+                PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
+                float4 h4;
+                if (FUSE >= 2) {
+                    Hit hh;
+                    const bool f = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
+                    h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), f ? 1.0f : 0.0f);
+                } else {
+                    h4 = w.hit[slot];
+                }
                 PathState ps;
                 ps.o = mk(o.x, o.y, o.z);
                 ps.d = mk(d.x, d.y, d.z);
@@ -234,7 +256,6 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                 h.prim = __float_as_uint(h4.y);
                 h.slot = __float_as_uint(h4.z);
                 h.u = h.v = 0.0f;
-                PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
                 Aov aov;
                 NeeReq nr;
                 nr.kind = 0;
@@ -246,17 +267,23 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                                : shade_faithful(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr);
                 }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
+                shadow = nr.kind != 0;
+                if (FUSE >= 1 && shadow && shadow_visible<W, CNT>(S, nr, C)) ps.L = add(ps.L, nr.c);
+                if (C.err) atomicOr(&c->error, 1u);
+                if (CNT) {
+                    nodes += C.nodes;
+                    tris += C.tris;
+                }
                 Lv = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
                 w.L[slot] = Lv;
                 off = m.w;
-                shadow = nr.kind != 0;
-                if (shadow) {
+                if (FUSE == 0 && shadow) {
                     w.sh_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.tmax);
                     w.sh_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, __uint_as_float(nr.kind));
                     w.sh_c[slot] = make_float4(nr.c.x, nr.c.y, nr.c.z, 0.0f);
                 }
                 uint32_t mx_ = (m.x & 0xFFFFu) | ((depth + 1) << 16) | (ps.prev_delta ? kPrevDelta : 0u);
-                if (!cont && shadow) mx_ |= kFinish;
+                if (FUSE == 0 && !cont && shadow) mx_ |= kFinish;
                 m.x = mx_;
                 w.meta[slot] = m;
                 if (cont) {
@@ -264,12 +291,17 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                     w.d[slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, 0.0f);
                     w.T[slot] = make_float4(ps.T.x, ps.T.y, ps.T.z, ps.prev_pdf);
                 }
-                finishing = !cont && !shadow;
+                finishing = !cont && (FUSE >= 1 || !shadow);
             }
-            warp_push(valid && shadow, slot, w.qsh, &c->sh_count);
+            if (FUSE == 0) warp_push(valid && shadow, slot, w.qsh, &c->sh_count);
+            else warp_count(valid && shadow, &c->sh_count);
             warp_push(valid && cont, slot, q_out(w, *c), &c->out_count);
             finish_and_refill(w, c, valid && finishing, slot, Lv, off);
         }
+    }
+    if (CNT && FUSE >= 1) {
+        atomicAdd(&c->nodes, nodes);
+        atomicAdd(&c->tris, tris);
     }
 }
 
@@ -452,18 +484,24 @@ struct Workspace {
 
 size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 
+// The per-bounce kernels of one loop iteration for a fusion level.
+template <int W, int FUSE, bool CNT>
+void launch_bounce(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
+    if (FUSE <= 1) k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
+    k_wf_shade<W, FUSE, CNT><<<grid, block, 0, st>>>(wf);
+    if (FUSE == 0) k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+}
+
 // Host-driven loop: the same kernels launched from the host, which polls the
 // done flag every 8 iterations (for profilers that cannot see into graphs
 // with conditional nodes, and for runtimes without them).
-template <int W, bool CNT>
+template <int W, int FUSE, bool CNT>
 crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
     unsigned int *done_h = nullptr;
     CRG_CUDA(ctx, cudaHostAlloc(&done_h, sizeof(unsigned int), cudaHostAllocDefault));
     crg_status rc = CRG_OK;
     for (uint32_t it = 0; it < max_iters + 8; ++it) {
-        k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
-        k_wf_shade<W><<<grid, block, 0, st>>>(wf);
-        k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+        launch_bounce<W, FUSE, CNT>(wf, grid, block, st);
         k_wf_control<<<1, 32, 0, st>>>(wf, 0, 0);
         k_wf_resolve<<<grid, 256, 0, st>>>(wf);
         k_wf_generate<<<grid, 256, 0, st>>>(wf, 0);
@@ -482,7 +520,7 @@ crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t bloc
     return rc;
 }
 
-template <int W, bool CNT>
+template <int W, int FUSE, bool CNT>
 crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st,
                bool host_loop) {
     // prologue on the caller's stream
@@ -490,7 +528,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
     k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
     k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
     CRG_CUDA(ctx, cudaGetLastError());
-    if (host_loop) return run_host<W, CNT>(ctx, wf, grid, block, max_iters, st);
+    if (host_loop) return run_host<W, FUSE, CNT>(ctx, wf, grid, block, max_iters, st);
     // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -523,9 +561,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
             rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
             break;
         }
-        k_wf_extend<W, CNT><<<grid, block, 0, cap>>>(wf);
-        k_wf_shade<W><<<grid, block, 0, cap>>>(wf);
-        k_wf_shadow<W, CNT><<<grid, block, 0, cap>>>(wf);
+        launch_bounce<W, FUSE, CNT>(wf, grid, block, cap);
         k_wf_control<<<1, 32, 0, cap>>>(wf, handle, 1);
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
@@ -541,6 +577,55 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
     if (graph) cudaGraphDestroy(graph);
     if (cap) cudaStreamDestroy(cap);
     return rc;
+}
+
+template <int W, int FUSE>
+int occupancy_of(int block) {
+    int a = 0, b = 0, c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shade<W, FUSE, false>, block, 0);
+    a = b;
+    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false>, block, 0) == cudaSuccess)
+        a = std::min(a, c);
+    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false>, block, 0) == cudaSuccess)
+        a = std::min(a, c);
+    cudaGetLastError();
+    return std::max(a, 1);
+}
+
+int occupancy(uint32_t width, uint32_t fuse, int block) {
+    switch (width * 4 + fuse) {
+    case 8: return occupancy_of<2, 0>(block);
+    case 9: return occupancy_of<2, 1>(block);
+    case 10: return occupancy_of<2, 2>(block);
+    case 16: return occupancy_of<4, 0>(block);
+    case 17: return occupancy_of<4, 1>(block);
+    case 18: return occupancy_of<4, 2>(block);
+    case 32: return occupancy_of<8, 0>(block);
+    case 33: return occupancy_of<8, 1>(block);
+    default: return occupancy_of<8, 2>(block);
+    }
+}
+
+template <int W>
+crg_status dispatch_w(crg_context *ctx, const Wf &wf, uint32_t fuse, bool cnt, uint32_t grid, uint32_t block,
+                      uint32_t max_iters, cudaStream_t st, bool hl) {
+    switch (fuse * 2 + (cnt ? 1 : 0)) {
+    case 0: return run<W, 0, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 1: return run<W, 0, true>(ctx, wf, grid, block, max_iters, st, hl);
+    case 2: return run<W, 1, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 3: return run<W, 1, true>(ctx, wf, grid, block, max_iters, st, hl);
+    case 4: return run<W, 2, false>(ctx, wf, grid, block, max_iters, st, hl);
+    default: return run<W, 2, true>(ctx, wf, grid, block, max_iters, st, hl);
+    }
+}
+
+crg_status dispatch(crg_context *ctx, const Wf &wf, uint32_t width, uint32_t fuse, bool cnt, uint32_t grid,
+                    uint32_t block, uint32_t max_iters, cudaStream_t st, bool hl) {
+    switch (width) {
+    case 2: return dispatch_w<2>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
+    case 4: return dispatch_w<4>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
+    default: return dispatch_w<8>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
+    }
 }
 
 } // namespace
@@ -647,13 +732,9 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     CRG_CUDA(ctx, cudaMemcpyAsync(d_vd, vdev.data(), sizeof(ViewDev) * nviews, cudaMemcpyHostToDevice, st));
     CRG_CUDA(ctx, cudaMemcpyAsync(d_sg, segs.data(), sizeof(Segment) * segs.size(), cudaMemcpyHostToDevice, st));
     CRG_CUDA(ctx, cudaMemcpyAsync(d_ch, chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, st));
-    // persistent grid: resident blocks of the heaviest kernel on every SM
-    int per_sm = 0;
-    cudaError_t e;
-    if (width == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<2>, (int)o.block_size, 0);
-    else if (width == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<4>, (int)o.block_size, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<8>, (int)o.block_size, 0);
-    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    // persistent grid: resident blocks of the launched kernels on every SM
+    const uint32_t fuse = o.fuse ? o.fuse - 1 : 0; // fusion level 0..2
+    int per_sm = occupancy(width, fuse, (int)o.block_size);
     const uint32_t grid = (uint32_t)(std::max(ctx->sm_count, 1) * per_sm);
     // every chunk needs at most (samples / P + 1) refills of max_bounces + 1 iterations
     unsigned long long iters = 16;
@@ -663,11 +744,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
     if (o.max_iterations) max_iters = o.max_iterations;
     const bool cnt = o.count_work != 0, hl = o.host_loop != 0;
-    switch (width) {
-    case 2: rc = cnt ? run<2, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<2, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
-    case 4: rc = cnt ? run<4, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<4, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
-    default: rc = cnt ? run<8, true>(ctx, wf, grid, o.block_size, max_iters, st, hl) : run<8, false>(ctx, wf, grid, o.block_size, max_iters, st, hl); break;
-    }
+    rc = dispatch(ctx, wf, width, fuse, cnt, grid, o.block_size, max_iters, st, hl);
     if (rc != CRG_OK) return rc;
     Ctrl host{};
     CRG_CUDA(ctx, cudaMemcpyAsync(&host, wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));

@@ -331,6 +331,10 @@ typedef struct crg_wavefront_opts {
                                nodes visited and triangles tested */
     uint32_t host_loop;     /* 1 = drive the loop from the host instead of one graph with a
                                device-side condition (same kernels; for profilers) */
+    uint32_t fuse;          /* stage fusion (films are identical for every value):
+                               1 = separate extend / shade / shadow kernels and queues;
+                               2 = the shadow test runs inside shade (no shadow queue);
+                               3 = extend + shade + shadow in one kernel per bounce */
 } crg_wavefront_opts;
 
 /* Renders every view of a batch in one launch of the wavefront form (one CUDA

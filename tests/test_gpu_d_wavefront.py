@@ -33,7 +33,10 @@ def _same(a, b):
 
 @pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
 @pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64),
-                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1)])
+                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1),
+                                  dict(path_pool=1000, chunk_samples=5000, fuse=2),
+                                  dict(path_pool=1000, chunk_samples=5000, fuse=3, fetch=32, block_size=256),
+                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1, fuse=3)])
 def test_single_view_matches_megakernel(ctx, mode, rr, opts):
     sc = _box_variant("materials")
     s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
@@ -63,14 +66,18 @@ def test_batch_of_uneven_views_and_scenes(ctx):
     ]
     try:
         refs = [_mega(ctx, (sa, sb)[si], cam, st) for si, cam, st in views]
-        films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
-        ctx.check(api.render_batch([sa, sb], views, films, dict(path_pool=2048, chunk_samples=4096)))
-        for f, r in zip(films, refs):
-            _same(f.download(f64=True), r)
-            f.close()
-        stats = api.batch_stats(ctx)
-        assert stats["samples"] == sum(st.width * st.height * st.spp for _, _, st in views)
-        assert stats["segments"] >= stats["samples"]
+        counts = set()
+        for fuse in (1, 2, 3):
+            films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
+            ctx.check(api.render_batch([sa, sb], views, films, dict(path_pool=2048, chunk_samples=4096, fuse=fuse)))
+            for f, r in zip(films, refs):
+                _same(f.download(f64=True), r)
+                f.close()
+            stats = api.batch_stats(ctx)
+            assert stats["samples"] == sum(st.width * st.height * st.spp for _, _, st in views)
+            assert stats["segments"] >= stats["samples"]
+            counts.add((stats["segments"], stats["shadow_rays"]))
+        assert len(counts) == 1, counts  # same rays traced at every fusion level
     finally:
         sa.close()
         sb.close()
