@@ -85,7 +85,7 @@ class View(C.Structure):
 class WavefrontOpts(C.Structure):
     _fields_ = [("path_pool", C.c_uint32), ("chunk_samples", C.c_uint32), ("block_size", C.c_uint32),
                 ("fetch", C.c_uint32), ("max_iterations", C.c_uint32), ("count_work", C.c_uint32),
-                ("host_loop", C.c_uint32), ("fuse", C.c_uint32)]
+                ("host_loop", C.c_uint32), ("fuse", C.c_uint32), ("refill", C.c_uint32)]
 
 
 class RenderStats(C.Structure):

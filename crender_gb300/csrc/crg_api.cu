@@ -637,7 +637,9 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         for (uint32_t u = 0; u < v; ++u)
             if (films[u] == films[v]) return set_error(ctx, CRG_ERR_INVALID_ARG, "films must be distinct");
     }
-    crg_wavefront_opts o{1u << 22, 1u << 25, 128, 64, 0, 0, 0, 1};
+    // defaults: 32M paths in flight (about 5 GB of path state), 128M-sample chunks (2 GB of
+    // sample slots), split stages with per-lane refill in the traversal stages
+    crg_wavefront_opts o{1u << 25, 1u << 27, 128, 32, 0, 0, 0, 1, 16};
     if (opts) {
         if (opts->path_pool) o.path_pool = opts->path_pool;
         if (opts->chunk_samples) o.chunk_samples = opts->chunk_samples;
@@ -647,11 +649,13 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         o.count_work = opts->count_work;
         o.host_loop = opts->host_loop;
         if (opts->fuse) o.fuse = opts->fuse;
+        if (opts->refill) o.refill = opts->refill == 0xFFFFFFFFu ? 0u : opts->refill;
     }
     if ((o.block_size != 64 && o.block_size != 128 && o.block_size != 256) || o.fetch % 32 || o.fetch > 4096 ||
-        o.path_pool > (1u << 28) || o.fuse > 3)
+        o.path_pool > (1u << 28) || o.fuse > 3 || o.refill > 32)
         return set_error(ctx, CRG_ERR_INVALID_ARG,
-                         "wavefront options: block_size 64/128/256, fetch a multiple of 32, path_pool <= 2^28, fuse <= 3");
+                         "wavefront options: block_size 64/128/256, fetch a multiple of 32, path_pool <= 2^28, fuse <= 3, "
+                         "refill <= 32");
     return render_batch(ctx, scenes, nscenes, views, films, nviews, o, (cudaStream_t)stream, &ctx->batch_stats);
 }
 

@@ -405,4 +405,55 @@ __device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const 
     occluded = T.occluded;
 }
 
+// Persistent traversal with per-lane ray refill (the "dynamic fetch" of Aila
+// & Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
+// A warp runs the loop with all lanes converged; a lane whose query is done
+// takes the next index from *head (one atomic per refill, for all idle lanes
+// at once) as soon as at least `min_refill` lanes are idle, so long queries
+// no longer hold the short ones' lanes idle.  Between refill checks each busy
+// lane advances its query by up to STEPS node visits.
+//   fetch(idx, payload&, r&, tmax&, nodes&, tris&) -> bool: loads query idx;
+//        false = the query was completed inside fetch (no traversal needed)
+//   done(payload, const Trav&): consumes a finished query
+template <int W, bool ANY, bool COUNT, int STEPS, class Fetch, class Done>
+__device__ __forceinline__ void dyn_traverse(unsigned int *head, unsigned int n, uint32_t min_refill, Fetch &&fetch,
+                                             Done &&done, TravStats &st, uint32_t &err) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool has = false, exhausted = false;
+    uint32_t payload = 0;
+    RayPre r;
+    Trav T;
+    uint2 stack[kStack];
+    const uint4 *nodes = nullptr;
+    const float4 *tris = nullptr;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !has);
+        if (!exhausted && idle != 0u && ((uint32_t)__popc(idle) >= min_refill || idle == 0xFFFFFFFFu)) {
+            const uint32_t cnt = (uint32_t)__popc(idle);
+            unsigned int base = 0;
+            if (lane == 0) base = atomicAdd(head, cnt);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + cnt >= n) exhausted = true;
+            if (!has) {
+                const unsigned int my = base + (unsigned int)__popc(idle & ((1u << lane) - 1u));
+                if (my < n) {
+                    float tmax;
+                    if (fetch(my, payload, r, tmax, nodes, tris)) {
+                        trav_init(T, r, tmax);
+                        has = true;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, has)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (has && trav_step<W, ANY, COUNT>(T, stack, nodes, tris, r, STEPS, st, err)) {
+            has = false;
+            done(payload, T);
+        }
+    }
+}
+
 } // namespace crg

@@ -79,7 +79,10 @@ struct Wf {
     const ViewDev *views;
     const Segment *segs;
     const Chunk *chunks;
-    uint32_t nchunks, P, fetch, pad_;
+    uint32_t nchunks, P, fetch;
+    uint32_t refill;       // extend: 0 = static fetch of `fetch` entries, else the per-lane refill threshold
+    uint32_t refill_sh;    // shadow: the same (0 when a batch can produce sun requests)
+    uint32_t pad_[3];
     float4 *o, *d, *T, *L; // T.w = prev_pdf
     uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
     float4 *hit;           // t, prim bits, triangle slot bits, found
@@ -357,6 +360,78 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
     }
 }
 
+// Extend with per-lane ray refill (dyn_traverse): the same hits as k_wf_extend.
+template <int W, bool CNT>
+__global__ void __launch_bounds__(256) k_wf_extend_dyn(Wf w) {
+    Ctrl *c = w.ctrl;
+    const unsigned int n = c->in_count;
+    const uint32_t *in = q_in(w, *c);
+    TravStats st{0, 0};
+    uint32_t err = 0;
+    dyn_traverse<W, false, CNT, 4>(
+        &c->head_ext, n, w.refill,
+        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
+            slot = in[qi];
+            const SceneDev &S = w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene];
+            nodes = S.nodes;
+            tris = S.tris;
+            const float4 o = w.o[slot], d = w.d[slot];
+            r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+            tmax = INFINITY;
+            return true;
+        },
+        [&](uint32_t slot, const Trav &T) {
+            const bool found = T.best_prim != 0xFFFFFFFFu;
+            w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot), found ? 1.0f : 0.0f);
+        },
+        st, err);
+    if (err) atomicOr(&c->error, 1u);
+    if (CNT) {
+        atomicAdd(&c->nodes, (unsigned long long)st.nodes);
+        atomicAdd(&c->tris, (unsigned long long)st.tris);
+    }
+}
+
+// Shadow tests with per-lane ray refill, for batches whose shadow requests
+// are all emitter tests (any hit below tmax); sun requests (faithful
+// estimator with the sun on) go through k_wf_shadow.
+template <int W, bool CNT>
+__global__ void __launch_bounds__(256) k_wf_shadow_dyn(Wf w) {
+    Ctrl *c = w.ctrl;
+    const unsigned int n = c->sh_count;
+    TravStats st{0, 0};
+    uint32_t err = 0;
+    dyn_traverse<W, true, CNT, 4>(
+        &c->head_sh, n, w.refill_sh,
+        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
+            slot = w.qsh[qi];
+            const SceneDev &S = w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene];
+            const float4 so = w.sh_o[slot], sd = w.sh_d[slot];
+            nodes = S.nodes;
+            tris = S.tris;
+            r = ray_prep(so.x, so.y, so.z, sd.x, sd.y, sd.z, 1e-5f);
+            tmax = so.w;
+            return true;
+        },
+        [&](uint32_t slot, const Trav &T) {
+            const uint4 m = w.meta[slot];
+            float4 Lv = w.L[slot];
+            if (!T.occluded) {
+                const float4 sc = w.sh_c[slot];
+                const v3 L = add(mk(Lv.x, Lv.y, Lv.z), mk(sc.x, sc.y, sc.z));
+                Lv = make_float4(L.x, L.y, L.z, 0.0f);
+                w.L[slot] = Lv;
+            }
+            finish_and_refill(w, c, (m.x & kFinish) != 0u, slot, Lv, m.w);
+        },
+        st, err);
+    if (err) atomicOr(&c->error, 1u);
+    if (CNT) {
+        atomicAdd(&c->nodes, (unsigned long long)st.nodes);
+        atomicAdd(&c->tris, (unsigned long long)st.tris);
+    }
+}
+
 __global__ void k_wf_control(Wf w, cudaGraphConditionalHandle handle, int in_graph) {
     if (threadIdx.x != 0) return;
     Ctrl *c = w.ctrl;
@@ -487,9 +562,15 @@ size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 // The per-bounce kernels of one loop iteration for a fusion level.
 template <int W, int FUSE, bool CNT>
 void launch_bounce(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
-    if (FUSE <= 1) k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
+    if (FUSE <= 1) {
+        if (wf.refill) k_wf_extend_dyn<W, CNT><<<grid, block, 0, st>>>(wf);
+        else k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
+    }
     k_wf_shade<W, FUSE, CNT><<<grid, block, 0, st>>>(wf);
-    if (FUSE == 0) k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+    if (FUSE == 0) {
+        if (wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<grid, block, 0, st>>>(wf);
+        else k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+    }
 }
 
 // Host-driven loop: the same kernels launched from the host, which polls the
@@ -586,7 +667,11 @@ int occupancy_of(int block) {
     a = b;
     if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
+    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false>, block, 0) == cudaSuccess)
+        a = std::min(a, c);
     if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false>, block, 0) == cudaSuccess)
+        a = std::min(a, c);
+    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     cudaGetLastError();
     return std::max(a, 1);
@@ -715,6 +800,11 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.nchunks = (uint32_t)chunks.size();
     wf.P = P;
     wf.fetch = o.fetch;
+    wf.refill = o.refill;
+    bool sun_requests = false; // the faithful estimator's sun test steps through alpha surfaces
+    for (uint32_t v = 0; v < nviews; ++v)
+        if (vdev[v].set.mode == CRG_MODE_FAITHFUL && scenes[vdev[v].scene]->sun_enabled) sun_requests = true;
+    wf.refill_sh = sun_requests ? 0u : o.refill;
     wf.o = (float4 *)take(n_f4);
     wf.d = (float4 *)take(n_f4);
     wf.T = (float4 *)take(n_f4);

@@ -321,20 +321,25 @@ typedef struct crg_view {
 /* Wavefront knobs (the autotuner's search space besides the BVH width).
  * Zero fields take the defaults. */
 typedef struct crg_wavefront_opts {
-    uint32_t path_pool;     /* paths in flight (default 4,194,304) */
-    uint32_t chunk_samples; /* samples resolved into the films per chunk (default 33,554,432) */
+    uint32_t path_pool;     /* paths in flight (default 33,554,432; at most the chunk's samples) */
+    uint32_t chunk_samples; /* samples resolved into the films per chunk (default 134,217,728) */
     uint32_t block_size;    /* threads per block of the persistent kernels: 64, 128 or 256 (default 128) */
-    uint32_t fetch;         /* queue entries a warp takes per atomic, multiple of 32 (default 64) */
+    uint32_t fetch;         /* queue entries a warp takes per atomic, multiple of 32 (default 32) */
     uint32_t max_iterations;/* cap on the device-side loop (0 = a bound derived from the batch);
                                reaching it ends the frame with CRG_ERR_TIMEOUT */
     uint32_t count_work;    /* 1 = instrumented kernels: crg_batch_stats_get also reports
                                nodes visited and triangles tested */
     uint32_t host_loop;     /* 1 = drive the loop from the host instead of one graph with a
                                device-side condition (same kernels; for profilers) */
-    uint32_t fuse;          /* stage fusion (films are identical for every value):
+    uint32_t fuse;          /* stage fusion (films are identical for every value; default 1):
                                1 = separate extend / shade / shadow kernels and queues;
                                2 = the shadow test runs inside shade (no shadow queue);
                                3 = extend + shade + shadow in one kernel per bounce */
+    uint32_t refill;        /* traversal stages (extend, shadow): 1..32 = per-lane refill: a
+                               lane whose ray is done takes a new one as soon as this many
+                               lanes of its warp are idle (dynamic fetch; default 16);
+                               0xFFFFFFFF = off: each warp takes `fetch` queue entries and
+                               runs them to completion */
 } crg_wavefront_opts;
 
 /* Renders every view of a batch in one launch of the wavefront form (one CUDA

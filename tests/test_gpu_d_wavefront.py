@@ -32,11 +32,17 @@ def _same(a, b):
 
 
 @pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
-@pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64),
-                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1),
+OFF = 0xFFFFFFFF  # refill off: static per-warp fetch
+
+
+@pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64, refill=OFF),
+                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1, refill=OFF, fetch=64),
                                   dict(path_pool=1000, chunk_samples=5000, fuse=2),
                                   dict(path_pool=1000, chunk_samples=5000, fuse=3, fetch=32, block_size=256),
-                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1, fuse=3)])
+                                  dict(path_pool=4096, chunk_samples=20000, host_loop=1, fuse=3),
+                                  dict(path_pool=1000, chunk_samples=5000, refill=8),
+                                  dict(path_pool=1000, chunk_samples=5000, refill=1, fuse=2, block_size=256),
+                                  dict(path_pool=4096, chunk_samples=20000, refill=32, host_loop=1)])
 def test_single_view_matches_megakernel(ctx, mode, rr, opts):
     sc = _box_variant("materials")
     s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
@@ -69,7 +75,8 @@ def test_batch_of_uneven_views_and_scenes(ctx):
         counts = set()
         for fuse in (1, 2, 3):
             films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
-            ctx.check(api.render_batch([sa, sb], views, films, dict(path_pool=2048, chunk_samples=4096, fuse=fuse)))
+            ctx.check(api.render_batch([sa, sb], views, films, dict(path_pool=2048, chunk_samples=4096, fuse=fuse,
+                                                                     refill=(OFF, 4, 8)[fuse - 1])))
             for f, r in zip(films, refs):
                 _same(f.download(f64=True), r)
                 f.close()
@@ -81,6 +88,25 @@ def test_batch_of_uneven_views_and_scenes(ctx):
     finally:
         sa.close()
         sb.close()
+
+
+@pytest.mark.parametrize("refill", [OFF, 8])
+def test_faithful_sun_matches_megakernel(ctx, refill):
+    """Sun requests (closest hits stepping past alpha-zero surfaces) keep the
+    static shadow stage even when per-lane refill is asked for."""
+    sc = _box_variant("materials")
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    s.set_sun(True, dict(direction=(0.3, -1.0, 0.2)))
+    st = api.make_settings(32, 24, 5, max_bounces=6, rr_depth=0, mode=0, seed=4, aspect=32 / 24)
+    try:
+        ref = _mega(ctx, s, sc["camera"], st)
+        assert ref["sum"].sum() > 0
+        f = api.Film(ctx, 32, 24, f64=True)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], dict(refill=refill, path_pool=700)))
+        _same(f.download(f64=True), ref)
+        f.close()
+    finally:
+        s.close()
 
 
 def test_accumulates_after_megakernel_passes(ctx):
