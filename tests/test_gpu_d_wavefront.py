@@ -31,10 +31,10 @@ def _same(a, b):
         assert bad == 0, f"{k}: {bad} values differ"
 
 
-@pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
 OFF = 0xFFFFFFFF  # refill off: static per-warp fetch
 
 
+@pytest.mark.parametrize("mode,rr", [(1, 3), (0, 0)])
 @pytest.mark.parametrize("opts", [None, dict(path_pool=1000, chunk_samples=5000, fetch=32, block_size=64, refill=OFF),
                                   dict(path_pool=4096, chunk_samples=20000, host_loop=1, refill=OFF, fetch=64),
                                   dict(path_pool=1000, chunk_samples=5000, fuse=2),
