@@ -88,6 +88,15 @@ class WavefrontOpts(C.Structure):
                 ("host_loop", C.c_uint32), ("fuse", C.c_uint32), ("refill", C.c_uint32)]
 
 
+class AutotuneOpts(C.Structure):
+    _fields_ = [("sample_budget", C.c_uint64), ("widths", C.c_uint32), ("reuse", C.c_uint32)]
+
+
+class AutotuneTrial(C.Structure):
+    _fields_ = [("opts", WavefrontOpts), ("width", C.c_uint32), ("ms", C.c_float), ("msamples_per_s", C.c_float),
+                ("pad_", C.c_uint32)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("segments", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("iterations", C.c_uint64)]
@@ -172,6 +181,8 @@ CRG_SIGNATURES = [
     ("crg_film_loss_l2", C.c_int, [vp, vp, vp, vp, c_stream]),
     ("crg_render_batch", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
     ("crg_batch_stats_get", C.c_int, [vp, P(RenderStats)]),
+    ("crg_autotune_batch", C.c_int, [P(vp), C.c_uint32, P(View), C.c_uint32, P(AutotuneOpts), P(WavefrontOpts),
+                                     P(C.c_uint32), P(AutotuneTrial), C.c_uint32, P(C.c_uint32), c_stream]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_scene_set_counting", C.c_int, [vp, C.c_int]),
 ]

@@ -260,6 +260,31 @@ def render_batch(scenes, views, films, opts=None, stream=None):
     return ctx.lib.crg_render_batch(sc, len(scenes), vs, fl, len(views), C.byref(o), stream)
 
 
+OPT_FIELDS = ("path_pool", "chunk_samples", "block_size", "fetch", "max_iterations", "count_work", "host_loop", "fuse",
+              "refill")
+
+
+def autotune_batch(scenes, views, sample_budget=0, widths=0, reuse=True, stream=None):
+    """crg_autotune_batch: returns (options dict for render_batch, BVH width, trials list)."""
+    ctx = scenes[0].ctx
+    sc = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
+    vs = (_abi.View * len(views))()
+    for i, (si, cam, st) in enumerate(views):
+        vs[i].scene = si
+        vs[i].camera = make_camera(cam)
+        vs[i].settings = st
+    o = _abi.AutotuneOpts(int(sample_budget), int(widths), int(bool(reuse)))
+    best, width, n = _abi.WavefrontOpts(), C.c_uint32(), C.c_uint32()
+    cap = 64
+    trials = (_abi.AutotuneTrial * cap)()
+    ctx.check(ctx.lib.crg_autotune_batch(sc, len(scenes), vs, len(views), C.byref(o), C.byref(best), C.byref(width),
+                                         trials, cap, C.byref(n), stream))
+    opts = {k: getattr(best, k) for k in OPT_FIELDS}
+    log = [dict({k: getattr(t.opts, k) for k in OPT_FIELDS}, width=t.width, ms=t.ms, msamples_per_s=t.msamples_per_s)
+           for t in trials[:min(n.value, cap)]]
+    return opts, width.value, log
+
+
 def batch_stats(ctx) -> dict:
     s = _abi.RenderStats()
     ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))

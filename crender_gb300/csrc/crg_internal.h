@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -20,6 +21,11 @@ struct crg_context {
     int sm_count = 0;
     DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
     crg_render_stats batch_stats{};
+    struct Tuned {
+        crg_wavefront_opts opts;
+        uint32_t width;
+    };
+    std::map<std::string, Tuned> tune_cache; // autotuner results by batch shape
 };
 
 struct crg_scene {

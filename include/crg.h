@@ -355,6 +355,36 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
                             crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
                             crg_stream stream);
 
+/* Autotuner of the wavefront form.  Renders a reduced copy of the batch (each
+ * view's spp scaled down so the trial holds about sample_budget samples, into
+ * scratch films) under candidate settings and keeps the fastest by device
+ * time: BVH width (the scenes are rebuilt with their build options at each
+ * width tried, and left built at the winner), stage fusion, per-lane refill,
+ * queue fetch size, block size and path pool, searched one knob at a time
+ * from the defaults.  Every candidate renders identical films, so the choice
+ * only trades speed.  Results are cached in the context by batch shape. */
+typedef struct crg_autotune_opts {
+    uint64_t sample_budget; /* samples per trial batch (0 = 134,217,728) */
+    uint32_t widths;        /* BVH widths to try, bit mask of 2 | 4 | 8 (0 = keep the scenes' width) */
+    uint32_t reuse;         /* 1 = return the cached result for a batch of the same shape */
+} crg_autotune_opts;
+
+typedef struct crg_autotune_trial {
+    crg_wavefront_opts opts;
+    uint32_t width;
+    float ms;               /* device time of the trial batch */
+    float msamples_per_s;
+    uint32_t pad_;
+} crg_autotune_trial;
+
+/* Writes the best options to *best and the BVH width to *best_width (scenes
+ * are left built at it); up to trials_cap trials to `trials` (may be NULL)
+ * and their count to *ntrials (may be NULL; 0 when the cache answered). */
+crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, uint32_t nviews,
+                              const crg_autotune_opts *opts, crg_wavefront_opts *best, uint32_t *best_width,
+                              crg_autotune_trial *trials, uint32_t trials_cap, uint32_t *ntrials,
+                              crg_stream stream);
+
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replaces the material table (same count, e.g. after an optimiser step)

@@ -164,3 +164,34 @@ def test_displaced_scene_small(ctx, orc):
     o = orc.render(sc, sc["camera"], st, skybox=sc["skybox"])
     _same(ref, o)
     assert np.isfinite(ref["sum"]).all() and ref["sum"].mean() > 0
+
+
+def test_autotune_picks_options_that_render_identically(ctx):
+    """The autotuner's trials run on scratch films; its pick (and the BVH width
+    it leaves the scenes at) renders the same films as the megakernel; a
+    second call for the same batch shape is answered from the cache."""
+    a = _box_variant("plain")
+    b = _box_variant("materials")
+    sa = api.Scene(ctx, a["verts"], a["mat_idx"], a["mats"]).build(8, 1)
+    sb = api.Scene(ctx, b["verts"], b["mat_idx"], b["mats"]).build(8, 1)
+    views = [(0, a["camera"], api.make_settings(64, 48, 16, 8, 3, 1, 1, 64 / 48)),
+             (1, b["camera"], api.make_settings(32, 32, 64, 10, 3, 1, 2)),
+             (0, a["camera"], api.make_settings(40, 40, 8, 6, 0, 0, 3))]
+    try:
+        opts, width, trials = api.autotune_batch([sa, sb], views, sample_budget=1 << 17, widths=4 | 8)
+        assert width in (4, 8) and sa.info()["width"] == width and sb.info()["width"] == width
+        assert len(trials) >= 8 and all(t["ms"] > 0 for t in trials)
+        fastest = min(trials, key=lambda t: t["ms"])
+        assert fastest["width"] == width
+        assert all(fastest[k] == opts[k] for k in ("fuse", "refill", "fetch", "block_size", "path_pool"))
+        refs = [_mega(ctx, (sa, sb)[si], cam, st) for si, cam, st in views]
+        films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
+        ctx.check(api.render_batch([sa, sb], views, films, opts))
+        for f, r in zip(films, refs):
+            _same(f.download(f64=True), r)
+            f.close()
+        again, width2, trials2 = api.autotune_batch([sa, sb], views, sample_budget=1 << 17, widths=4 | 8)
+        assert again == opts and width2 == width and trials2 == []
+    finally:
+        sa.close()
+        sb.close()
