@@ -180,7 +180,7 @@ def test_autotune_picks_options_that_render_identically(ctx):
     try:
         opts, width, trials = api.autotune_batch([sa, sb], views, sample_budget=1 << 17, widths=4 | 8)
         assert width in (4, 8) and sa.info()["width"] == width and sb.info()["width"] == width
-        assert len(trials) >= 8 and all(t["ms"] > 0 for t in trials)
+        assert len(trials) >= 7 and all(t["ms"] > 0 for t in trials)
         fastest = min(trials, key=lambda t: t["ms"])
         assert fastest["width"] == width
         assert all(fastest[k] == opts[k] for k in ("fuse", "refill", "fetch", "block_size", "path_pool"))
