@@ -116,7 +116,8 @@ def workload_config(w):
     if w == "batch":
         return {"workload": "64 uneven views of the box (36 tris) and displaced (4,196,562 tris) scenes, "
                             "resolutions 128^2..1920x1080, spp 16/64/256, depth 8/16, RR from 3, extended estimator; "
-                            "wavefront form, one graph launch per batch; BVH width 8 with treelets",
+                            "wavefront form, one graph launch per batch, options and BVH width from the autotuner; "
+                            "treelet-optimised BVH",
                 "views": 64, "samples_per_step": 4728979456, "l2": L2_NOTE}
     if w == "box":
         return {"workload": "box scene (36 tris) 512x512, 64 spp, 8 segments, RR from 3, extended estimator, megakernel",
@@ -244,11 +245,13 @@ def time_to_rmse(ctx, api, scenes, timer, stream, target=1e-2):
     st = api.make_settings(512, 512, spp, 8, 3, 1, 1)
     f = api.Film(ctx, 512, 512)
     t_mega = timer.steps(lambda: (f.reset(stream), api.render(s, sc["camera"], st, f, stream)), 1, 1)[0]
-    t_wave = timer.steps(lambda: (f.reset(stream), ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], None, stream))), 1, 1)[0]
+    tuned, width, _ = api.autotune_batch([s], [(0, sc["camera"], st)], sample_budget=1 << 27, widths=4 | 8, stream=stream)
+    t_wave = timer.steps(lambda: (f.reset(stream), ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], tuned, stream))), 1, 1)[0]
     f.close()
     s.close()
     return {"target_rmse": target, "spp": spp, "rmse": rmse, "reference": "FP64 16384-spp box image, independent seed",
-            "megakernel_s": t_mega / 1e3, "wavefront_s": t_wave / 1e3}
+            "megakernel_s": t_mega / 1e3, "wavefront_s": t_wave / 1e3,
+            "wavefront_opts": dict(tuned, width=width), "note": "wavefront options from crg_autotune_batch (untimed)"}
 
 
 def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
@@ -426,10 +429,17 @@ def main():
         films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
         units = sum(st.width * st.height * st.spp for _, _, st in views)
 
+        # autotuner (untimed): BVH width, stage fusion, refill, fetch, block size, path pool
+        t0 = time.perf_counter()
+        tuned, tuned_width, trials = api.autotune_batch([sb, sd], views, sample_budget=1 << 28, widths=4 | 8, stream=S)
+        out["autotune"] = {"seconds": time.perf_counter() - t0, "width": tuned_width, "opts": tuned,
+                           "trials": len(trials), "trial_batch_samples": 1 << 28,
+                           "best_trial_msamples_per_s": max(t["msamples_per_s"] for t in trials)}
+
         def wave():
             for f in films:
                 f.reset(S)
-            ctx.check(api.render_batch([sb, sd], views, films, None, S))
+            ctx.check(api.render_batch([sb, sd], views, films, tuned, S))
 
         def mega():
             for (si, cam, st), f in zip(views, films):
@@ -439,17 +449,21 @@ def main():
         # instrumented wavefront pass (untimed): traversal work for the byte count
         for f in films:
             f.reset(S)
-        ctx.check(api.render_batch([sb, sd], views, films, dict(count_work=1), S))
+        ctx.check(api.render_batch([sb, sd], views, films, dict(tuned, count_work=1), S))
         torch.cuda.synchronize()
         work = api.batch_stats(ctx)
         rays = work["segments"] + work["shadow_rays"]
         algo = rays * 48 + work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
         with ClockSampler(local) as clk:
             ms = timer.steps(wave, args.steps, args.warmup)
+        if tuned_width != 8:  # the megakernel runs at its own best width (8)
+            sb.build(8, 1, stream=S)
+            sd.build(8, 1, stream=S)
         mega_ms = timer.steps(mega, 2, 1)
         out["megakernel"] = {"value": units / (sum(mega_ms) / len(mega_ms) / 1e3) / 1e6, "unit": unit,
                              "ms_per_step": sum(mega_ms) / len(mega_ms),
-                             "how": "same 64 views, one crg_render call per view (the drop-in), 1 warm-up + 2 steps"}
+                             "how": "same 64 views, one crg_render call per view (the drop-in), BVH width 8, "
+                                    "1 warm-up + 2 steps"}
         out["work"] = {**work, "mrays_per_step": rays / 1e6}
         kernel = "wavefront frame: one graph launch (k_wf_extend / k_wf_shade / k_wf_shadow / control / resolve)"
         launches = None  # counted below from the iteration count
@@ -465,12 +479,12 @@ def main():
         d2h = sum(o.array.nbytes for o in outs)
 
         def e2e_step():
-            a = api.Scene(ctx, *[p.array for p in pins["box"]]).build(8, 1, stream=S)
-            b = api.Scene(ctx, *[p.array for p in pins["disp"]]).build(8, 1, stream=S)
+            a = api.Scene(ctx, *[p.array for p in pins["box"]]).build(tuned_width, 1, stream=S)
+            b = api.Scene(ctx, *[p.array for p in pins["disp"]]).build(tuned_width, 1, stream=S)
             b.set_skybox(disp["skybox"])
             for f in films:
                 f.reset(S)
-            ctx.check(api.render_batch([a, b], views, films, None, S))
+            ctx.check(api.render_batch([a, b], views, films, tuned, S))
             for f, o in zip(films, outs):
                 ctx.check(ctx.lib.crg_film_download(f.h, o.ptr, None, None, None, None, None, S))
             a.close()
@@ -618,8 +632,10 @@ def main():
     value = units * args.steps * world / total_s / 1e6
     achieved = algo / (total_s / args.steps) / 1e9
     if launches is None:
-        # per frame: 3 prologue kernels + 7 graph kernels per device-loop iteration
-        launches = args.steps * (3 + 7 * int(out["work"]["iterations"]))
+        # per frame: 3 prologue kernels + per device-loop iteration: the bounce kernels (3 split, 2 with the shadow
+        # test in shade, 1 fused) + control, resolve, generate, generated
+        fuse = out.get("autotune", {}).get("opts", {}).get("fuse", 1) or 1
+        launches = args.steps * (3 + (4 + (3, 2, 1)[fuse - 1]) * int(out["work"]["iterations"]))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
