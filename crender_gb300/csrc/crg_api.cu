@@ -196,6 +196,7 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
     if ((rc = dev_alloc(ctx, s->mats, sizeof(crg_material) * (size_t)(nmat ? nmat : 1))) != CRG_OK) return rc;
     if ((rc = dev_alloc(ctx, s->err, 64)) != CRG_OK) return rc;
     if ((rc = dev_alloc(ctx, s->counters, 64)) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, s->qhead, 64)) != CRG_OK) return rc;
     CRG_CUDA(ctx, cudaMemset(s->err.ptr, 0, 64));
     CRG_CUDA(ctx, cudaMemset(s->counters.ptr, 0, 64));
     if (ntri) CRG_CUDA(ctx, cudaMemcpy(s->mat_idx.ptr, mat_idx, sizeof(uint32_t) * ntri, cudaMemcpyHostToDevice));
@@ -206,7 +207,7 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
 void scene_free(crg_scene *s) {
     if (!s) return;
     DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_cdf, &s->light_pdf, &s->mat_light_pdf,
-                      &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters};
+                      &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead};
     for (DevBuf *b : bufs) dev_free(*b);
     delete s;
 }

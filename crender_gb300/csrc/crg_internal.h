@@ -60,6 +60,7 @@ struct crg_scene {
     DevBuf wide;   // node_bytes * n_wide_capacity
     DevBuf tris;   // float4[3*ntri]
     DevBuf err;    // uint32 device error word
+    DevBuf qhead;  // uint32 work counter of the persistent query kernels
     // statistics
     int counting = 0;
     DevBuf counters; // unsigned long long[4]: samples, segments, shadow rays
