@@ -102,6 +102,12 @@ class RenderStats(C.Structure):
                 ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("iterations", C.c_uint64)]
 
 
+class PostSettings(C.Structure):
+    _fields_ = [("bloom", C.c_uint32), ("bloom_threshold", C.c_float), ("bloom_strength", C.c_float),
+                ("gray_scale", C.c_uint32), ("tonemapping", C.c_uint32), ("tonemap_type", C.c_int32),
+                ("exposure", C.c_float), ("gamma", C.c_float), ("mode", C.c_uint32), ("pad_", C.c_uint32)]
+
+
 # numpy views of the same layouts
 RAY_DTYPE = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
@@ -123,6 +129,8 @@ SHADE_METAL, SHADE_SMOOTH, SHADE_GLASS = 0, 1, 2
 MODE_FAITHFUL, MODE_EXTENDED = 0, 1
 CAMERA_PERSPECTIVE, CAMERA_ORTHOGRAPHIC = 0, 1
 FILM_F64, FILM_AOV = 1, 2
+TONEMAP_LINEAR, TONEMAP_REINHARD, TONEMAP_JIM_RICHARD, TONEMAP_UNCHARTED = 0, 1, 2, 3
+POST_FAITHFUL, POST_FULL = 0, 1
 INVALID_PRIM = 0xFFFFFFFF
 NOALLOC_MAX_TRIS = 16384
 
@@ -175,6 +183,8 @@ CRG_SIGNATURES = [
     ("crg_film_download", C.c_int, [vp, vp, vp, vp, vp, vp, vp, c_stream]),
     ("crg_film_device_ptrs", C.c_int, [vp, P(vp), P(vp), P(vp)]),
     ("crg_film_display", C.c_int, [vp, vp, c_stream]),
+    ("crg_post_settings_default", C.c_int, [P(PostSettings)]),
+    ("crg_post_process", C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, P(PostSettings), c_stream]),
     ("crg_render", C.c_int, [vp, P(Camera), P(Settings), vp, c_stream]),
     ("crg_scene_set_materials", C.c_int, [vp, vp, C.c_uint32]),
     ("crg_backward", C.c_int, [vp, P(Camera), P(Settings), vp, vp, vp, c_stream]),
@@ -235,6 +245,7 @@ ORC_SIGNATURES = [
     ("orc_render", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), P(OrcFilm), C.c_int]),
     ("orc_render_rows", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), P(OrcFilm), C.c_uint32, C.c_uint32, C.c_int]),
     ("orc_adjoint", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), vp, vp, vp, C.c_int]),
+    ("orc_post_process", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, P(PostSettings)]),
     ("orc_camera_ray", None, [P(Camera), P(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_float, vp, vp]),
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),

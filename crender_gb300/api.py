@@ -311,3 +311,25 @@ def backward(scene: Scene, camera: dict, settings: _abi.Settings, adjoint: Devic
     cam = make_camera(camera)
     scene.ctx.check(scene.ctx.lib.crg_backward(scene.h, C.byref(cam), C.byref(settings), adjoint.ptr,
                                                grad_colour.ptr, grad_emission.ptr, stream))
+
+
+def post_settings(**kw) -> _abi.PostSettings:
+    """crg_post_settings with the reference defaults (post_processor.h:20-40), then `kw`."""
+    s = _abi.PostSettings()
+    check(load().crg_post_settings_default(C.byref(s)))
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def post_process(ctx: Context, src: DeviceBuffer, dst: DeviceBuffer, width: int, height: int,
+                 settings: _abi.PostSettings, stream=None):
+    """crg_post_process on device RGBA32F images (cr::post_processor::process)."""
+    assert src.nbytes >= width * height * 16 and dst.nbytes >= width * height * 16
+    ctx.check(ctx.lib.crg_post_process(ctx.h, src.ptr, dst.ptr, width, height, C.byref(settings), stream))
+
+
+def film_display(film: Film, dst: DeviceBuffer, stream=None):
+    """crg_film_display: clamp(sum / spp, 0, 1)^(1/2.2) into a device RGBA32F image."""
+    assert dst.nbytes >= film.width * film.height * 16
+    film.ctx.check(film.ctx.lib.crg_film_display(film.h, dst.ptr, stream))

@@ -260,6 +260,7 @@ crg_status crg_context_create(int device, crg_context **out) {
 crg_status crg_context_destroy(crg_context *ctx) {
     if (!ctx) return CRG_ERR_INVALID_ARG;
     dev_free(ctx->wf_ws);
+    dev_free(ctx->post_ws);
     delete ctx;
     return CRG_OK;
 }

@@ -20,6 +20,7 @@ struct crg_context {
     std::string last_error;
     int sm_count = 0;
     DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
+    DevBuf post_ws; // post-process ping-pong images, grow-only
     crg_render_stats batch_stats{};
     struct Tuned {
         crg_wavefront_opts opts;

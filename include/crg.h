@@ -297,6 +297,63 @@ crg_status crg_film_device_ptrs(crg_film *film, float **sum_rgb, double **sum64,
  * buffer (renderer.cpp:371-383, the image behind renderer::current_progress). */
 crg_status crg_film_display(crg_film *film, float *d_rgba, crg_stream stream);
 
+/* ------------------------------------------------------------------ post-processing */
+
+/* Tone-mapping operators of the reference's post-process shader
+ * (assets/app/shaders/post_process.comp:49-108, selected by tonemapping_type). */
+typedef enum crg_tonemap {
+    CRG_TONEMAP_LINEAR = 0,      /* exposure, then gamma */
+    CRG_TONEMAP_REINHARD = 1,    /* c / (c + 1), then gamma */
+    CRG_TONEMAP_JIM_RICHARD = 2, /* Hejl-Burgess-Dawson filmic curve (gamma built in) */
+    CRG_TONEMAP_UNCHARTED = 3    /* Hable's Uncharted 2 curve, white point 11.2, then gamma */
+} crg_tonemap;
+
+/* FAITHFUL reproduces two coverage quirks of cr::post_processor:
+ *  - its compute dispatches are floor(W/8) x floor(H/8) groups of 8x8
+ *    (post_processor.cpp:219-222, 280-283), so pixels with x >= 8*floor(W/8) or
+ *    y >= 8*floor(H/8) come out as zero (the cleared target texture);
+ *  - the bloom brightness pass visits pixel (i % W, i / H) for i < W*H
+ *    (post_processor.cpp:296-307): on a non-square image some pixels are never
+ *    thresholded (visits with i / H >= H, an out-of-bounds access in the
+ *    reference, are skipped).
+ * FULL processes every pixel and thresholds every pixel once. */
+typedef enum crg_post_mode { CRG_POST_FAITHFUL = 0, CRG_POST_FULL = 1 } crg_post_mode;
+
+/* Fields and defaults follow cr::post_processor::bloom_settings,
+ * gray_scale_settings and tonemapping_settings
+ * (src/render/post/post_processor.h:20-40); crg_post_settings_default fills them. */
+typedef struct crg_post_settings {
+    uint32_t bloom;        /* default 0 */
+    float bloom_threshold; /* luminance below which a pixel does not bloom, default 0.7 */
+    float bloom_strength;  /* default 1 */
+    uint32_t gray_scale;   /* default 0 */
+    uint32_t tonemapping;  /* default 0 */
+    int32_t tonemap_type;  /* crg_tonemap, default LINEAR; other values leave the colour as is */
+    float exposure;        /* default 1 */
+    float gamma;           /* default 2.2 */
+    uint32_t mode;         /* crg_post_mode, default FAITHFUL */
+    uint32_t pad_;
+} crg_post_settings; /* 40 bytes */
+
+crg_status crg_post_settings_default(crg_post_settings *settings);
+
+/* Post-processes a device RGBA32F image [height][width][4] (typically the
+ * output of crg_film_display) into d_dst (same shape; must not alias d_src).
+ * Replaces cr::post_processor::process (src/render/post/post_processor.cpp:110-244)
+ * with its OpenGL compute passes restated as CUDA kernels:
+ *   bloom      threshold on luminance dot(rgb, (0.2126, 0.7152, 0.0722))
+ *              (_brightness, :296-307), then 10 separable 15-tap Gaussian passes
+ *              alternating horizontal / vertical (_blur, :246-294; blur.comp),
+ *              added with bloom_strength;
+ *   gray_scale 0.2126 r + 0.7162 g + 0.0722 b (post_process.comp:110-114, as written);
+ *   tonemapping one of crg_tonemap with exposure and gamma.
+ * Texels outside the image read as zero.  With no effect enabled the image is
+ * copied unchanged, as the reference returns its input.  The blur's two
+ * ping-pong images live in a grow-only workspace of the context (2 x W x H x
+ * 16 bytes); calls on one context must not overlap. */
+crg_status crg_post_process(crg_context *ctx, const float *d_src, float *d_dst, uint32_t width, uint32_t height,
+                            const crg_post_settings *settings, crg_stream stream);
+
 /* ------------------------------------------------------------------ render */
 
 /* Renders settings->spp more samples per pixel into the film with the

@@ -94,6 +94,11 @@ int orc_render_rows(const orc_scene_desc *scene, const crg_camera *cam, const cr
 int orc_adjoint(const orc_scene_desc *scene, const crg_camera *cam, const crg_settings *set, const float *adj,
                 double *grad_colour, double *grad_emission, int nthreads);
 
+/* Post-processing (bloom, gray scale, tone mapping) of an RGBA32F image
+ * [h][w][4], restating cr::post_processor::process step by step
+ * (src/render/post/post_processor.cpp:110-307). */
+int orc_post_process(const float *src, float *dst, uint32_t w, uint32_t h, const crg_post_settings *s);
+
 /* Camera ray of pixel (px, py) with jitter (jx, jy) (for unit tests). */
 void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx,
                     float jy, float *org, float *dir);

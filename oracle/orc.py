@@ -154,3 +154,13 @@ def adjoint(scene: dict, camera: dict, settings: _abi.Settings, adj: np.ndarray,
     rc = lib().orc_adjoint(C.byref(d), C.byref(cam), C.byref(settings), ptr(adj), ptr(gc), ptr(ge), nthreads)
     assert rc == 0, rc
     return gc.reshape(nmat, 3), ge
+
+
+def post_process(img: np.ndarray, settings: _abi.PostSettings) -> np.ndarray:
+    """CPU restatement of cr::post_processor::process on an RGBA32F image [h, w, 4]."""
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape[:2]
+    out = np.zeros_like(img)
+    rc = lib().orc_post_process(ptr(img), ptr(out), w, h, C.byref(settings))
+    assert rc == 0, rc
+    return out
