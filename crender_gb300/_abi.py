@@ -213,6 +213,11 @@ class OrcSceneDesc(C.Structure):
         ("sun_enabled", C.c_int),
         ("sun", Sun),
         ("build", P(BuildOpts)),
+        ("uvs", vp),
+        ("ntex", C.c_uint32),
+        ("tex_rgba", P(vp)),
+        ("tex_w", vp),
+        ("tex_h", vp),
     ]
 
 

@@ -114,18 +114,28 @@ class PinnedArray:
 class Scene:
     """cr::scene over the GPU path: geometry, materials, sky, sun, BVH."""
 
-    def __init__(self, ctx: Context, verts, mat_idx, mats):
+    def __init__(self, ctx: Context, verts, mat_idx, mats, uvs=None):
         self.ctx = ctx
         self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
         self.mat_idx = np.ascontiguousarray(mat_idx, np.uint32)
         self.mats = np.ascontiguousarray(mats)
+        self.uvs = None if uvs is None else np.ascontiguousarray(uvs, np.float32).reshape(-1, 6)
         self.ntri = self.verts.shape[0]
         self.h = C.c_void_p()
         ctx.check(
             ctx.lib.crg_scene_create(
-                ctx.h, ptr(self.verts), self.ntri, None, ptr(self.mat_idx), ptr(self.mats), len(self.mats), C.byref(self.h)
+                ctx.h, ptr(self.verts), self.ntri, ptr(self.uvs), ptr(self.mat_idx), ptr(self.mats), len(self.mats),
+                C.byref(self.h)
             )
         )
+
+    def set_textures(self, textures):
+        """crg_scene_set_textures: a list of RGBA32F [h, w, 4] arrays (empty list removes them)."""
+        texs = [np.ascontiguousarray(t, np.float32) for t in textures]
+        arr = (C.c_void_p * max(len(texs), 1))(*[ptr(t) for t in texs])
+        w = np.array([t.shape[1] for t in texs] or [0], np.uint32)
+        h = np.array([t.shape[0] for t in texs] or [0], np.uint32)
+        self.ctx.check(self.ctx.lib.crg_scene_set_textures(self.h, len(texs), arr, ptr(w), ptr(h)))
 
     def build(self, width=8, treelet=0, leaf_max=3, rounds=3, stream=None):
         self.opts = _abi.BuildOpts(width, treelet, leaf_max, rounds)

@@ -207,7 +207,8 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
 void scene_free(crg_scene *s) {
     if (!s) return;
     DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_cdf, &s->light_pdf, &s->mat_light_pdf,
-                      &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead};
+                      &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead,
+                      &s->uvs, &s->texels, &s->tex_info};
     for (DevBuf *b : bufs) dev_free(*b);
     delete s;
 }
@@ -315,7 +316,6 @@ crg_status crg_stream_sync(crg_context *ctx, crg_stream stream) {
 
 crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri, const float *uvs, const uint32_t *mat_idx,
                             const crg_material *mats, uint32_t nmat, crg_scene **out) {
-    (void)uvs;
     if (ntri > 0 && !verts) return set_error(ctx, CRG_ERR_INVALID_ARG, "null vertex array");
     if (out) *out = nullptr;
     crg_scene *s = nullptr;
@@ -324,6 +324,12 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
     if (rc == CRG_OK && ntri) {
         const cudaError_t e = cudaMemcpy(s->verts.ptr, verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(verts)");
+    }
+    // per-corner texture coordinates (the ATTRIBUTE buffer of model.cpp:80-90)
+    if (rc == CRG_OK && ntri && uvs) rc = dev_alloc(ctx, s->uvs, sizeof(float) * 6 * (size_t)ntri);
+    if (rc == CRG_OK && ntri && uvs) {
+        const cudaError_t e = cudaMemcpy(s->uvs.ptr, uvs, sizeof(float) * 6 * (size_t)ntri, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(uvs)");
     }
     if (rc == CRG_OK) {
         compute_areas(s, verts);
@@ -412,12 +418,34 @@ crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun) 
 
 crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba, const uint32_t *widths,
                                   const uint32_t *heights) {
-    (void)rgba;
-    (void)widths;
-    (void)heights;
     if (!scene) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scene->ctx;
+    if (count > 0 && (!rgba || !widths || !heights)) return set_error(ctx, CRG_ERR_INVALID_ARG, "null texture arrays");
+    std::vector<uint32_t> info(4 * (size_t)count);
+    size_t total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (!rgba[i] || widths[i] == 0 || heights[i] == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty texture");
+        info[4 * i + 0] = (uint32_t)(total & 0xFFFFFFFFu);
+        info[4 * i + 1] = (uint32_t)(total >> 32);
+        info[4 * i + 2] = widths[i];
+        info[4 * i + 3] = heights[i];
+        total += (size_t)widths[i] * heights[i];
+    }
+    dev_free(scene->texels);
+    dev_free(scene->tex_info);
+    scene->ntex = 0;
     if (count == 0) return CRG_OK;
-    return set_error(scene->ctx, CRG_ERR_UNSUPPORTED, "textured materials are not supported by this build");
+    crg_status rc;
+    if ((rc = dev_alloc(ctx, scene->texels, 16 * total)) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, scene->tex_info, 16 * (size_t)count)) != CRG_OK) return rc;
+    for (uint32_t i = 0; i < count; ++i) {
+        const size_t first = ((size_t)info[4 * i + 1] << 32) | info[4 * i];
+        CRG_CUDA(ctx, cudaMemcpy((float *)scene->texels.ptr + 4 * first, rgba[i], 16 * (size_t)widths[i] * heights[i],
+                                 cudaMemcpyHostToDevice));
+    }
+    CRG_CUDA(ctx, cudaMemcpy(scene->tex_info.ptr, info.data(), 16 * (size_t)count, cudaMemcpyHostToDevice));
+    scene->ntex = count;
+    return CRG_OK;
 }
 
 crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info) {
@@ -691,6 +719,9 @@ crg_status crg_backward(crg_scene *scene, const crg_camera *camera, const crg_se
     if (s.width == 0 || s.height == 0 || s.spp == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty adjoint pass");
     if (camera->mode > CRG_CAMERA_ORTHOGRAPHIC) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad camera mode");
     if (scene->sun_enabled) return set_error(ctx, CRG_ERR_UNSUPPORTED, "adjoint: the sun belongs to the faithful estimator");
+    for (const crg_material &m : scene->host_mats)
+        if (m.tex >= 0 && (uint32_t)m.tex < scene->ntex)
+            return set_error(ctx, CRG_ERR_UNSUPPORTED, "adjoint: textured materials have no colour parameter");
     return launch_backward(scene, camera_params(*camera), s, d_adjoint, d_grad_colour, d_grad_emission, (cudaStream_t)stream);
 }
 

@@ -39,6 +39,11 @@ struct crg_scene {
     DevBuf mats;    // crg_material[nmat]
     std::vector<crg_material> host_mats;
     std::vector<uint32_t> host_mat_idx;
+    // texture coordinates and textures (cr::image entities referenced by crg_material::tex)
+    DevBuf uvs;       // float[ntri*6] per-corner (u, v), primitive order; empty = none
+    DevBuf texels;    // float4 texels of all textures, concatenated
+    DevBuf tex_info;  // uint4 per texture: {first texel (low 32 bits), first texel (high 32 bits), width, height}
+    uint32_t ntex = 0;
     // emissive triangles (power-weighted CDF)
     uint32_t nlights = 0;
     std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table

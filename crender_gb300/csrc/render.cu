@@ -163,6 +163,10 @@ SceneDev scene_dev(const crg_scene *s) {
     S.light_pdf = (const float *)s->light_pdf.ptr;
     S.mat_light_pdf = (const float *)s->mat_light_pdf.ptr;
     S.verts = (const float *)s->verts.ptr;
+    S.uvs = (const float *)s->uvs.ptr;
+    S.texels = (const float4 *)s->texels.ptr;
+    S.tex_info = (const uint4 *)s->tex_info.ptr;
+    S.ntex = s->texels.ptr ? s->ntex : 0;
     S.nlights = s->nlights;
     S.ntri = s->ntri;
     S.sky = (const float4 *)s->sky.ptr;

@@ -27,6 +27,10 @@ struct SceneDev {
     const float *mat_light_pdf;
     const float4 *sky;
     const float *verts;
+    const float *uvs;       // float[ntri*6] per-corner texture coordinates, or null
+    const float4 *texels;   // all textures' texels, concatenated
+    const uint4 *tex_info;  // per texture: first texel (lo, hi), width, height
+    uint32_t ntex;
     uint32_t nlights, ntri;
     uint32_t sky_w, sky_h;
     float sky_rot_u, sky_rot_v;
@@ -83,6 +87,35 @@ __device__ __forceinline__ uint32_t texel_index(float u, uint32_t n) {
     unsigned long long i = 0;
     if (f >= 0.0f) i = f < 4.6e18f ? (unsigned long long)f : 0ull;
     return (uint32_t)(i % n);
+}
+
+// ------------------------------------------------------------------ textures
+// process_hit takes the colour from the material's texture at the hit's
+// interpolated texture coordinate when it has one (renderer.cpp:30-35,
+// image::get_uv at image.h:104-109), else the material colour.
+__device__ __forceinline__ bool textured(const SceneDev &S, const crg_material &m) {
+    return m.tex >= 0 && (uint32_t)m.tex < S.ntex;
+}
+
+__device__ __forceinline__ float4 tex_lookup(const SceneDev &S, int32_t tex, float u, float v) {
+    const uint4 ti = __ldg(&S.tex_info[tex]);
+    const uint32_t x = texel_index(u, ti.z), y = texel_index(v, ti.w);
+    const size_t base = ((size_t)ti.y << 32) | ti.x;
+    return __ldg(&S.texels[base + x + (size_t)y * ti.z]);
+}
+
+// Barycentric interpolation of the per-corner coordinates (rtcInterpolate0 of
+// the vertex attribute buffer, src/objects/model.cpp:39-47); (0, 0) without
+// coordinates.
+__device__ __forceinline__ void interp_uv(const SceneDev &S, uint32_t prim, float b1, float b2, float &u, float &v) {
+    if (!S.uvs) {
+        u = v = 0.0f;
+        return;
+    }
+    const float *t = S.uvs + (size_t)prim * 6;
+    const float b0 = (1.0f - b1) - b2;
+    u = (b0 * __ldg(t + 0) + b1 * __ldg(t + 2)) + b2 * __ldg(t + 4);
+    v = (b0 * __ldg(t + 1) + b1 * __ldg(t + 3)) + b2 * __ldg(t + 5);
 }
 
 __device__ __forceinline__ v3 sample_sky(const SceneDev &S, v3 d) {
@@ -144,6 +177,24 @@ __device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tm
     return occ;
 }
 
+// Colour (RGBA) of the surface a ray (o, d) hit on triangle slot `slot`.  The
+// barycentrics are recomputed with the traversal's watertight test, a pure
+// function of ray and triangle, so every form of the renderer (and the CPU
+// oracle) reads the same texel whatever produced the hit.
+__device__ inline float4 hit_colour(const SceneDev &S, const crg_material &m, uint32_t prim, uint32_t slot, v3 o, v3 d) {
+    if (!textured(S, m)) return make_float4(m.colour[0], m.colour[1], m.colour[2], m.colour[3]);
+    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+    TriHit th;
+    float b1 = 0.0f, b2 = 0.0f;
+    if (watertight(r, __ldg(&S.tris[slot * 3 + 0]), __ldg(&S.tris[slot * 3 + 1]), __ldg(&S.tris[slot * 3 + 2]), th)) {
+        b1 = th.V / th.det;
+        b2 = th.W / th.det;
+    }
+    float u, v;
+    interp_uv(S, prim, b1, b2, u, v);
+    return tex_lookup(S, m.tex, u, v);
+}
+
 // ------------------------------------------------------------------ path state
 // One path between bounces.  Shading a bounce (shade_faithful / shade_extended)
 // consumes the closest hit (or miss) of the current segment, updates the
@@ -202,7 +253,8 @@ __device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set
     slot_verts(S, h.slot, a, b, c);
     const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
     const crg_material &m = S.mats[__ldg(&S.mat_idx[h.prim])];
-    const float c0 = m.colour[0], c1 = m.colour[1], c2 = m.colour[2], c3 = m.colour[3];
+    const float4 col = hit_colour(S, m, h.prim, h.slot, ps.o, ps.d);
+    const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;
     if (c3 == 0.0f) {
         ps.o = add(p, mul(ps.d, 0.1f));
         return true;
@@ -363,7 +415,16 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
     const float cos_l = absf(dot(Ngl, wi));
     if (!(cos_l > 0.0f)) return;
     const crg_material &lm = S.mats[__ldg(&S.mat_idx[prim])];
-    const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
+    float lc0 = lm.colour[0], lc1 = lm.colour[1], lc2 = lm.colour[2];
+    if (textured(S, lm)) {
+        float tu, tv;
+        interp_uv(S, prim, b1, b2, tu, tv);
+        const float4 t = tex_lookup(S, lm.tex, tu, tv);
+        lc0 = t.x;
+        lc1 = t.y;
+        lc2 = t.z;
+    }
+    const v3 Le = mk(lc0 * lm.emission, lc1 * lm.emission, lc2 * lm.emission);
     const float p_light = (__ldg(&S.light_pdf[j]) * d2) / cos_l;
     v3 f;
     float p_bsdf, cos_i;
@@ -418,7 +479,8 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
     const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
     const uint32_t mi = __ldg(&S.mat_idx[h.prim]);
     const crg_material &m = S.mats[mi];
-    const float c0 = m.colour[0], c1 = m.colour[1], c2 = m.colour[2], c3 = m.colour[3];
+    const float4 col = hit_colour(S, m, h.prim, h.slot, ps.o, ps.d);
+    const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;
     if (c3 == 0.0f) {
         ps.o = add(p, mul(ps.d, 0.1f));
         return true;
@@ -536,7 +598,7 @@ __device__ __forceinline__ bool shadow_visible(const SceneDev &S, const NeeReq &
         Hit sh;
         C.shadow++;
         if (!closest<W, CNT>(S, so, nr.d, INFINITY, sh, C)) return true;
-        if (S.mats[__ldg(&S.mat_idx[sh.prim])].colour[3] != 0.0f) return false;
+        if (hit_colour(S, S.mats[__ldg(&S.mat_idx[sh.prim])], sh.prim, sh.slot, so, nr.d).w != 0.0f) return false;
         so = add(add(so, mul(nr.d, sh.t)), mul(nr.d, 0.1f));
     }
 }

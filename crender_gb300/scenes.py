@@ -109,6 +109,49 @@ def box_scene():
     return dict(verts=np.ascontiguousarray(verts), mat_idx=np.asarray(mids, np.uint32), mats=mats, camera=camera)
 
 
+def textured_box(seed=5):
+    """The box scene with per-corner texture coordinates and four textures
+    (cr::image entities referenced by material `tex`):
+      0  a 16x16 two-tone checker on the floor, ceiling and back wall;
+      1  a 32x32 texture on both inner boxes whose alpha is zero in a grid of
+         holes (pass-through texels, renderer.cpp:37-41);
+      2  an 8x8 colour gradient on the light (a textured emitter);
+      3  a 4x4 noise texture on the left wall.
+    Coordinates are the corner positions projected on the two axes of the
+    face's plane, scaled so textures repeat across a face."""
+    sc = box_scene()
+    v = sc["verts"].reshape(-1, 3, 3).astype(np.float64)
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    ax = np.argmax(np.abs(n), axis=1)
+    uvs = np.zeros((len(v), 3, 2))
+    for t in range(len(v)):
+        a, b = [k for k in range(3) if k != ax[t]]
+        uvs[t, :, 0] = v[t, :, a] * 2.0
+        uvs[t, :, 1] = v[t, :, b] * 2.0
+    r = np.random.default_rng(seed)
+    ii, jj = np.meshgrid(np.arange(16), np.arange(16), indexing="ij")
+    checker = np.where(((ii // 4 + jj // 4) % 2 == 0)[..., None], [0.8, 0.8, 0.75, 1.0], [0.3, 0.35, 0.6, 1.0])
+    holes = np.tile([0.9, 0.7, 0.3, 1.0], (32, 32, 1))
+    hi, hj = np.meshgrid(np.arange(32), np.arange(32), indexing="ij")
+    holes[(hi % 8 < 3) & (hj % 8 < 3), 3] = 0.0
+    gi, gj = np.meshgrid(np.linspace(0.4, 1.0, 8), np.linspace(0.5, 1.0, 8), indexing="ij")
+    grad = np.stack([gi, gj, np.full_like(gi, 0.8), np.ones_like(gi)], -1)
+    noise = np.concatenate([r.uniform(0.2, 0.8, (4, 4, 3)), np.ones((4, 4, 1))], -1)
+    mats = material_table(
+        [
+            {"colour": (0.73, 0.73, 0.73, 1.0), "tex": 0},
+            {"colour": (0.63, 0.065, 0.05, 1.0), "tex": 3},
+            {"colour": (0.14, 0.45, 0.09, 1.0)},
+            {"colour": (1.0, 1.0, 1.0, 1.0), "emission": 17.0, "tex": 2},
+            {"colour": (0.73, 0.73, 0.73, 1.0), "tex": 1},
+        ]
+    )
+    mat_idx = sc["mat_idx"].copy()
+    mat_idx[10:34] = 4  # the two inner boxes
+    textures = [t.astype(np.float32) for t in (checker, holes, grad, noise)]
+    return dict(sc, mats=mats, mat_idx=mat_idx, uvs=uvs.reshape(-1, 6).astype(np.float32), textures=textures)
+
+
 def soup(n=1 << 20, seed=1, sigma=0.01):
     """Random triangle soup: centroids U[0,1]^3, vertex offsets N(0, sigma^2) per axis."""
     rng = np.random.default_rng(seed)

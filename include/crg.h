@@ -191,7 +191,15 @@ crg_status crg_scene_set_skybox(crg_scene *scene, const float *rgba, uint32_t w,
 /* Sun light for the faithful estimator; replaces cr::scene::set_sun_enabled
  * and cr::registry::set_sun (scene.cpp:113-121, registry.cpp:248-256). sun may be NULL (defaults). */
 crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun);
-/* Diffuse textures (RGBA32F), referenced by crg_material::tex. */
+/* Textures: `count` host RGBA32F images rgba[i] of widths[i] x heights[i]
+ * ([h][w][4], cr::image layout), replacing any earlier set.  A material with
+ * 0 <= tex < count takes its RGBA colour from texture `tex` at the hit's
+ * texture coordinate — the per-corner uvs of crg_scene_create interpolated
+ * with the hit's barycentrics, (0, 0) without uvs — by nearest texel with
+ * modulo wrap, as process_hit and image::get_uv do (src/render/renderer.cpp:30-35,
+ * src/objects/image.h:104-109); alpha 0 there is a pass-through surface.  An
+ * emissive textured material emits texture colour x emission.  Other tex
+ * values mean "no texture".  count = 0 removes the textures. */
 crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba,
                                   const uint32_t *widths, const uint32_t *heights);
 

@@ -66,6 +66,10 @@ typedef struct orc_scene_desc {
     int sun_enabled;
     crg_sun sun;
     const crg_build_opts *build; /* BVH options (NULL = defaults) */
+    const float *uvs;            /* ntri*6 per-corner texture coordinates, or NULL */
+    uint32_t ntex;               /* textures (crg_scene_set_textures) */
+    const float *const *tex_rgba;
+    const uint32_t *tex_w, *tex_h;
 } orc_scene_desc;
 
 typedef struct orc_film {

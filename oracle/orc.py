@@ -91,6 +91,8 @@ def closest_f64(verts, rays):
 
 
 def scene_desc(scene: dict, sun_enabled=False, sun=None, skybox=None, sky_rot=(0.0, 0.0), build=None):
+    """orc_scene_desc of a scene dict {verts, mat_idx, mats[, uvs, textures]}; textures
+    is a list of RGBA32F [h, w, 4] arrays."""
     from crender_gb300.api import make_sun
 
     d = _abi.OrcSceneDesc()
@@ -99,6 +101,17 @@ def scene_desc(scene: dict, sun_enabled=False, sun=None, skybox=None, sky_rot=(0
     d.verts, d.mat_idx, d.mats = ptr(keep[0]), ptr(keep[1]), ptr(keep[2])
     d.ntri = keep[0].size // 9
     d.nmat = len(keep[2])
+    if scene.get("uvs") is not None:
+        uv = np.ascontiguousarray(scene["uvs"], np.float32)
+        keep.append(uv)
+        d.uvs = ptr(uv)
+    texs = [np.ascontiguousarray(t, np.float32) for t in scene.get("textures") or []]
+    if texs:
+        arr = (C.c_void_p * len(texs))(*[ptr(t) for t in texs])
+        tw = np.array([t.shape[1] for t in texs], np.uint32)
+        th = np.array([t.shape[0] for t in texs], np.uint32)
+        keep += [texs, arr, tw, th]
+        d.ntex, d.tex_rgba, d.tex_w, d.tex_h = len(texs), C.cast(arr, C.POINTER(C.c_void_p)), ptr(tw), ptr(th)
     if skybox is not None:
         sk = np.ascontiguousarray(skybox, np.float32)
         keep.append(sk)

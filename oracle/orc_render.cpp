@@ -118,6 +118,11 @@ struct Scene {
     std::vector<uint32_t> light_prim;
     std::vector<float> light_cdf, light_pdf;
     std::vector<float> mat_light_pdf;
+    /* texture coordinates and textures */
+    const float *uvs = nullptr;
+    uint32_t ntex = 0;
+    const float *const *tex_rgba = nullptr;
+    const uint32_t *tex_w = nullptr, *tex_h = nullptr;
 };
 
 /* image::get_uv (src/objects/image.h:104-109): nearest texel, modulo wrap. */
@@ -137,6 +142,40 @@ v3 sample_sky(const Scene &S, v3 d) {
     const uint64_t y = texel_index(v + S.sky_rot_v, S.sky_h);
     const float *t = S.sky + (x + y * S.sky_w) * 4;
     return mk(t[0], t[1], t[2]);
+}
+
+/* process_hit's colour (renderer.cpp:30-35): texture `tex` at the hit's
+ * interpolated texture coordinate (rtcInterpolate0, model.cpp:39-47), nearest
+ * texel with modulo wrap, else the material colour.  (b1, b2) are the
+ * barycentrics of vertices 1 and 2. */
+bool textured(const Scene &S, const crg_material &m) { return m.tex >= 0 && (uint32_t)m.tex < S.ntex; }
+
+void interp_uv(const Scene &S, uint32_t prim, float b1, float b2, float &u, float &v) {
+    if (!S.uvs) {
+        u = v = 0.0f;
+        return;
+    }
+    const float *t = S.uvs + (size_t)prim * 6;
+    const float b0 = (1.0f - b1) - b2;
+    u = (b0 * t[0] + b1 * t[2]) + b2 * t[4];
+    v = (b0 * t[1] + b1 * t[3]) + b2 * t[5];
+}
+
+const float *tex_lookup(const Scene &S, int32_t tex, float u, float v) {
+    const uint32_t w = S.tex_w[tex], h = S.tex_h[tex];
+    const uint64_t x = texel_index(u, w), y = texel_index(v, h);
+    return S.tex_rgba[tex] + (x + y * w) * 4;
+}
+
+/* RGBA colour of the surface at a closest hit. */
+void hit_colour(const Scene &S, const crg_material &m, const crg_hit &h, float col[4]) {
+    const float *c = m.colour;
+    if (textured(S, m)) {
+        float u, v;
+        interp_uv(S, h.prim, h.u, h.v, u, v);
+        c = tex_lookup(S, m.tex, u, v);
+    }
+    for (int k = 0; k < 4; ++k) col[k] = c[k];
 }
 
 struct Ctx {
@@ -192,7 +231,8 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
         tri_verts(S, h.prim, a, b, c);
         const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
         const crg_material &m = S.mats[S.mat_idx[h.prim]];
-        const float *col = m.colour;
+        float col[4];
+        hit_colour(S, m, h, col);
         if (col[3] == 0.0f) {
             o = add(p, mul(d, 0.1f));
             continue;
@@ -248,8 +288,9 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
             C.shadow++;
             bool blocked = cast(S, so, sd, kInf, sh);
             while (blocked) {
-                const crg_material &sm = S.mats[S.mat_idx[sh.prim]];
-                if (sm.colour[3] != 0.0f) break;
+                float scol[4];
+                hit_colour(S, S.mats[S.mat_idx[sh.prim]], sh, scol);
+                if (scol[3] != 0.0f) break;
                 so = add(add(so, mul(sd, sh.t)), mul(sd, 0.1f));
                 C.shadow++;
                 blocked = cast(S, so, sd, kInf, sh);
@@ -420,7 +461,13 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
     crg_ray sr{{po.x, po.y, po.z}, 1e-5f, {wi.x, wi.y, wi.z}, dist * 0.999f};
     if (orc_internal::any(S.bvh, sr)) return mk(0, 0, 0);
     const crg_material &lm = S.mats[S.mat_idx[prim]];
-    const v3 Le = mk(lm.colour[0] * lm.emission, lm.colour[1] * lm.emission, lm.colour[2] * lm.emission);
+    const float *lc = lm.colour;
+    if (textured(S, lm)) {
+        float tu, tv;
+        interp_uv(S, prim, b1, b2, tu, tv);
+        lc = tex_lookup(S, lm.tex, tu, tv);
+    }
+    const v3 Le = mk(lc[0] * lm.emission, lc[1] * lm.emission, lc[2] * lm.emission);
     const float p_light = (S.light_pdf[j] * d2) / cos_l;
     v3 f, bsdf_dlog;
     float p_bsdf, cos_i;
@@ -473,7 +520,8 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
         const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
         const uint32_t mi = S.mat_idx[h.prim];
         const crg_material &m = S.mats[mi];
-        const float *col = m.colour;
+        float col[4];
+        hit_colour(S, m, h, col);
         if (col[3] == 0.0f) {
             o = add(p, mul(d, 0.1f));
             continue;
@@ -596,6 +644,11 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
     S.sky_rot_v = D.sky_rot_v;
     S.sun_on = D.sun_enabled != 0;
     S.sun = D.sun;
+    S.uvs = D.uvs;
+    S.ntex = (D.tex_rgba && D.tex_w && D.tex_h) ? D.ntex : 0;
+    S.tex_rgba = D.tex_rgba;
+    S.tex_w = D.tex_w;
+    S.tex_h = D.tex_h;
     /* registry.cpp:44-48: sun frame = build_local(-direction) */
     S.sun_frame = build_local(mk(-D.sun.direction[0], -D.sun.direction[1], -D.sun.direction[2]));
     S.sun_cos = (float)std::cos((double)D.sun.size);
