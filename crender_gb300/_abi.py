@@ -169,6 +169,7 @@ CRG_SIGNATURES = [
     ("crg_scene_set_skybox", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_float, C.c_float]),
     ("crg_scene_set_sun", C.c_int, [vp, C.c_int, P(Sun)]),
     ("crg_scene_set_textures", C.c_int, [vp, C.c_uint32, P(vp), vp, vp]),
+    ("crg_scene_set_instances", C.c_int, [vp, vp, C.c_uint32]),
     ("crg_scene_bvh_info", C.c_int, [vp, P(BvhInfo)]),
     ("crg_scene_bvh_download", C.c_int, [vp, vp, vp, vp, vp]),
     ("crg_build_bvh_noalloc", C.c_int, [vp, C.c_uint32, P(BuildOpts), vp, C.c_size_t, vp, vp, P(BvhInfo), c_stream]),
@@ -218,6 +219,8 @@ class OrcSceneDesc(C.Structure):
         ("tex_rgba", P(vp)),
         ("tex_w", vp),
         ("tex_h", vp),
+        ("xforms", vp),
+        ("ninst", C.c_uint32),
     ]
 
 
@@ -251,6 +254,7 @@ ORC_SIGNATURES = [
     ("orc_render_rows", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), P(OrcFilm), C.c_uint32, C.c_uint32, C.c_int]),
     ("orc_adjoint", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), vp, vp, vp, C.c_int]),
     ("orc_post_process", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, P(PostSettings)]),
+    ("orc_scene_intersect", C.c_int, [P(OrcSceneDesc), vp, vp, vp, C.c_uint64]),
     ("orc_camera_ray", None, [P(Camera), P(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_float, vp, vp]),
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),

@@ -129,6 +129,15 @@ class Scene:
             )
         )
 
+    def set_instances(self, xforms):
+        """crg_scene_set_instances: [n, 4, 4] row-major matrices (numpy convention), sent
+        column-major as glm stores them; None or an empty array removes the instances."""
+        if xforms is None or len(xforms) == 0:
+            self.ctx.check(self.ctx.lib.crg_scene_set_instances(self.h, None, 0))
+            return
+        x = np.ascontiguousarray(np.transpose(np.asarray(xforms, np.float32), (0, 2, 1)))
+        self.ctx.check(self.ctx.lib.crg_scene_set_instances(self.h, ptr(x), len(x)))
+
     def set_textures(self, textures):
         """crg_scene_set_textures: a list of RGBA32F [h, w, 4] arrays (empty list removes them)."""
         texs = [np.ascontiguousarray(t, np.float32) for t in textures]

@@ -134,17 +134,23 @@ crg_status prepare_lights(crg_scene *s) {
         }
     }
     std::vector<uint32_t> &mat_idx = s->host_mat_idx;
-    std::vector<uint32_t> prim;
+    std::vector<uint32_t> prim, inst;
     std::vector<double> w;
     double total = 0.0;
-    for (uint32_t p = 0; p < s->ntri; ++p) {
-        const uint32_t m = mat_idx[p];
-        if (!(lum[m] > 0.0)) continue;
-        const double wt = s->tri_area[p] * lum[m];
-        prim.push_back(p);
-        w.push_back(wt);
-        total += wt;
-    }
+    // entries in instance-major, primitive order; an instanced scene weighs
+    // each emitter copy by its world area
+    const uint32_t ncopy = s->ninst ? s->ninst : 1;
+    for (uint32_t j = 0; j < ncopy; ++j)
+        for (uint32_t p = 0; p < s->ntri; ++p) {
+            const uint32_t m = mat_idx[p];
+            if (!(lum[m] > 0.0)) continue;
+            const double area = s->ninst ? s->inst_area[(size_t)j * s->ntri + p] : s->tri_area[p];
+            const double wt = area * lum[m];
+            prim.push_back(p);
+            inst.push_back(j);
+            w.push_back(wt);
+            total += wt;
+        }
     std::vector<float> mpdf(nmat, 0.0f);
     s->nlights = 0;
     if (total > 0.0) {
@@ -165,11 +171,77 @@ crg_status prepare_lights(crg_scene *s) {
         CRG_CUDA(s->ctx, cudaMemcpy(s->light_prim.ptr, prim.data(), 4 * prim.size(), cudaMemcpyHostToDevice));
         CRG_CUDA(s->ctx, cudaMemcpy(s->light_cdf.ptr, cdf.data(), 4 * cdf.size(), cudaMemcpyHostToDevice));
         CRG_CUDA(s->ctx, cudaMemcpy(s->light_pdf.ptr, pdf.data(), 4 * pdf.size(), cudaMemcpyHostToDevice));
+        if (s->ninst) {
+            if ((rc = dev_alloc(s->ctx, s->light_inst, 4 * inst.size())) != CRG_OK) return rc;
+            CRG_CUDA(s->ctx, cudaMemcpy(s->light_inst.ptr, inst.data(), 4 * inst.size(), cudaMemcpyHostToDevice));
+        }
     }
     crg_status rc;
     if ((rc = dev_alloc(s->ctx, s->mat_light_pdf, 4 * (size_t)(nmat ? nmat : 1))) != CRG_OK) return rc;
     if (nmat) CRG_CUDA(s->ctx, cudaMemcpy(s->mat_light_pdf.ptr, mpdf.data(), 4 * nmat, cudaMemcpyHostToDevice));
     return CRG_OK;
+}
+
+// Affine 4x4 (column-major, glm::mat4 layout) -> device rows {inverse, forward}.
+// The inverse is formed in double from the float entries (adjugate / det of
+// the 3x3 part, t' = -A^-1 t) and rounded once.  False if the matrix is not
+// affine or not invertible.
+bool instance_rows(const float *x, float rows[24]) {
+    if (x[3] != 0.0f || x[7] != 0.0f || x[11] != 0.0f || x[15] != 1.0f) return false;
+    double a[3][3], t[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) a[r][c] = (double)x[4 * c + r];
+        t[r] = (double)x[12 + r];
+    }
+    const double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+    const double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+    const double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    const double det = (a[0][0] * c00 + a[0][1] * c01) + a[0][2] * c02;
+    if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+    double inv[3][3];
+    inv[0][0] = c00 / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = c01 / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = c02 / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    for (int r = 0; r < 3; ++r) {
+        const double ti = -((inv[r][0] * t[0] + inv[r][1] * t[1]) + inv[r][2] * t[2]);
+        for (int c = 0; c < 3; ++c) rows[4 * r + c] = (float)inv[r][c];
+        rows[4 * r + 3] = (float)ti;
+        for (int c = 0; c < 3; ++c) rows[12 + 4 * r + c] = x[4 * c + r];
+        rows[12 + 4 * r + 3] = x[12 + r];
+    }
+    for (int k = 0; k < 24; ++k)
+        if (!std::isfinite(rows[k])) return false;
+    return true;
+}
+
+// World areas (double) of every triangle under every instance.
+void instance_areas(crg_scene *s, const float *verts) {
+    s->inst_area.assign((size_t)s->ninst * s->ntri, 0.0);
+    for (uint32_t j = 0; j < s->ninst; ++j) {
+        const float *x = &s->host_xf[16 * (size_t)j];
+        for (uint32_t p = 0; p < s->ntri; ++p) {
+            double w[3][3];
+            for (int k = 0; k < 3; ++k) {
+                const float *v = verts + (size_t)p * 9 + 3 * k;
+                for (int r = 0; r < 3; ++r)
+                    w[k][r] = (((double)x[r] * v[0] + (double)x[4 + r] * v[1]) + (double)x[8 + r] * v[2]) + (double)x[12 + r];
+            }
+            double e1[3], e2[3];
+            for (int r = 0; r < 3; ++r) {
+                e1[r] = w[1][r] - w[0][r];
+                e2[r] = w[2][r] - w[0][r];
+            }
+            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                         cz = e1[0] * e2[1] - e1[1] * e2[0];
+            s->inst_area[(size_t)j * s->ntri + p] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+        }
+    }
 }
 
 crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
@@ -208,7 +280,7 @@ void scene_free(crg_scene *s) {
     if (!s) return;
     DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_cdf, &s->light_pdf, &s->mat_light_pdf,
                       &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead,
-                      &s->uvs, &s->texels, &s->tex_info};
+                      &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst};
     for (DevBuf *b : bufs) dev_free(*b);
     delete s;
 }
@@ -446,6 +518,35 @@ crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float 
     CRG_CUDA(ctx, cudaMemcpy(scene->tex_info.ptr, info.data(), 16 * (size_t)count, cudaMemcpyHostToDevice));
     scene->ntex = count;
     return CRG_OK;
+}
+
+crg_status crg_scene_set_instances(crg_scene *scene, const float *xforms, uint32_t ninst) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scene->ctx;
+    if (ninst > 0 && !xforms) return set_error(ctx, CRG_ERR_INVALID_ARG, "null transform array");
+    if (ninst > (1u << 16)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 65536 instances");
+    std::vector<float> rows(24 * (size_t)ninst);
+    for (uint32_t j = 0; j < ninst; ++j)
+        if (!instance_rows(xforms + 16 * (size_t)j, &rows[24 * (size_t)j]))
+            return set_error(ctx, CRG_ERR_INVALID_ARG, "instance transform is not an invertible affine matrix");
+    // emitter copies are weighed by their world areas: the vertices come back to the host once
+    std::vector<float> hv((size_t)scene->ntri * 9);
+    if (ninst && scene->ntri)
+        CRG_CUDA(ctx, cudaMemcpy(hv.data(), scene->verts.ptr, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost));
+    dev_free(scene->inst);
+    dev_free(scene->light_inst);
+    scene->ninst = 0;
+    scene->host_xf.assign(xforms, xforms + 16 * (size_t)ninst);
+    scene->host_rows = rows;
+    scene->inst_area.clear();
+    if (ninst) {
+        crg_status rc = dev_alloc(ctx, scene->inst, sizeof(float) * rows.size());
+        if (rc != CRG_OK) return rc;
+        CRG_CUDA(ctx, cudaMemcpy(scene->inst.ptr, rows.data(), sizeof(float) * rows.size(), cudaMemcpyHostToDevice));
+        scene->ninst = ninst;
+        instance_areas(scene, hv.data());
+    }
+    return prepare_lights(scene);
 }
 
 crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info) {

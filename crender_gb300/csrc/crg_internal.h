@@ -44,6 +44,14 @@ struct crg_scene {
     DevBuf texels;    // float4 texels of all textures, concatenated
     DevBuf tex_info;  // uint4 per texture: {first texel (low 32 bits), first texel (high 32 bits), width, height}
     uint32_t ntex = 0;
+    // instances (cr::entity::instances::transforms): 4x4 column-major affine
+    // transforms as given, and per instance 6 float4 rows (inverse, forward)
+    uint32_t ninst = 0;
+    std::vector<float> host_xf;   // 16 floats per instance
+    std::vector<float> host_rows; // 24 floats per instance (the device layout)
+    std::vector<double> inst_area; // world area of triangle p under instance j at [j * ntri + p]
+    DevBuf inst;       // float4[6 * ninst]
+    DevBuf light_inst; // uint32 per emitter entry (instanced scenes)
     // emissive triangles (power-weighted CDF)
     uint32_t nlights = 0;
     std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table

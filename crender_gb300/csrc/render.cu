@@ -167,6 +167,9 @@ SceneDev scene_dev(const crg_scene *s) {
     S.texels = (const float4 *)s->texels.ptr;
     S.tex_info = (const uint4 *)s->tex_info.ptr;
     S.ntex = s->texels.ptr ? s->ntex : 0;
+    S.inst = (const float4 *)s->inst.ptr;
+    S.light_inst = (const uint32_t *)s->light_inst.ptr;
+    S.ninst = s->inst.ptr ? s->ninst : 0;
     S.nlights = s->nlights;
     S.ntri = s->ntri;
     S.sky = (const float4 *)s->sky.ptr;

@@ -31,6 +31,12 @@ struct SceneDev {
     const float4 *texels;   // all textures' texels, concatenated
     const uint4 *tex_info;  // per texture: first texel (lo, hi), width, height
     uint32_t ntex;
+    // instances (cr::entity::instances::transforms, model.cpp:99-126): per
+    // instance 6 float4 rows: the inverse (3 rows of [A | t]) then the forward
+    // transform; ninst = 0 means the mesh is used as is
+    const float4 *inst;
+    const uint32_t *light_inst; // instance of each emitter entry (instanced scenes)
+    uint32_t ninst;
     uint32_t nlights, ntri;
     uint32_t sky_w, sky_h;
     float sky_rot_u, sky_rot_v;
@@ -53,9 +59,14 @@ struct FilmDev {
     uint32_t width, height;
 };
 
+// Closest hit.  For an instanced scene t is the parameter along the
+// instance's object-space ray (hit_geom turns it into the world point and
+// distance) and inst the instance; otherwise inst = kNoInst and t is the
+// world distance.
+constexpr uint32_t kNoInst = 0xFFFFFFFFu;
 struct Hit {
     float t, u, v;
-    uint32_t prim, slot;
+    uint32_t prim, slot, inst;
 };
 
 struct PathCtx;
@@ -149,12 +160,78 @@ struct PathCtx {
     unsigned long long nodes, tris; // traversal work, counted only in the instrumented variant
 };
 
+// ------------------------------------------------------------------ instances
+// Row-form affine transforms: x' = ((r.x * x + r.y * y) + r.z * z) + r.w.
+__device__ __forceinline__ v3 xf_point(const float4 *R, v3 p) {
+    const float4 a = __ldg(&R[0]), b = __ldg(&R[1]), c = __ldg(&R[2]);
+    return mk(((a.x * p.x + a.y * p.y) + a.z * p.z) + a.w, ((b.x * p.x + b.y * p.y) + b.z * p.z) + b.w,
+              ((c.x * p.x + c.y * p.y) + c.z * p.z) + c.w);
+}
+__device__ __forceinline__ v3 xf_vector(const float4 *R, v3 v) {
+    const float4 a = __ldg(&R[0]), b = __ldg(&R[1]), c = __ldg(&R[2]);
+    return mk((a.x * v.x + a.y * v.y) + a.z * v.z, (b.x * v.x + b.y * v.y) + b.z * v.z, (c.x * v.x + c.y * v.y) + c.z * v.z);
+}
+
+// model::intersect's object-space ray of instance j: inverse(T) * (o, 1) and
+// normalize(inverse(T) * (d, 0)); len = |inverse(T) * d|.
+__device__ __forceinline__ void inst_ray(const SceneDev &S, uint32_t j, v3 o, v3 d, v3 &oo, v3 &od, float &len) {
+    const float4 *R = S.inst + 6 * (size_t)j;
+    oo = xf_point(R, o);
+    const v3 dr = xf_vector(R, d);
+    len = sqrtf(dot(dr, dr));
+    od = normalize(dr);
+}
+
+// World point T * (oo + od * t) of an object-space hit and its distance from
+// the world origin o (model.cpp:117-121).
+__device__ __forceinline__ v3 inst_point(const SceneDev &S, uint32_t j, v3 oo, v3 od, float t) {
+    return xf_point(S.inst + 6 * (size_t)j + 3, add(oo, mul(od, t)));
+}
+__device__ __forceinline__ float vdist(v3 a, v3 b) {
+    const v3 e = sub(a, b);
+    return sqrtf(dot(e, e));
+}
+
+// Slack of the object-space bound that prunes an instance's traversal by the
+// best world distance so far: the bound stays above the parameter at which
+// the world distance reaches the best one, so pruning never changes the result
+// of the reference's loop over instances.
+constexpr float kInstSlack = 1.0001f;
+
+// Closest hit with tmin < t (object space for instances, as the reference's
+// tnear) and world distance below tmax.
 template <int W, bool CNT>
-__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C) {
-    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+__device__ __forceinline__ bool closest_t(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, Hit &h, PathCtx &C) {
     bool occ;
     TravStats st{0, 0};
-    traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
+    if (S.ninst == 0) {
+        const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
+        traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
+        h.inst = kNoInst;
+    } else {
+        // model::intersect (model.cpp:99-126): every instance in order, closest
+        // world distance wins, ties to the earlier instance
+        const float dl = sqrtf(dot(d, d));
+        float best = tmax;
+        h.prim = 0xFFFFFFFFu;
+        h.inst = kNoInst;
+        for (uint32_t j = 0; j < S.ninst; ++j) {
+            v3 oo, od;
+            float len;
+            inst_ray(S, j, o, d, oo, od, len);
+            const float bound = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
+            const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+            Hit hj;
+            traverse<W, false, CNT>(S.nodes, S.tris, r, bound, hj.t, hj.prim, hj.slot, hj.u, hj.v, occ, st, C.err);
+            if (hj.prim == 0xFFFFFFFFu) continue;
+            const float dist = vdist(inst_point(S, j, oo, od, hj.t), o);
+            if (dist < best) {
+                best = dist;
+                h = hj;
+                h.inst = j;
+            }
+        }
+    }
     if (CNT) {
         C.nodes += st.nodes;
         C.tris += st.tris;
@@ -163,13 +240,31 @@ __device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tma
 }
 
 template <int W, bool CNT>
-__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C) {
-    const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+__device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C) {
+    return closest_t<W, CNT>(S, o, d, 1e-5f, tmax, h, C);
+}
+
+// Any hit with tmin < t < tmax.  Instanced: any instance with a hit whose
+// object-space parameter is below tmax * |inverse(T) d| / |d|.
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded_t(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, PathCtx &C) {
     float t, u, v;
     uint32_t p, sl;
-    bool occ;
+    bool occ = false;
     TravStats st{0, 0};
-    traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
+    if (S.ninst == 0) {
+        const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
+        traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
+    } else {
+        const float dl = sqrtf(dot(d, d));
+        for (uint32_t j = 0; j < S.ninst && !occ; ++j) {
+            v3 oo, od;
+            float len;
+            inst_ray(S, j, o, d, oo, od, len);
+            const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+            traverse<W, true, CNT>(S.nodes, S.tris, r, (tmax * len) / dl, t, p, sl, u, v, occ, st, C.err);
+        }
+    }
     if (CNT) {
         C.nodes += st.nodes;
         C.tris += st.tris;
@@ -177,11 +272,52 @@ __device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tm
     return occ;
 }
 
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C) {
+    return occluded_t<W, CNT>(S, o, d, 1e-5f, tmax, C);
+}
+
+// Geometry of a closest hit of the ray (o, d): world point, geometric normal,
+// world distance, and the ray in the triangle's own space (for barycentrics).
+// WORLD_N = false keeps the object-space normal of an instanced hit, as the
+// reference does (model.cpp:117-121 maps only the point back).
+struct HitGeom {
+    v3 p, Ng;
+    float dist;
+    v3 ro, rd;
+};
+template <bool WORLD_N>
+__device__ __forceinline__ HitGeom hit_geom(const SceneDev &S, const Hit &h, v3 o, v3 d) {
+    HitGeom g;
+    v3 a, b, c;
+    slot_verts(S, h.slot, a, b, c);
+    if (h.inst == kNoInst) {
+        g.p = add(o, mul(d, h.t));
+        g.dist = h.t;
+        g.ro = o;
+        g.rd = d;
+    } else {
+        float len;
+        inst_ray(S, h.inst, o, d, g.ro, g.rd, len);
+        g.p = inst_point(S, h.inst, g.ro, g.rd, h.t);
+        g.dist = vdist(g.p, o);
+        if (WORLD_N) {
+            const float4 *F = S.inst + 6 * (size_t)h.inst + 3;
+            a = xf_point(F, a);
+            b = xf_point(F, b);
+            c = xf_point(F, c);
+        }
+    }
+    g.Ng = normalize(cross(sub(b, a), sub(c, a)));
+    return g;
+}
+
 // Colour (RGBA) of the surface a ray (o, d) hit on triangle slot `slot`.  The
 // barycentrics are recomputed with the traversal's watertight test, a pure
 // function of ray and triangle, so every form of the renderer (and the CPU
 // oracle) reads the same texel whatever produced the hit.
 __device__ inline float4 hit_colour(const SceneDev &S, const crg_material &m, uint32_t prim, uint32_t slot, v3 o, v3 d) {
+    // (o, d) is the ray in the triangle's space (HitGeom::ro / rd)
     if (!textured(S, m)) return make_float4(m.colour[0], m.colour[1], m.colour[2], m.colour[3]);
     const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
     TriHit th;
@@ -248,12 +384,10 @@ __device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set
         ps.L = add(ps.L, mulv(ps.T, env));
         return false;
     }
-    const v3 p = add(ps.o, mul(ps.d, h.t));
-    v3 a, b, c;
-    slot_verts(S, h.slot, a, b, c);
-    const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+    const HitGeom hg = hit_geom<false>(S, h, ps.o, ps.d);
+    const v3 p = hg.p, Ng = hg.Ng;
     const crg_material &m = S.mats[__ldg(&S.mat_idx[h.prim])];
-    const float4 col = hit_colour(S, m, h.prim, h.slot, ps.o, ps.d);
+    const float4 col = hit_colour(S, m, h.prim, h.slot, hg.ro, hg.rd);
     const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;
     if (c3 == 0.0f) {
         ps.o = add(p, mul(ps.d, 0.1f));
@@ -290,7 +424,7 @@ __device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set
     if (i == 0) {
         aov.albedo = albedo;
         aov.normal = Ng;
-        aov.depth = h.t;
+        aov.depth = hg.dist;
     }
     ps.T = mulv(ps.T, albedo);
     ps.L = add(ps.L, mul(ps.T, m.emission));
@@ -400,6 +534,12 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
     const uint32_t prim = __ldg(&S.light_prim[j]);
     v3 a, b, c;
     prim_verts(S, prim, a, b, c);
+    if (S.ninst) {
+        const float4 *F = S.inst + 6 * (size_t)__ldg(&S.light_inst[j]) + 3;
+        a = xf_point(F, a);
+        b = xf_point(F, b);
+        c = xf_point(F, c);
+    }
     const float su = sqrtf(g.y);
     const float b0 = 1.0f - su, b1 = su * (1.0f - g.z), b2 = su * g.z;
     const v3 pl = add(add(mul(a, b0), mul(b, b1)), mul(c, b2));
@@ -473,13 +613,11 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
         if (tape) tape->env(contrib);
         return false;
     }
-    const v3 p = add(ps.o, mul(ps.d, h.t));
-    v3 a, b, c;
-    slot_verts(S, h.slot, a, b, c);
-    const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+    const HitGeom hg = hit_geom<true>(S, h, ps.o, ps.d);
+    const v3 p = hg.p, Ng = hg.Ng;
     const uint32_t mi = __ldg(&S.mat_idx[h.prim]);
     const crg_material &m = S.mats[mi];
-    const float4 col = hit_colour(S, m, h.prim, h.slot, ps.o, ps.d);
+    const float4 col = hit_colour(S, m, h.prim, h.slot, hg.ro, hg.rd);
     const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;
     if (c3 == 0.0f) {
         ps.o = add(p, mul(ps.d, 0.1f));
@@ -491,7 +629,7 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
     if (i == 0) {
         aov.albedo = rgb;
         aov.normal = Ng;
-        aov.depth = h.t;
+        aov.depth = hg.dist;
     }
     const float emission = m.emission;
     if (emission > 0.0f) {
@@ -503,7 +641,7 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
         } else {
             const float cos_l = absf(cos_nd);
             if (cos_l > 0.0f) {
-                const float pl = (__ldg(&S.mat_light_pdf[mi]) * (h.t * h.t)) / cos_l;
+                const float pl = (__ldg(&S.mat_light_pdf[mi]) * (hg.dist * hg.dist)) / cos_l;
                 const float w = (ps.prev_pdf * ps.prev_pdf) / (ps.prev_pdf * ps.prev_pdf + pl * pl);
                 const v3 contrib = mul(mulv(ps.T, Le), w);
                 ps.L = add(ps.L, contrib);
@@ -598,8 +736,9 @@ __device__ __forceinline__ bool shadow_visible(const SceneDev &S, const NeeReq &
         Hit sh;
         C.shadow++;
         if (!closest<W, CNT>(S, so, nr.d, INFINITY, sh, C)) return true;
-        if (hit_colour(S, S.mats[__ldg(&S.mat_idx[sh.prim])], sh.prim, sh.slot, so, nr.d).w != 0.0f) return false;
-        so = add(add(so, mul(nr.d, sh.t)), mul(nr.d, 0.1f));
+        const HitGeom hg = hit_geom<false>(S, sh, so, nr.d);
+        if (hit_colour(S, S.mats[__ldg(&S.mat_idx[sh.prim])], sh.prim, sh.slot, hg.ro, hg.rd).w != 0.0f) return false;
+        so = add(hg.p, mul(nr.d, 0.1f));
     }
 }
 

@@ -7,11 +7,41 @@
 // error word instead of trapping).
 #include <algorithm>
 
-#include "crg_dev.cuh"
-#include "crg_internal.h"
+#include "render_common.cuh"
 
 namespace crg {
 namespace {
+
+// Queries on an instanced scene: model::intersect's loop over the instances
+// (model.cpp:99-126) through the shared closest / any-hit functions.  The
+// ray's tmin applies in each instance's object space (the reference's tnear);
+// t is the world distance of the hit point.
+template <int W, bool ANY>
+__global__ void __launch_bounds__(128) k_intersect_inst(rc::SceneDev S, const float4 *__restrict__ rays,
+                                                       float4 *__restrict__ hits, uint32_t *__restrict__ occluded,
+                                                       uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 r0 = __ldg(&rays[2 * i]);
+    const float4 r1 = __ldg(&rays[2 * i + 1]);
+    const v3 o = mk(r0.x, r0.y, r0.z), d = mk(r1.x, r1.y, r1.z);
+    rc::PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
+    if (ANY) {
+        occluded[i] = rc::occluded_t<W, false>(S, o, d, r0.w, r1.w, C) ? 1u : 0u;
+    } else {
+        rc::Hit h;
+        if (rc::closest_t<W, false>(S, o, d, r0.w, r1.w, h, C)) {
+            v3 oo, od;
+            float len;
+            rc::inst_ray(S, h.inst, o, d, oo, od, len);
+            const float t = rc::vdist(rc::inst_point(S, h.inst, oo, od, h.t), o);
+            hits[i] = make_float4(t, __uint_as_float(h.prim), h.u, h.v);
+        } else {
+            hits[i] = make_float4(INFINITY, __uint_as_float(0xFFFFFFFFu), 0.0f, 0.0f);
+        }
+    }
+    if (C.err) atomicOr(S.err, C.err);
+}
 
 // One thread per ray.  (A persistent-block variant that refilled idle lanes
 // from a shared-memory counter between traversal slices measured 21% slower
@@ -95,6 +125,15 @@ constexpr uint32_t kAnyRefill = 4;
 template <int W>
 void launch_w(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded, uint32_t *nodes, uint32_t *tris,
               uint64_t n, bool any, cudaStream_t st) {
+    if (s->ninst && s->ntri > 0) {
+        const rc::SceneDev S = rc::scene_dev(s);
+        const uint64_t blocks = (n + 127) / 128;
+        if (any) k_intersect_inst<W, true><<<blocks, 128, 0, st>>>(S, (const float4 *)rays, nullptr, occluded, n);
+        else k_intersect_inst<W, false><<<blocks, 128, 0, st>>>(S, (const float4 *)rays, (float4 *)hits, nullptr, n);
+        if (nodes) cudaMemsetAsync(nodes, 0, 4 * n, st);
+        if (tris) cudaMemsetAsync(tris, 0, 4 * n, st);
+        return;
+    }
     if (any && n >= (1u << 16) && n < 0xFFFF0000ull && s->ntri > 0) {
         int per_sm = 0;
         if (any) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_intersect_dyn<W, true>, 128, 0);

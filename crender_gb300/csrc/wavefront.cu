@@ -91,6 +91,11 @@ struct Wf {
     float4 *slots;         // radiance per sample of the current chunk
 };
 
+// hit.w of a path slot: 0 = miss, 1 = hit on the plain mesh, 2 + j = hit on instance j.
+__device__ __forceinline__ float pack_found(bool found, uint32_t inst) {
+    return __uint_as_float(found ? (inst == kNoInst ? 1u : inst + 2u) : 0u);
+}
+
 __device__ __forceinline__ uint32_t *q_in(const Wf &w, const Ctrl &c) { return c.parity ? w.qb : w.qa; }
 __device__ __forceinline__ uint32_t *q_out(const Wf &w, const Ctrl &c) { return c.parity ? w.qa : w.qb; }
 
@@ -187,7 +192,7 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
             Hit h;
             const bool found = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
-            w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), found ? 1.0f : 0.0f);
+            w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), pack_found(found, h.inst));
             if (C.err) atomicOr(&c->error, 1u);
             if (CNT) {
                 nodes += C.nodes;
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                 if (FUSE >= 2) {
                     Hit hh;
                     const bool f = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
-                    h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), f ? 1.0f : 0.0f);
+                    h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), pack_found(f, hh.inst));
                 } else {
                     h4 = w.hit[slot];
                 }
@@ -259,6 +264,8 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                 h.prim = __float_as_uint(h4.y);
                 h.slot = __float_as_uint(h4.z);
                 h.u = h.v = 0.0f;
+                const uint32_t fw = __float_as_uint(h4.w);
+                h.inst = fw >= 2u ? fw - 2u : kNoInst;
                 Aov aov;
                 NeeReq nr;
                 nr.kind = 0;
@@ -266,8 +273,8 @@ __global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
                     cont = false; // max_bounces == 0: the megakernel traces nothing for this sample
                 } else {
                     cont = V.set.mode == CRG_MODE_EXTENDED
-                               ? shade_extended(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr)
-                               : shade_faithful(S, V.set, C, depth, ps, h4.w != 0.0f, h, aov, nr);
+                               ? shade_extended(S, V.set, C, depth, ps, fw != 0u, h, aov, nr)
+                               : shade_faithful(S, V.set, C, depth, ps, fw != 0u, h, aov, nr);
                 }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
                 shadow = nr.kind != 0;
@@ -382,7 +389,8 @@ __global__ void __launch_bounds__(256) k_wf_extend_dyn(Wf w) {
         },
         [&](uint32_t slot, const Trav &T) {
             const bool found = T.best_prim != 0xFFFFFFFFu;
-            w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot), found ? 1.0f : 0.0f);
+            w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot),
+                                      pack_found(found, kNoInst));
         },
         st, err);
     if (err) atomicOr(&c->error, 1u);
@@ -800,11 +808,16 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.nchunks = (uint32_t)chunks.size();
     wf.P = P;
     wf.fetch = o.fetch;
-    wf.refill = o.refill;
+    // per-lane refill resumes a traversal of one mesh; a ray through instances
+    // loops over them, so batches with an instanced scene use the static kernels
+    bool instanced = false;
+    for (uint32_t i = 0; i < nscenes; ++i)
+        if (scenes[i]->ninst) instanced = true;
+    wf.refill = instanced ? 0u : o.refill;
     bool sun_requests = false; // the faithful estimator's sun test steps through alpha surfaces
     for (uint32_t v = 0; v < nviews; ++v)
         if (vdev[v].set.mode == CRG_MODE_FAITHFUL && scenes[vdev[v].scene]->sun_enabled) sun_requests = true;
-    wf.refill_sh = sun_requests ? 0u : o.refill;
+    wf.refill_sh = (sun_requests || instanced) ? 0u : o.refill;
     wf.o = (float4 *)take(n_f4);
     wf.d = (float4 *)take(n_f4);
     wf.T = (float4 *)take(n_f4);

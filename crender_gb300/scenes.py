@@ -152,6 +152,31 @@ def textured_box(seed=5):
     return dict(sc, mats=mats, mat_idx=mat_idx, uvs=uvs.reshape(-1, 6).astype(np.float32), textures=textures)
 
 
+def affine(translate=(0.0, 0.0, 0.0), rotate_deg=(0.0, 0.0, 0.0), scale=(1.0, 1.0, 1.0)):
+    """4x4 row-major T * Ry * Rx * Rz * S (float32)."""
+    ax, ay, az = np.radians(np.asarray(rotate_deg, np.float64))
+    rx = np.array([[1, 0, 0], [0, np.cos(ax), -np.sin(ax)], [0, np.sin(ax), np.cos(ax)]])
+    ry = np.array([[np.cos(ay), 0, np.sin(ay)], [0, 1, 0], [-np.sin(ay), 0, np.cos(ay)]])
+    rz = np.array([[np.cos(az), -np.sin(az), 0], [np.sin(az), np.cos(az), 0], [0, 0, 1]])
+    m = np.eye(4)
+    m[:3, :3] = ry @ rx @ rz @ np.diag(np.asarray(scale, np.float64))
+    m[:3, 3] = translate
+    return m.astype(np.float32)
+
+
+def instanced_box():
+    """Three instances of the box scene's mesh (cr::entity::instances): the
+    identity, a copy moved right, turned 30 degrees about y and scaled
+    non-uniformly, and a copy moved left and up, tilted 10 degrees about x;
+    the camera is pulled back to see all three."""
+    sc = box_scene()
+    inst = np.stack([affine(),
+                     affine((1.25, 0.0, 0.35), (0.0, 30.0, 0.0), (0.8, 1.1, 0.9)),
+                     affine((-1.2, 0.25, 0.2), (10.0, 0.0, 0.0), (1.0, 1.0, 1.0))])
+    camera = dict(position=(0.5, 0.65, -3.2), rotation=(0.0, 0.0, 0.0), fov=45.0, mode=0, scale=1.0)
+    return dict(sc, instances=inst, camera=camera)
+
+
 def soup(n=1 << 20, seed=1, sigma=0.01):
     """Random triangle soup: centroids U[0,1]^3, vertex offsets N(0, sigma^2) per axis."""
     rng = np.random.default_rng(seed)

@@ -203,6 +203,23 @@ crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun);
 crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba,
                                   const uint32_t *widths, const uint32_t *heights);
 
+/* Instances of the scene's mesh: `ninst` affine 4x4 transforms, 16 floats
+ * each, column-major as glm::mat4 stores them (last row 0 0 0 1).  Replaces
+ * cr::entity::instances::transforms and the per-instance loop of
+ * cr::model::intersect (src/objects/model.cpp:99-126, registry.cpp:73-74):
+ * a ray is transformed into each instance's object space (origin by
+ * inverse(T), direction by inverse(T) and renormalised), traced there with
+ * tnear 1e-5, and the hit whose world point T * p is closest to the ray
+ * origin wins (ties to the earlier instance).  The faithful estimator keeps
+ * the reference's object-space normal (model.cpp maps only the point back);
+ * the extended estimator shades with the world-space normal, and its emitter
+ * table holds one copy of every emissive triangle per instance, weighed by
+ * world area.  Inverses are formed once here (in double), not per ray.
+ * ninst = 0 (the default) uses the mesh as is, without any transform.  The
+ * BVH is not rebuilt.  Instanced batches run the wavefront form without
+ * per-lane refill. */
+crg_status crg_scene_set_instances(crg_scene *scene, const float *xforms, uint32_t ninst);
+
 /* Introspection of the built structure (for parity checks against a CPU build). */
 typedef struct crg_bvh_info {
     uint32_t ntri;

@@ -70,6 +70,8 @@ typedef struct orc_scene_desc {
     uint32_t ntex;               /* textures (crg_scene_set_textures) */
     const float *const *tex_rgba;
     const uint32_t *tex_w, *tex_h;
+    const float *xforms;         /* ninst*16 column-major affine transforms (crg_scene_set_instances), or NULL */
+    uint32_t ninst;
 } orc_scene_desc;
 
 typedef struct orc_film {
@@ -102,6 +104,12 @@ int orc_adjoint(const orc_scene_desc *scene, const crg_camera *cam, const crg_se
  * [h][w][4], restating cr::post_processor::process step by step
  * (src/render/post/post_processor.cpp:110-307). */
 int orc_post_process(const float *src, float *dst, uint32_t w, uint32_t h, const crg_post_settings *s);
+
+/* Batched queries on a scene description, instances included (the semantics
+ * of crg_intersect_closest / crg_intersect_any): hits (t = world distance) or,
+ * when occluded is non-NULL, any-hit flags. */
+int orc_scene_intersect(const orc_scene_desc *scene, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
+                        uint64_t n);
 
 /* Camera ray of pixel (px, py) with jitter (jx, jy) (for unit tests). */
 void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx,

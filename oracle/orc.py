@@ -112,6 +112,11 @@ def scene_desc(scene: dict, sun_enabled=False, sun=None, skybox=None, sky_rot=(0
         th = np.array([t.shape[0] for t in texs], np.uint32)
         keep += [texs, arr, tw, th]
         d.ntex, d.tex_rgba, d.tex_w, d.tex_h = len(texs), C.cast(arr, C.POINTER(C.c_void_p)), ptr(tw), ptr(th)
+    if scene.get("instances") is not None and len(scene["instances"]):
+        # [n, 4, 4] row-major -> column-major (glm::mat4 layout)
+        xf = np.ascontiguousarray(np.transpose(np.asarray(scene["instances"], np.float32), (0, 2, 1)))
+        keep.append(xf)
+        d.xforms, d.ninst = ptr(xf), len(xf)
     if skybox is not None:
         sk = np.ascontiguousarray(skybox, np.float32)
         keep.append(sk)
@@ -175,5 +180,20 @@ def post_process(img: np.ndarray, settings: _abi.PostSettings) -> np.ndarray:
     h, w = img.shape[:2]
     out = np.zeros_like(img)
     rc = lib().orc_post_process(ptr(img), ptr(out), w, h, C.byref(settings))
+    assert rc == 0, rc
+    return out
+
+
+def scene_intersect(scene: dict, rays: np.ndarray, any_hit=False):
+    """crg_intersect_closest / _any semantics on a scene dict (instances included)."""
+    d, keep = scene_desc(scene)
+    rays = np.ascontiguousarray(rays)
+    n = len(rays)
+    if any_hit:
+        out = np.zeros(n, np.uint32)
+        rc = lib().orc_scene_intersect(C.byref(d), ptr(rays), None, ptr(out), n)
+    else:
+        out = np.zeros(n, _abi.HIT_DTYPE)
+        rc = lib().orc_scene_intersect(C.byref(d), ptr(rays), ptr(out), None, n)
     assert rc == 0, rc
     return out

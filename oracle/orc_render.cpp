@@ -123,7 +123,14 @@ struct Scene {
     uint32_t ntex = 0;
     const float *const *tex_rgba = nullptr;
     const uint32_t *tex_w = nullptr, *tex_h = nullptr;
+    /* instances: per instance 24 floats, the inverse's 3 rows [A | t] then the
+     * forward transform's; empty = the mesh as is */
+    uint32_t ninst = 0;
+    std::vector<float> inst_rows;
+    std::vector<uint32_t> light_inst;
 };
+
+constexpr uint32_t kNoInst = 0xFFFFFFFFu;
 
 /* image::get_uv (src/objects/image.h:104-109): nearest texel, modulo wrap. */
 uint64_t texel_index(float u, uint32_t n) {
@@ -185,16 +192,122 @@ struct Ctx {
     uint64_t segments = 0, shadow = 0;
 };
 
-bool cast(const Scene &S, v3 o, v3 d, float tmax, crg_hit &h) {
-    crg_ray r{{o.x, o.y, o.z}, 1e-5f, {d.x, d.y, d.z}, tmax};
-    return orc_internal::closest(S.bvh, r, h);
+/* ---- instances (cr::entity::instances, model::intersect at model.cpp:99-126) */
+v3 xf_point(const float *R, v3 p) {
+    return mk(((R[0] * p.x + R[1] * p.y) + R[2] * p.z) + R[3], ((R[4] * p.x + R[5] * p.y) + R[6] * p.z) + R[7],
+              ((R[8] * p.x + R[9] * p.y) + R[10] * p.z) + R[11]);
 }
+v3 xf_vector(const float *R, v3 v) {
+    return mk((R[0] * v.x + R[1] * v.y) + R[2] * v.z, (R[4] * v.x + R[5] * v.y) + R[6] * v.z,
+              (R[8] * v.x + R[9] * v.y) + R[10] * v.z);
+}
+/* the object-space ray: inverse(T) (o, 1) and normalize(inverse(T) (d, 0)) */
+void inst_ray(const Scene &S, uint32_t j, v3 o, v3 d, v3 &oo, v3 &od, float &len) {
+    const float *R = &S.inst_rows[24 * (size_t)j];
+    oo = xf_point(R, o);
+    const v3 dr = xf_vector(R, d);
+    len = std::sqrt(dot(dr, dr));
+    od = normalize(dr);
+}
+v3 inst_point(const Scene &S, uint32_t j, v3 oo, v3 od, float t) {
+    return xf_point(&S.inst_rows[24 * (size_t)j + 12], add(oo, mul(od, t)));
+}
+float vdist(v3 a, v3 b) {
+    const v3 e = sub(a, b);
+    return std::sqrt(dot(e, e));
+}
+
+/* Closest hit.  Instanced scenes run the reference's loop literally: each
+ * instance traced to infinity in its object space, the world distance
+ * |T p - o| recomputed, the smaller one kept (ties to the earlier instance);
+ * h.t is then the object-space parameter and inst the instance. */
+bool cast_query(const Scene &S, v3 o, v3 d, float tmin, float tmax, crg_hit &h, uint32_t &inst) {
+    inst = kNoInst;
+    if (S.ninst == 0) {
+        crg_ray r{{o.x, o.y, o.z}, tmin, {d.x, d.y, d.z}, tmax};
+        return orc_internal::closest(S.bvh, r, h);
+    }
+    float best = tmax;
+    bool found = false;
+    for (uint32_t j = 0; j < S.ninst; ++j) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, j, o, d, oo, od, len);
+        crg_ray r{{oo.x, oo.y, oo.z}, tmin, {od.x, od.y, od.z}, kInf};
+        crg_hit hj;
+        if (!orc_internal::closest(S.bvh, r, hj)) continue;
+        const float dist = vdist(inst_point(S, j, oo, od, hj.t), o);
+        if (dist < best) {
+            best = dist;
+            h = hj;
+            inst = j;
+            found = true;
+        }
+    }
+    return found;
+}
+
+bool cast(const Scene &S, v3 o, v3 d, float tmax, crg_hit &h, uint32_t &inst) {
+    return cast_query(S, o, d, 1e-5f, tmax, h, inst);
+}
+
+/* Any hit below tmax; instanced: any instance with a hit whose object-space
+ * parameter is below tmax |inverse(T) d| / |d|. */
+bool occluded_query(const Scene &S, v3 o, v3 d, float tmin, float tmax) {
+    if (S.ninst == 0) {
+        crg_ray r{{o.x, o.y, o.z}, tmin, {d.x, d.y, d.z}, tmax};
+        return orc_internal::any(S.bvh, r);
+    }
+    const float dl = std::sqrt(dot(d, d));
+    for (uint32_t j = 0; j < S.ninst; ++j) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, j, o, d, oo, od, len);
+        crg_ray r{{oo.x, oo.y, oo.z}, tmin, {od.x, od.y, od.z}, (tmax * len) / dl};
+        if (orc_internal::any(S.bvh, r)) return true;
+    }
+    return false;
+}
+
+bool occluded(const Scene &S, v3 o, v3 d, float tmax) { return occluded_query(S, o, d, 1e-5f, tmax); }
 
 void tri_verts(const Scene &S, uint32_t prim, v3 &a, v3 &b, v3 &c) {
     const float *v = S.verts + (size_t)prim * 9;
     a = mk(v[0], v[1], v[2]);
     b = mk(v[3], v[4], v[5]);
     c = mk(v[6], v[7], v[8]);
+}
+
+/* World point, geometric normal and world distance of a closest hit.  The
+ * faithful estimator keeps an instanced hit's object-space normal, as
+ * model.cpp:117-121 maps only the point back; world_n transforms the
+ * triangle first. */
+struct Geom {
+    v3 p, Ng;
+    float dist;
+};
+Geom hit_geom(const Scene &S, const crg_hit &h, uint32_t inst, v3 o, v3 d, bool world_n) {
+    Geom g;
+    v3 a, b, c;
+    tri_verts(S, h.prim, a, b, c);
+    if (inst == kNoInst) {
+        g.p = add(o, mul(d, h.t));
+        g.dist = h.t;
+    } else {
+        v3 oo, od;
+        float len;
+        inst_ray(S, inst, o, d, oo, od, len);
+        g.p = inst_point(S, inst, oo, od, h.t);
+        g.dist = vdist(g.p, o);
+        if (world_n) {
+            const float *F = &S.inst_rows[24 * (size_t)inst + 12];
+            a = xf_point(F, a);
+            b = xf_point(F, b);
+            c = xf_point(F, c);
+        }
+    }
+    g.Ng = normalize(cross(sub(b, a), sub(c, a)));
+    return g;
 }
 
 /* sampling.h:156-166 (cr::sampling::sphere) */
@@ -219,17 +332,16 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
     v3 T = mk(1, 1, 1), L = mk(0, 0, 0);
     for (uint32_t i = 0; i < set.max_bounces; ++i) {
         crg_hit h;
+        uint32_t hinst;
         C.segments++;
-        if (!cast(S, o, d, kInf, h)) {
+        if (!cast(S, o, d, kInf, h, hinst)) {
             const v3 env = sample_sky(S, d);
             if (i == 0) aov.albedo = env;
             L = add(L, mulv(T, env));
             break;
         }
-        const v3 p = add(o, mul(d, h.t));
-        v3 a, b, c;
-        tri_verts(S, h.prim, a, b, c);
-        const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+        const Geom hg = hit_geom(S, h, hinst, o, d, false);
+        const v3 p = hg.p, Ng = hg.Ng;
         const crg_material &m = S.mats[S.mat_idx[h.prim]];
         float col[4];
         hit_colour(S, m, h, col);
@@ -267,7 +379,7 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
         if (i == 0) {
             aov.albedo = albedo;
             aov.normal = Ng;
-            aov.depth = h.t;
+            aov.depth = hg.dist;
         }
         T = mulv(T, albedo);
         L = add(L, mul(T, m.emission));
@@ -285,15 +397,16 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
                              (F.t.z * lv.x + F.n.z * lv.y) + F.b.z * lv.z);
             const float cosine = clampf(dot(Ng, sd), 0.0f, 1.0f);
             crg_hit sh;
+            uint32_t sinst;
             C.shadow++;
-            bool blocked = cast(S, so, sd, kInf, sh);
+            bool blocked = cast(S, so, sd, kInf, sh, sinst);
             while (blocked) {
                 float scol[4];
                 hit_colour(S, S.mats[S.mat_idx[sh.prim]], sh, scol);
                 if (scol[3] != 0.0f) break;
-                so = add(add(so, mul(sd, sh.t)), mul(sd, 0.1f));
+                so = add(hit_geom(S, sh, sinst, so, sd, false).p, mul(sd, 0.1f));
                 C.shadow++;
-                blocked = cast(S, so, sd, kInf, sh);
+                blocked = cast(S, so, sd, kInf, sh, sinst);
             }
             if (!blocked) {
                 const v3 ms = mk(-S.sun.direction[0], -S.sun.direction[1], -S.sun.direction[2]);
@@ -443,6 +556,12 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
     const uint32_t prim = S.light_prim[j];
     v3 a, b, c;
     tri_verts(S, prim, a, b, c);
+    if (S.ninst) {
+        const float *F = &S.inst_rows[24 * (size_t)S.light_inst[j] + 12];
+        a = xf_point(F, a);
+        b = xf_point(F, b);
+        c = xf_point(F, c);
+    }
     const float su = std::sqrt(g.y);
     const float b0 = 1.0f - su, b1 = su * (1.0f - g.z), b2 = su * g.z;
     const v3 pl = add(add(mul(a, b0), mul(b, b1)), mul(c, b2));
@@ -458,8 +577,7 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
     const float cos_l = absf(dot(Ngl, wi));
     if (!(cos_l > 0.0f)) return mk(0, 0, 0);
     C.shadow++;
-    crg_ray sr{{po.x, po.y, po.z}, 1e-5f, {wi.x, wi.y, wi.z}, dist * 0.999f};
-    if (orc_internal::any(S.bvh, sr)) return mk(0, 0, 0);
+    if (occluded(S, po, wi, dist * 0.999f)) return mk(0, 0, 0);
     const crg_material &lm = S.mats[S.mat_idx[prim]];
     const float *lc = lm.colour;
     if (textured(S, lm)) {
@@ -506,18 +624,17 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
     bool prev_delta = true;
     for (uint32_t i = 0; i < set.max_bounces; ++i) {
         crg_hit h;
+        uint32_t hinst;
         C.segments++;
-        if (!cast(S, o, d, kInf, h)) {
+        if (!cast(S, o, d, kInf, h, hinst)) {
             const v3 env = sample_sky(S, d);
             if (i == 0) aov.albedo = env;
             L = add(L, mulv(T, env));
             if (tape) tape->env(mulv(T, env));
             break;
         }
-        const v3 p = add(o, mul(d, h.t));
-        v3 a, b, c;
-        tri_verts(S, h.prim, a, b, c);
-        const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
+        const Geom hg = hit_geom(S, h, hinst, o, d, true);
+        const v3 p = hg.p, Ng = hg.Ng;
         const uint32_t mi = S.mat_idx[h.prim];
         const crg_material &m = S.mats[mi];
         float col[4];
@@ -532,7 +649,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
         if (i == 0) {
             aov.albedo = rgb;
             aov.normal = Ng;
-            aov.depth = h.t;
+            aov.depth = hg.dist;
         }
         if (m.emission > 0.0f) {
             const v3 Le = mk(col[0] * m.emission, col[1] * m.emission, col[2] * m.emission);
@@ -542,7 +659,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
             } else {
                 const float cos_l = absf(cos_nd);
                 if (cos_l > 0.0f) {
-                    const float pl = (S.mat_light_pdf[mi] * (h.t * h.t)) / cos_l;
+                    const float pl = (S.mat_light_pdf[mi] * (hg.dist * hg.dist)) / cos_l;
                     const float w = (prev_pdf * prev_pdf) / (prev_pdf * prev_pdf + pl * pl);
                     L = add(L, mul(mulv(T, Le), w));
                     if (tape) tape->emit(mul(mulv(T, Le), w), mi);
@@ -628,6 +745,36 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
     return L;
 }
 
+/* Inverse of an affine 4x4 (column-major) in double, rounded once to rows
+ * [A^-1 | -A^-1 t], followed by the forward rows [A | t] as given. */
+void inverse_rows(const float *x, float rows[24]) {
+    double a[3][3], t[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) a[r][c] = (double)x[4 * c + r];
+        t[r] = (double)x[12 + r];
+    }
+    double inv[3][3];
+    const double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+    const double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+    const double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    const double det = (a[0][0] * c00 + a[0][1] * c01) + a[0][2] * c02;
+    inv[0][0] = c00 / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = c01 / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = c02 / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) rows[4 * r + c] = (float)inv[r][c];
+        rows[4 * r + 3] = (float)-((inv[r][0] * t[0] + inv[r][1] * t[1]) + inv[r][2] * t[2]);
+        for (int c = 0; c < 3; ++c) rows[12 + 4 * r + c] = x[4 * c + r];
+        rows[12 + 4 * r + 3] = x[12 + r];
+    }
+}
+
 void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
     orc_bvh *bvh = nullptr;
     orc_bvh_build(D.verts, D.ntri, D.build, &bvh);
@@ -662,25 +809,46 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
             lum[m] = 0.2126 * (double)r + 0.7152 * (double)g + 0.0722 * (double)b;
         }
     }
+    /* instances: inverse rows formed in double and rounded once; the emitter
+     * table holds one entry per (instance, emissive triangle), instance-major,
+     * weighed by the world area */
+    S.ninst = (D.xforms && D.ninst) ? D.ninst : 0;
+    S.inst_rows.assign(24 * (size_t)S.ninst, 0.0f);
+    for (uint32_t j = 0; j < S.ninst; ++j) inverse_rows(D.xforms + 16 * (size_t)j, &S.inst_rows[24 * (size_t)j]);
     std::vector<double> w;
     double total = 0.0;
-    for (uint32_t p = 0; p < D.ntri; ++p) {
-        const uint32_t m = D.mat_idx[p];
-        if (!(lum[m] > 0.0)) continue;
-        const float *v = D.verts + (size_t)p * 9;
-        double e1[3], e2[3];
-        for (int a = 0; a < 3; ++a) {
-            e1[a] = (double)v[3 + a] - (double)v[a];
-            e2[a] = (double)v[6 + a] - (double)v[a];
+    const uint32_t ncopy = S.ninst ? S.ninst : 1;
+    for (uint32_t j = 0; j < ncopy; ++j)
+        for (uint32_t p = 0; p < D.ntri; ++p) {
+            const uint32_t m = D.mat_idx[p];
+            if (!(lum[m] > 0.0)) continue;
+            double wv[3][3];
+            for (int k = 0; k < 3; ++k) {
+                const float *v = D.verts + (size_t)p * 9 + 3 * k;
+                for (int r = 0; r < 3; ++r) {
+                    if (S.ninst) {
+                        const float *x = D.xforms + 16 * (size_t)j;
+                        wv[k][r] = (((double)x[r] * v[0] + (double)x[4 + r] * v[1]) + (double)x[8 + r] * v[2]) +
+                                   (double)x[12 + r];
+                    } else {
+                        wv[k][r] = (double)v[r];
+                    }
+                }
+            }
+            double e1[3], e2[3];
+            for (int a = 0; a < 3; ++a) {
+                e1[a] = wv[1][a] - wv[0][a];
+                e2[a] = wv[2][a] - wv[0][a];
+            }
+            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                         cz = e1[0] * e2[1] - e1[1] * e2[0];
+            const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+            const double wt = area * lum[m];
+            S.light_prim.push_back(p);
+            S.light_inst.push_back(j);
+            w.push_back(wt);
+            total += wt;
         }
-        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
-                     cz = e1[0] * e2[1] - e1[1] * e2[0];
-        const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-        const double wt = area * lum[m];
-        S.light_prim.push_back(p);
-        w.push_back(wt);
-        total += wt;
-    }
     S.mat_light_pdf.assign(D.nmat, 0.0f);
     if (!(total > 0.0)) {
         S.light_prim.clear();
@@ -871,6 +1039,37 @@ int orc_render(const orc_scene_desc *desc, const crg_camera *cam, const crg_sett
     const int rc = orc_render_rows(desc, cam, set, film, 0, set ? set->height : 0, nthreads);
     if (rc == CRG_OK) film->spp += set->spp;
     return rc;
+}
+
+int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
+                        uint64_t n) {
+    if (!desc || !rays || (!hits && !occluded)) return CRG_ERR_INVALID_ARG;
+    Scene S;
+    orc_bvh *bvh = nullptr;
+    prepare(*desc, S, &bvh);
+    for (uint64_t i = 0; i < n; ++i) {
+        const crg_ray &r = rays[i];
+        const v3 o = mk(r.org[0], r.org[1], r.org[2]), d = mk(r.dir[0], r.dir[1], r.dir[2]);
+        if (occluded) {
+            occluded[i] = occluded_query(S, o, d, r.tmin, r.tmax) ? 1u : 0u;
+            continue;
+        }
+        crg_hit h;
+        uint32_t inst;
+        if (cast_query(S, o, d, r.tmin, r.tmax, h, inst)) {
+            if (inst != kNoInst) {
+                v3 oo, od;
+                float len;
+                inst_ray(S, inst, o, d, oo, od, len);
+                h.t = vdist(inst_point(S, inst, oo, od, h.t), o);
+            }
+            hits[i] = h;
+        } else {
+            hits[i] = crg_hit{kInf, 0xFFFFFFFFu, 0.0f, 0.0f};
+        }
+    }
+    orc_bvh_free(bvh);
+    return CRG_OK;
 }
 
 } /* extern "C" */
