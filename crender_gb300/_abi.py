@@ -164,6 +164,8 @@ CRG_SIGNATURES = [
     ("crg_host_free", C.c_int, [vp, vp]),
     ("crg_scene_create", C.c_int, [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, P(vp)]),
     ("crg_scene_create_device", C.c_int, [vp, vp, C.c_uint32, vp, vp, C.c_uint32, P(vp)]),
+    ("crg_scene_create_indexed", C.c_int, [vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, C.c_uint32,
+                                           P(vp)]),
     ("crg_scene_destroy", C.c_int, [vp]),
     ("crg_scene_build", C.c_int, [vp, P(BuildOpts), c_stream]),
     ("crg_scene_set_skybox", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_float, C.c_float]),

@@ -129,6 +129,24 @@ class Scene:
             )
         )
 
+    @classmethod
+    def from_indexed(cls, ctx: Context, positions, vertex_indices, mat_idx, mats, texcoords=None, tex_indices=None):
+        """crg_scene_create_indexed: indexed positions / texture coordinates expanded on the device."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(vertex_indices, np.uint32).reshape(-1, 3)
+        self.mat_idx = np.ascontiguousarray(mat_idx, np.uint32)
+        self.mats = np.ascontiguousarray(mats)
+        tc = None if texcoords is None else np.ascontiguousarray(texcoords, np.float32).reshape(-1, 2)
+        ti = None if tex_indices is None else np.ascontiguousarray(tex_indices, np.int32).reshape(-1, 3)
+        self.ntri = len(idx)
+        self.h = C.c_void_p()
+        ctx.check(ctx.lib.crg_scene_create_indexed(ctx.h, ptr(pos), len(pos), ptr(idx), self.ntri, ptr(tc),
+                                                   0 if tc is None else len(tc), ptr(ti), ptr(self.mat_idx),
+                                                   ptr(self.mats), len(self.mats), C.byref(self.h)))
+        return self
+
     def set_instances(self, xforms):
         """crg_scene_set_instances: [n, 4, 4] row-major matrices (numpy convention), sent
         column-major as glm stores them; None or an empty array removes the instances."""

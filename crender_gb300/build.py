@@ -41,7 +41,8 @@ def build_host(libcrg: str) -> str:
     so = os.path.join(OUT, "libcrg_host.so")
     exe = os.path.join(OUT, "crg_host_selftest")
     link = ["-L", OUT, "-lcrg", "-Wl,-rpath,$ORIGIN", "-pthread"]
-    log = _run([CXX, *CXXFLAGS, "-shared", os.path.join(HOST, "crg_host.cpp"), "-o", so + ".tmp", *link])
+    log = _run([CXX, *CXXFLAGS, "-shared", os.path.join(HOST, "crg_host.cpp"), os.path.join(HOST, "obj_loader.cpp"),
+                "-o", so + ".tmp", *link])
     os.replace(so + ".tmp", so)
     log += _run([CXX, *CXXFLAGS, os.path.join(HOST, "selftest.cpp"), "-o", exe + ".tmp", "-lcrg_host", *link])
     os.replace(exe + ".tmp", exe)

@@ -4,6 +4,7 @@
 // records a message in the context.  Nothing here computes rays or samples:
 // the host side only validates arguments, copies inputs, prepares the
 // emissive-triangle table and launches kernels.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -105,20 +106,46 @@ __global__ void k_display(const float *__restrict__ sum, float4 *__restrict__ ou
     }
 }
 
+// persist_and_expand (registry.cpp:13-24) on the device: corner c of the
+// de-indexed mesh takes position vidx[c] and texture coordinate tidx[c]
+// ((0, 0) for -1 or an index past the coordinates).  Gathers 12 + 8 bytes and
+// writes 12 + 8 bytes per corner.
+__global__ void k_expand(const float *__restrict__ pos, const uint32_t *__restrict__ vidx, const float *__restrict__ tc,
+                         const int32_t *__restrict__ tidx, uint32_t ntc, float *__restrict__ verts, float *__restrict__ uvs,
+                         size_t ncorner) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncorner; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t k = vidx[c];
+        verts[3 * c + 0] = pos[3 * k + 0];
+        verts[3 * c + 1] = pos[3 * k + 1];
+        verts[3 * c + 2] = pos[3 * k + 2];
+        if (uvs) {
+            const int32_t t = tidx ? tidx[c] : -1;
+            float u = 0.0f, v = 0.0f;
+            if (t >= 0 && (uint32_t)t < ntc) {
+                u = tc[2 * (size_t)t];
+                v = tc[2 * (size_t)t + 1];
+            }
+            uvs[2 * c + 0] = u;
+            uvs[2 * c + 1] = v;
+        }
+    }
+}
+
 // Per-triangle areas in double from the float vertices (kept on the host so
 // the emitter table can be rebuilt when materials change).
+double tri_area_of(const float *v) {
+    double e1[3], e2[3];
+    for (int a = 0; a < 3; ++a) {
+        e1[a] = (double)v[3 + a] - (double)v[a];
+        e2[a] = (double)v[6 + a] - (double)v[a];
+    }
+    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+    return 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+}
+
 void compute_areas(crg_scene *s, const float *verts) {
     s->tri_area.assign(s->ntri, 0.0);
-    for (uint32_t p = 0; p < s->ntri; ++p) {
-        const float *v = verts + (size_t)p * 9;
-        double e1[3], e2[3];
-        for (int a = 0; a < 3; ++a) {
-            e1[a] = (double)v[3 + a] - (double)v[a];
-            e2[a] = (double)v[6 + a] - (double)v[a];
-        }
-        const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
-        s->tri_area[p] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-    }
+    for (uint32_t p = 0; p < s->ntri; ++p) s->tri_area[p] = tri_area_of(verts + (size_t)p * 9);
 }
 
 // Emissive triangles weighted by area x luminance of colour*emission (double
@@ -405,6 +432,66 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
     }
     if (rc == CRG_OK) {
         compute_areas(s, verts);
+        rc = prepare_lights(s);
+    }
+    if (rc != CRG_OK) {
+        scene_free(s);
+        return rc;
+    }
+    *out = s;
+    return CRG_OK;
+}
+
+crg_status crg_scene_create_indexed(crg_context *ctx, const float *positions, uint32_t npos, const uint32_t *vertex_indices,
+                                    uint32_t ntri, const float *texcoords, uint32_t ntc, const int32_t *tex_indices,
+                                    const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat, crg_scene **out) {
+    if (ntri > 0 && (!positions || !vertex_indices)) return set_error(ctx, CRG_ERR_INVALID_ARG, "null positions or indices");
+    if (ntc > 0 && !texcoords) return set_error(ctx, CRG_ERR_INVALID_ARG, "null texture coordinates");
+    if (out) *out = nullptr;
+    for (size_t c = 0; c < 3 * (size_t)ntri; ++c)
+        if (vertex_indices[c] >= npos) return set_error(ctx, CRG_ERR_INVALID_ARG, "vertex index out of range");
+    crg_scene *s = nullptr;
+    crg_status rc = scene_common(ctx, ntri, mat_idx, mats, nmat, out, s);
+    const bool want_uv = tex_indices != nullptr;
+    DevBuf dpos, didx, dtc, dti;
+    const size_t nc = 3 * (size_t)ntri;
+    if (rc == CRG_OK) rc = dev_alloc(ctx, s->verts, sizeof(float) * 9 * (size_t)(ntri ? ntri : 1));
+    if (rc == CRG_OK && ntri) {
+        if (rc == CRG_OK) rc = dev_alloc(ctx, dpos, sizeof(float) * 3 * (size_t)npos);
+        if (rc == CRG_OK) rc = dev_alloc(ctx, didx, sizeof(uint32_t) * nc);
+        if (rc == CRG_OK && want_uv) rc = dev_alloc(ctx, s->uvs, sizeof(float) * 6 * (size_t)ntri);
+        if (rc == CRG_OK && want_uv) rc = dev_alloc(ctx, dti, sizeof(int32_t) * nc);
+        if (rc == CRG_OK && want_uv && ntc) rc = dev_alloc(ctx, dtc, sizeof(float) * 2 * (size_t)ntc);
+        cudaError_t e = cudaSuccess;
+        if (rc == CRG_OK) e = cudaMemcpy(dpos.ptr, positions, sizeof(float) * 3 * (size_t)npos, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess) e = cudaMemcpy(didx.ptr, vertex_indices, sizeof(uint32_t) * nc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess && want_uv)
+            e = cudaMemcpy(dti.ptr, tex_indices, sizeof(int32_t) * nc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess && want_uv && ntc)
+            e = cudaMemcpy(dtc.ptr, texcoords, sizeof(float) * 2 * (size_t)ntc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess) {
+            const unsigned blocks = (unsigned)std::min<size_t>((nc + 255) / 256, (size_t)std::max(ctx->sm_count, 1) * 8);
+            k_expand<<<blocks, 256>>>((const float *)dpos.ptr, (const uint32_t *)didx.ptr, (const float *)dtc.ptr,
+                                      (const int32_t *)dti.ptr, want_uv ? ntc : 0, (float *)s->verts.ptr,
+                                      want_uv ? (float *)s->uvs.ptr : nullptr, nc);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        }
+        if (rc == CRG_OK && e != cudaSuccess) rc = cuda_error(ctx, e, "k_expand");
+    }
+    dev_free(dpos);
+    dev_free(didx);
+    dev_free(dtc);
+    dev_free(dti);
+    if (rc == CRG_OK) {
+        // emitter areas from the same float positions the device copied
+        float tv[9];
+        s->tri_area.assign(ntri, 0.0);
+        for (uint32_t p = 0; p < ntri; ++p) {
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
+            s->tri_area[p] = tri_area_of(tv);
+        }
         rc = prepare_lights(s);
     }
     if (rc != CRG_OK) {

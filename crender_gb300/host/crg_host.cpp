@@ -140,20 +140,25 @@ void scene::add_model(const model_data &m) {
         if (k >= m.vertices.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: vertex index out of range");
     for (uint32_t k : m.material_indices)
         if (k >= m.materials.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: material index out of range");
-    if (have_uv)
-        for (uint32_t k : m.texture_indices)
-            if (k >= m.texture_coords.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: uv index out of range");
-    const uint32_t mat_base = (uint32_t)materials_.size();
-    verts_.reserve(verts_.size() + ntri * 9);
-    uvs_.reserve(uvs_.size() + ntri * 6);
+    for (const material_information &mi : m.materials)
+        if (mi.tex && *mi.tex >= m.textures.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: texture index out of range");
+    // register_model (registry.cpp:51-97) keeps the model's own index space;
+    // here the indices are rebased onto the scene-wide arrays
+    const uint32_t pos_base = (uint32_t)(positions_.size() / 3), tc_base = (uint32_t)(texcoords_.size() / 2);
+    const uint32_t mat_base = (uint32_t)materials_.size(), tex_base = (uint32_t)textures_.size();
+    for (const vec3 &v : m.vertices) positions_.insert(positions_.end(), {v.x, v.y, v.z});
+    for (const vec2 &t : m.texture_coords) texcoords_.insert(texcoords_.end(), {t.x, t.y});
     for (size_t i = 0; i < ni; ++i) {
-        const vec3 &v = m.vertices[m.vertex_indices[i]];
-        verts_.insert(verts_.end(), {v.x, v.y, v.z});
-        const vec2 uv = have_uv ? m.texture_coords[m.texture_indices[i]] : vec2{};
-        uvs_.insert(uvs_.end(), {uv.x, uv.y});
+        vidx_.push_back(pos_base + m.vertex_indices[i]);
+        const uint32_t t = have_uv ? m.texture_indices[i] : 0xFFFFFFFFu;
+        tidx_.push_back(t < m.texture_coords.size() ? (int32_t)(tc_base + t) : -1);
     }
     for (size_t t = 0; t < ntri; ++t) mat_idx_.push_back(mat_base + m.material_indices[t]);
-    materials_.insert(materials_.end(), m.materials.begin(), m.materials.end());
+    for (material_information mi : m.materials) {
+        if (mi.tex) mi.tex = tex_base + *mi.tex;
+        materials_.push_back(mi);
+    }
+    textures_.insert(textures_.end(), m.textures.begin(), m.textures.end());
     dirty_ = true;
 }
 
@@ -202,9 +207,21 @@ void scene::commit() {
     std::vector<crg_material> mats(materials_.size());
     for (size_t i = 0; i < mats.size(); ++i) mats[i] = to_crg(materials_[i]);
     crg_scene *fresh = nullptr;
-    check(crg_scene_create(ctx_, verts_.data(), (uint32_t)mat_idx_.size(), uvs_.data(), mat_idx_.data(), mats.data(),
-                           (uint32_t)mats.size(), &fresh));
-    crg_status s = crg_scene_build(fresh, &opts_, nullptr);
+    check(crg_scene_create_indexed(ctx_, positions_.data(), (uint32_t)(positions_.size() / 3), vidx_.data(),
+                                   (uint32_t)mat_idx_.size(), texcoords_.data(), (uint32_t)(texcoords_.size() / 2),
+                                   tidx_.data(), mat_idx_.data(), mats.data(), (uint32_t)mats.size(), &fresh));
+    crg_status s = CRG_OK;
+    if (!textures_.empty()) {
+        std::vector<const float *> px;
+        std::vector<uint32_t> w, h;
+        for (const image &t : textures_) {
+            px.push_back(t.data());
+            w.push_back((uint32_t)t.width());
+            h.push_back((uint32_t)t.height());
+        }
+        s = crg_scene_set_textures(fresh, (uint32_t)px.size(), px.data(), w.data(), h.data());
+    }
+    if (s == CRG_OK) s = crg_scene_build(fresh, &opts_, nullptr);
     if (s == CRG_OK && skybox_)
         s = crg_scene_set_skybox(fresh, skybox_->data(), (uint32_t)skybox_->width(), (uint32_t)skybox_->height(),
                                  sky_rot_.x, sky_rot_.y);
@@ -256,13 +273,22 @@ std::vector<intersection_record> scene::cast_rays(const std::vector<ray> &rays) 
         rec.prim_id = h.prim;
         rec.distance = h.t;
         rec.material = &materials_[mat_idx_[h.prim]];
-        const float *v = &verts_[(size_t)h.prim * 9];
+        float v[9];
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) v[3 * k + a] = positions_[3 * (size_t)vidx_[3 * (size_t)h.prim + k] + a];
         const double e1[3] = {(double)v[3] - v[0], (double)v[4] - v[1], (double)v[5] - v[2]};
         const double e2[3] = {(double)v[6] - v[0], (double)v[7] - v[1], (double)v[8] - v[2]};
         double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
         const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
         if (len > 0) rec.normal = {(float)(n[0] / len), (float)(n[1] / len), (float)(n[2] / len)};
-        const float *uv = &uvs_[(size_t)h.prim * 6];
+        float uv[6] = {0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 3; ++k) {
+            const int32_t t = tidx_[3 * (size_t)h.prim + k];
+            if (t >= 0) {
+                uv[2 * k] = texcoords_[2 * (size_t)t];
+                uv[2 * k + 1] = texcoords_[2 * (size_t)t + 1];
+            }
+        }
         const float w0 = 1.0f - h.u - h.v;
         rec.uv = {w0 * uv[0] + h.u * uv[2] + h.v * uv[4], w0 * uv[1] + h.u * uv[3] + h.v * uv[5]};
         const ray &r = rays[i];

@@ -51,7 +51,7 @@ public:
 };
 
 // cr::material::information without the GL texture plumbing: `tex` indexes
-// model_data::textures (texture sampling is not on the GPU path; see crg.h).
+// model_data::textures (sampled on the GPU, crg_scene_set_textures).
 struct material_information {
     enum type : unsigned char { metal = CRG_SHADE_METAL, smooth = CRG_SHADE_SMOOTH, glass = CRG_SHADE_GLASS };
     type shade_type = smooth;
@@ -92,9 +92,26 @@ struct model_data {
     std::vector<image> textures;
     std::vector<uint32_t> vertex_indices;   // 3 per triangle
     std::vector<uint32_t> material_indices; // 1 per triangle, into materials
-    std::vector<uint32_t> texture_indices;
+    std::vector<uint32_t> texture_indices;  // 3 per triangle or empty; 0xFFFFFFFF = none
     std::vector<uint32_t> normal_indices;
+    std::vector<std::string> texture_names; // map_Kd of each material ("" = none), as the MTL gave them
 };
+
+// Loads a Wavefront OBJ (and the MTL files it names, relative to `folder`,
+// default the OBJ's own folder) the way cr::asset_loader::load_model does
+// through tinyobjloader (src/util/asset_loader.cpp:182-303): positions,
+// texture coordinates and normals as listed; faces in file order,
+// triangulated (triangles as given, quads split along the shorter diagonal as
+// tinyobjloader does, larger polygons as a fan from their first corner);
+// 1-based or negative (relative) indices; one material per face from
+// `usemtl` (colour = Kd with alpha 1, smooth, no emission).  Faces before any
+// `usemtl`, or naming an unknown material, get an extra default material at
+// the end of the table (tinyobjloader reports -1 there, which the reference
+// would index out of bounds).  Image files named by map_Kd are recorded in
+// texture_names but not decoded (no image codec here): the material keeps its
+// Kd colour, as the reference does when a texture fails to load.  Throws
+// crg::host::error on unreadable files or malformed records.
+model_data load_model(const std::string &file, const std::string &folder = "");
 
 struct ray {
     vec3 origin, direction;
@@ -173,8 +190,13 @@ private:
     crg_scene *scene_ = nullptr;
     bool dirty_ = true;
     crg_build_opts opts_{8, 1, 3, 3};
-    std::vector<float> verts_;     // 9 per triangle
-    std::vector<float> uvs_;       // 6 per triangle
+    // models as added, indexed; expanded on the device at commit
+    // (crg_scene_create_indexed), so the host never holds the de-indexed copy
+    std::vector<float> positions_;  // 3 per vertex, all models
+    std::vector<uint32_t> vidx_;    // 3 per triangle, into positions_
+    std::vector<float> texcoords_;  // 2 per coordinate, all models
+    std::vector<int32_t> tidx_;     // 3 per triangle, into texcoords_ (-1 = none)
+    std::vector<image> textures_;   // all models' textures
     std::vector<uint32_t> mat_idx_;
     std::vector<material_information> materials_;
     std::optional<image> skybox_;

@@ -10,6 +10,7 @@
 // out: u64 spp1; float sums1[W*H*3]; u64 spp2; float sums2[W*H*3];
 //      u64 total_rays; per ray: u32 prim, float distance, float normal[3]
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -49,11 +50,76 @@ model_data make_model(const std::vector<float> &v, const std::vector<uint32_t> &
     return m;
 }
 
+// crg_host_selftest obj <file.obj> <out>: load_model only (no device).
+// out: u32 npos, ntc, ntri, nmat; float positions[npos*3]; float texcoords[ntc*2];
+//      u32 vertex_indices[ntri*3]; u32 texture_indices[ntri*3] (0xFFFFFFFF = none);
+//      u32 material_indices[ntri]; float colours[nmat*4]
+int obj_parse(const char *file, const char *out) {
+    try {
+        const model_data m = load_model(file);
+        FILE *g = std::fopen(out, "wb");
+        if (!g) return 2;
+        const uint32_t ntri = (uint32_t)(m.vertex_indices.size() / 3);
+        const uint32_t h[4] = {(uint32_t)m.vertices.size(), (uint32_t)m.texture_coords.size(), ntri,
+                               (uint32_t)m.materials.size()};
+        wr(g, h, 4);
+        for (const vec3 &v : m.vertices) wr(g, &v.x, 3);
+        for (const vec2 &t : m.texture_coords) wr(g, &t.x, 2);
+        wr(g, m.vertex_indices.data(), m.vertex_indices.size());
+        std::vector<uint32_t> ti(m.texture_indices);
+        if (ti.empty()) ti.assign(m.vertex_indices.size(), 0xFFFFFFFFu);
+        wr(g, ti.data(), ti.size());
+        wr(g, m.material_indices.data(), m.material_indices.size());
+        for (const material_information &mi : m.materials) wr(g, mi.colour, 4);
+        std::fclose(g);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "selftest: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// crg_host_selftest objrender <file.obj> <out> <W> <H> <spp>: load_model ->
+// scene::add_model (indexed, expanded on the device) -> faithful renderer with
+// the default sun, camera at (0, 0.5, -3) looking down +z, 60 degrees.
+// out: u64 spp; float sums[W*H*3]
+int obj_render(const char *file, const char *out, uint32_t W, uint32_t H, uint32_t spp) {
+    try {
+        scene sc(0);
+        sc.add_model(load_model(file));
+        camera *c = sc.camera();
+        c->fov = 60.0f;
+        c->rotate(vec3{0, 0, 0});
+        c->position = vec3{0.0f, 0.5f, -3.0f};
+        renderer::options o;
+        o.mode = CRG_MODE_FAITHFUL;
+        o.target_spp = spp;
+        renderer r(W, H, 6, &sc, o);
+        if (!r.wait_for_target(120.0)) return 1;
+        const uint64_t n = r.current_sample_count();
+        const std::vector<float> s1 = r.current_sums();
+        FILE *g = std::fopen(out, "wb");
+        if (!g) return 2;
+        wr(g, &n, 1);
+        wr(g, s1.data(), s1.size());
+        std::fclose(g);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "selftest: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char **argv) {
+    if (argc == 4 && std::strcmp(argv[1], "obj") == 0) return obj_parse(argv[2], argv[3]);
+    if (argc == 7 && std::strcmp(argv[1], "objrender") == 0)
+        return obj_render(argv[2], argv[3], (uint32_t)std::atoi(argv[4]), (uint32_t)std::atoi(argv[5]),
+                          (uint32_t)std::atoi(argv[6]));
     if (argc != 3) {
-        std::fprintf(stderr, "usage: %s <in> <out>\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <in> <out> | obj <file.obj> <out> | objrender <file.obj> <out> <W> <H> <spp>\n",
+                     argv[0]);
         return 2;
     }
     FILE *f = std::fopen(argv[1], "rb");

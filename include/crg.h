@@ -176,6 +176,21 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
 crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint32_t ntri,
                                    const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
                                    crg_scene **out);
+/* Same, from indexed geometry as the OBJ loader returns it
+ * (cr::asset_loader::model_data, src/util/asset_loader.cpp:182-303), expanded
+ * on the device instead of on the host (persist_and_expand in
+ * cr::registry::register_model, src/render/entities/registry.cpp:13-24, 51-66):
+ *   positions      host float[npos*3]
+ *   vertex_indices host uint32[ntri*3], each < npos
+ *   texcoords      optional host float[ntc*2]
+ *   tex_indices    optional host int32[ntri*3]; NULL = no texture coordinates;
+ *                  -1 or >= ntc gives (0, 0) (the reference would read out of bounds)
+ *   mat_idx, mats  as crg_scene_create
+ * Triangle p is (positions[vertex_indices[3p + k]], k = 0..2). */
+crg_status crg_scene_create_indexed(crg_context *ctx, const float *positions, uint32_t npos,
+                                    const uint32_t *vertex_indices, uint32_t ntri, const float *texcoords,
+                                    uint32_t ntc, const int32_t *tex_indices, const uint32_t *mat_idx,
+                                    const crg_material *mats, uint32_t nmat, crg_scene **out);
 crg_status crg_scene_destroy(crg_scene *scene);
 
 /* Builds the acceleration structure: LBVH (Morton codes, radix sort, Karras
