@@ -188,6 +188,7 @@ CRG_SIGNATURES = [
     ("crg_film_display", C.c_int, [vp, vp, c_stream]),
     ("crg_post_settings_default", C.c_int, [P(PostSettings)]),
     ("crg_post_process", C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, P(PostSettings), c_stream]),
+    ("crg_draft_render", C.c_int, [vp, P(Camera), C.c_uint32, C.c_uint32, C.c_float, vp, c_stream]),
     ("crg_render", C.c_int, [vp, P(Camera), P(Settings), vp, c_stream]),
     ("crg_scene_set_materials", C.c_int, [vp, vp, C.c_uint32]),
     ("crg_backward", C.c_int, [vp, P(Camera), P(Settings), vp, vp, vp, c_stream]),
@@ -257,6 +258,7 @@ ORC_SIGNATURES = [
     ("orc_adjoint", C.c_int, [P(OrcSceneDesc), P(Camera), P(Settings), vp, vp, vp, C.c_int]),
     ("orc_post_process", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, P(PostSettings)]),
     ("orc_scene_intersect", C.c_int, [P(OrcSceneDesc), vp, vp, vp, C.c_uint64]),
+    ("orc_draft_render", C.c_int, [P(OrcSceneDesc), P(Camera), C.c_uint32, C.c_uint32, C.c_float, vp]),
     ("orc_camera_ray", None, [P(Camera), P(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_float, vp, vp]),
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),

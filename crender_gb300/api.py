@@ -370,3 +370,10 @@ def film_display(film: Film, dst: DeviceBuffer, stream=None):
     """crg_film_display: clamp(sum / spp, 0, 1)^(1/2.2) into a device RGBA32F image."""
     assert dst.nbytes >= film.width * film.height * 16
     film.ctx.check(film.ctx.lib.crg_film_display(film.h, dst.ptr, stream))
+
+
+def draft_render(scene: Scene, camera: dict, width: int, height: int, dst: DeviceBuffer, aspect=1.0, stream=None):
+    """crg_draft_render: unlit nearest-surface colour over the skybox (cr::draft_renderer)."""
+    assert dst.nbytes >= width * height * 16
+    cam = make_camera(camera)
+    scene.ctx.check(scene.ctx.lib.crg_draft_render(scene.h, C.byref(cam), width, height, float(aspect), dst.ptr, stream))

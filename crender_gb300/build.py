@@ -16,7 +16,7 @@ from concurrent.futures import ThreadPoolExecutor
 ROOT = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(ROOT, "csrc")
 OUT = os.path.join(ROOT, "_build")
-SOURCES = ["crg_api.cu", "bvh_build.cu", "traverse.cu", "render.cu", "wavefront.cu", "adjoint.cu", "autotune.cu", "post.cu"]
+SOURCES = ["crg_api.cu", "bvh_build.cu", "traverse.cu", "render.cu", "wavefront.cu", "adjoint.cu", "autotune.cu", "post.cu", "draft.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",

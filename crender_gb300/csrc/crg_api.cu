@@ -801,6 +801,18 @@ crg_status crg_film_display(crg_film *film, float *d_rgba, crg_stream stream) {
     return CRG_OK;
 }
 
+crg_status crg_draft_render(crg_scene *scene, const crg_camera *camera, uint32_t width, uint32_t height, float aspect,
+                            float *d_rgba, crg_stream stream) {
+    if (!scene || !camera || !d_rgba) return set_error(scene ? scene->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
+    crg_context *ctx = scene->ctx;
+    if (!scene->built) return set_error(ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (width == 0 || height == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty image");
+    if ((uint64_t)width * height >= (1ull << 32)) return set_error(ctx, CRG_ERR_INVALID_ARG, "image too large");
+    if (camera->mode > CRG_CAMERA_ORTHOGRAPHIC) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad camera mode");
+    if (scene->ntri == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "scene has no triangles");
+    return launch_draft(scene, camera_params(*camera), width, height, aspect, d_rgba, (cudaStream_t)stream);
+}
+
 crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_settings *settings, crg_film *film, crg_stream stream) {
     if (!scene || !camera || !settings || !film) return set_error(scene ? scene->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
     crg_context *ctx = scene->ctx;

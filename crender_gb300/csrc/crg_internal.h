@@ -117,6 +117,10 @@ CamDev camera_params(const crg_camera &c);
 crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film,
                          cudaStream_t stream);
 
+// draft.cu
+crg_status launch_draft(crg_scene *s, const CamDev &cam, uint32_t w, uint32_t h, float aspect, float *d_rgba,
+                        cudaStream_t stream);
+
 // adjoint.cu
 crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &set, const float *adj, double *g_col,
                            double *g_em, cudaStream_t stream);

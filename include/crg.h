@@ -394,6 +394,19 @@ crg_status crg_post_settings_default(crg_post_settings *settings);
 crg_status crg_post_process(crg_context *ctx, const float *d_src, float *d_dst, uint32_t width, uint32_t height,
                             const crg_post_settings *settings, crg_stream stream);
 
+/* ------------------------------------------------------------------ draft preview */
+
+/* Draft-mode preview: the unlit colour of the nearest surface at every pixel
+ * centre (the material colour, or its texture at the hit's texture coordinate
+ * with its alpha) over the skybox, into a device RGBA32F image [height][width][4]
+ * in the film's pixel layout.  Replaces cr::draft_renderer::render's OpenGL
+ * passes (src/render/draft/draft_renderer.cpp:150-271, draft_mode.vert/.frag,
+ * draft_mode_background.comp) with one ray per pixel through the built BVH;
+ * the rasteriser's near / far planes (0.1 / 10000 along the view axis, 0.01
+ * for orthographic) bound the rays.  `aspect` as crg_settings::aspect. */
+crg_status crg_draft_render(crg_scene *scene, const crg_camera *camera, uint32_t width, uint32_t height, float aspect,
+                            float *d_rgba, crg_stream stream);
+
 /* ------------------------------------------------------------------ render */
 
 /* Renders settings->spp more samples per pixel into the film with the

@@ -111,6 +111,10 @@ int orc_post_process(const float *src, float *dst, uint32_t w, uint32_t h, const
 int orc_scene_intersect(const orc_scene_desc *scene, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
                         uint64_t n);
 
+/* Draft preview (crg_draft_render semantics) into rgba[h*w*4]. */
+int orc_draft_render(const orc_scene_desc *scene, const crg_camera *cam, uint32_t w, uint32_t h, float aspect,
+                     float *rgba);
+
 /* Camera ray of pixel (px, py) with jitter (jx, jy) (for unit tests). */
 void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx,
                     float jy, float *org, float *dir);

@@ -197,3 +197,15 @@ def scene_intersect(scene: dict, rays: np.ndarray, any_hit=False):
         rc = lib().orc_scene_intersect(C.byref(d), ptr(rays), ptr(out), None, n)
     assert rc == 0, rc
     return out
+
+
+def draft_render(scene: dict, camera: dict, width: int, height: int, aspect=1.0, **kw):
+    """crg_draft_render semantics on the CPU: RGBA32F [height * width * 4], film layout."""
+    from crender_gb300.api import make_camera
+
+    d, keep = scene_desc(scene, **kw)
+    out = np.zeros(width * height * 4, np.float32)
+    cam = make_camera(camera)
+    rc = lib().orc_draft_render(C.byref(d), C.byref(cam), width, height, float(aspect), ptr(out))
+    assert rc == 0, rc
+    return out

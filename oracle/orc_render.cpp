@@ -1041,6 +1041,45 @@ int orc_render(const orc_scene_desc *desc, const crg_camera *cam, const crg_sett
     return rc;
 }
 
+/* Draft preview (cr::draft_renderer, draft_renderer.cpp:150-271): the unlit
+ * colour of the nearest surface at each pixel centre, within the
+ * rasteriser's near / far planes, over the skybox; film pixel layout. */
+int orc_draft_render(const orc_scene_desc *desc, const crg_camera *cam, uint32_t w, uint32_t h, float aspect,
+                     float *rgba) {
+    if (!desc || !cam || !rgba || w == 0 || h == 0) return CRG_ERR_INVALID_ARG;
+    Scene S;
+    orc_bvh *bvh = nullptr;
+    prepare(*desc, S, &bvh);
+    const CamParams cp = camera_params(*cam);
+    const v3 fwd = mk(cp.R[0][2], cp.R[1][2], cp.R[2][2]);
+    const float zn = cam->mode == CRG_CAMERA_ORTHOGRAPHIC ? 0.01f : 0.1f;
+    for (uint32_t py = 0; py < h; ++py)
+        for (uint32_t px = 0; px < w; ++px) {
+            const float x = ((float)px + 0.5f) / (float)w, y = ((float)py + 0.5f) / (float)h;
+            v3 o, d;
+            camera_ray(cp, x, y, aspect, o, d);
+            const float cz = dot(d, fwd);
+            crg_hit hit;
+            uint32_t inst = kNoInst;
+            float c[4];
+            if (cz > 0.0f && cast_query(S, o, d, zn / cz, 10000.0f / cz, hit, inst)) {
+                const crg_material &m = S.mats[S.mat_idx[hit.prim]];
+                hit_colour(S, m, hit, c);
+                if (!textured(S, m)) c[3] = 1.0f;
+            } else {
+                const v3 e = sample_sky(S, d);
+                c[0] = e.x;
+                c[1] = e.y;
+                c[2] = e.z;
+                c[3] = 1.0f;
+            }
+            float *out = rgba + ((size_t)(w - 1 - px) + (size_t)(h - 1 - py) * w) * 4;
+            for (int k = 0; k < 4; ++k) out[k] = c[k];
+        }
+    orc_bvh_free(bvh);
+    return CRG_OK;
+}
+
 int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
                         uint64_t n) {
     if (!desc || !rays || (!hits && !occluded)) return CRG_ERR_INVALID_ARG;
