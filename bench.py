@@ -112,7 +112,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+POST = dict(width=3840, height=2160)
+
+
+def post_settings_full(api):
+    """Every post-processing pass on: bloom (threshold 0.7, strength 1), gray scale off,
+    Uncharted tone curve with exposure 1.5 and gamma 2.2, every pixel covered."""
+    return api.post_settings(bloom=1, tonemapping=1, tonemap_type=3, exposure=1.5, mode=1)
+
+
+def post_image(w, h):
+    r = np.random.default_rng(7)
+    img = r.gamma(0.6, 0.8, (h, w, 4)).astype(np.float32)
+    img[..., 3] = 1.0
+    return img
+
+
 def workload_config(w):
+    if w == "post":
+        return {"workload": "post-processing of a 3840x2160 RGBA32F image: bloom threshold + 10 separable 15-tap "
+                            "blur passes + composite with the Uncharted tone curve (every pixel covered)",
+                "resolution": [POST["width"], POST["height"]], "l2": L2_NOTE}
     if w == "batch":
         return {"workload": "64 uneven views of the box (36 tris) and displaced (4,196,562 tris) scenes, "
                             "resolutions 128^2..1920x1080, spp 16/64/256, depth 8/16, RR from 3, extended estimator; "
@@ -153,6 +173,15 @@ def cpu_leg(workload):
         b.closest(rays)
         dt = time.perf_counter() - t0
         return (1 << 22) / dt / 1e6, f"4,194,304 of the 16,777,216 primary rays on the soup ({dt:.1f} s)"
+    if workload == "post":
+        from crender_gb300 import api as capi
+
+        W, H = POST["width"], POST["height"]
+        img = post_image(W, H)
+        t0 = time.perf_counter()
+        orc.post_process(img, post_settings_full(capi))
+        dt = time.perf_counter() - t0
+        return W * H / dt / 1e6, f"one full 3840x2160 image on one host core ({dt:.1f} s)"
     if workload == "inverse":
         sc = scenes.inverse_box(albedo=np.full((34, 3), 0.5), light_colour=np.full(3, 10 / 17))
         st = api.make_settings(256, 256, 32, 8, 3, 1, 1)
@@ -190,7 +219,7 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
-    unit = "Mrays/s" if args.workload == "soup" else "Msamples/s"
+    unit = {"soup": "Mrays/s", "post": "Mpixels/s"}.get(args.workload, "Msamples/s")
     print(json.dumps({
         "impl": "reference", "metric": unit, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -396,7 +425,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="crg", choices=["crg", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup", "inverse"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "box", "displaced", "soup", "inverse", "post"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE leg")
     ap.add_argument("--form", default="megakernel", choices=["megakernel", "wavefront"],
@@ -431,7 +460,7 @@ def main():
     timer = Timer(torch, stream, lambda: flush.fill_(rank & 0xFF))
     peak, peak_kind = measured_peaks()
     out = {}
-    unit = "Mrays/s" if args.workload == "soup" else "Msamples/s"
+    unit = {"soup": "Mrays/s", "post": "Mpixels/s"}.get(args.workload, "Msamples/s")
 
     if args.workload == "batch":
         box, disp = scenes.box_scene(), scenes.displaced_scene()
@@ -604,6 +633,43 @@ def main():
             out["time_to_rmse"] = time_to_rmse(ctx, api, scenes, timer, S)
     elif args.workload == "inverse":
         units, algo, kernel, launches, clk, ms = inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch)
+    elif args.workload == "post":
+        unit = "Mpixels/s"
+        W, H = POST["width"], POST["height"]
+        img = post_image(W, H)
+        src = api.DeviceBuffer.from_array(ctx, img)
+        dst = api.DeviceBuffer(ctx, img.nbytes)
+        ps = post_settings_full(api)
+        units = W * H
+        # per pixel: pass 0 reads the source and writes 16 B, passes 1-9 read and write 16 B each,
+        # the composite reads source + bloom and writes the output
+        algo = units * (10 * 32 + 48)
+
+        def step():
+            api.post_process(ctx, src, dst, W, H, ps, S)
+
+        with ClockSampler(local) as clk:
+            ms = timer.steps(step, args.steps, args.warmup)
+        kernel = "k_blur_h / k_blur_v x 10 + k_post_final (one crg_post_process call)"
+        launches = 11 * args.steps
+        pin_in = api.PinnedArray(ctx, img.shape, np.float32)
+        pin_out = api.PinnedArray(ctx, img.shape, np.float32)
+        pin_in.array[...] = img
+
+        def e2e_step():
+            ctx.check(ctx.lib.crg_memcpy_h2d(ctx.h, src.ptr, pin_in.ptr, img.nbytes, S))
+            api.post_process(ctx, src, dst, W, H, ps, S)
+            ctx.check(ctx.lib.crg_memcpy_d2h(ctx.h, pin_out.ptr, dst.ptr, img.nbytes, S))
+            ctx.check(ctx.lib.crg_stream_sync(ctx.h, S))
+
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        out["e2e"] = {"value": units * world / e2e_s / 1e6, "unit": unit, "h2d_bytes_per_step": int(img.nbytes),
+                      "d2h_bytes_per_step": int(img.nbytes), "ms_per_step": e2e_s * 1e3,
+                      "path": "crg_memcpy_h2d (pinned image) + crg_post_process + crg_memcpy_d2h (pinned)"}
     else:
         v = scenes.soup(1 << 20, 1)
         scene = api.Scene(ctx, v, np.zeros(len(v), np.uint32), scenes.material_table([{}])).build()
