@@ -220,6 +220,13 @@ struct TravStats {
     uint32_t nodes, tris;
 };
 
+// Slack on the best-hit bound when culling boxes: a triangle's computed t can
+// sit below its exact t by more than slab rounding (t = T / det loses digits on
+// large or grazing triangles; 2.8e-6 relative was seen on a floor coplanar with
+// a box face), so a box is kept while its entry lies within best_t * (1 + 2^-12).
+// The CPU oracle uses the same slack, so both find the closest computed t.
+constexpr float kHitSlack = 1.000244140625f;
+
 constexpr int kStack = 64;
 
 // Per-ray traversal state (resumable).
@@ -381,7 +388,7 @@ __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const uint4 *__
             else err = 1u;
         }
         if (COUNT) st.nodes++;
-        visit_node<W>(nodes, child, r, T.oct, T.best_t, T.ng, T.tg);
+        visit_node<W>(nodes, child, r, T.oct, T.best_t * kHitSlack, T.ng, T.tg);
     }
     return false;
 }

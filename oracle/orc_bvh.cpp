@@ -544,10 +544,14 @@ inline bool accept(float t, uint32_t prim, float tmin, float best_t, uint32_t be
     return t == best_t && best_prim != CRG_INVALID_PRIM && prim < best_prim;
 }
 
+/* Slack on the best-hit bound: a triangle's computed t can sit below its exact
+ * t by more than slab rounding (t = T / det on large or grazing triangles), so
+ * a box is kept while its entry lies within best_t * (1 + 2^-12); the GPU
+ * traversal uses the same slack, so both find the closest computed t. */
+constexpr float kHitSlack = 1.000244140625f;
+
 bool slab(const RayPre &r, const Box &b, float tmax, float *tnear = nullptr) {
-    /* the far bound keeps the tolerance after clamping to the best hit so far,
-     * so a box holding an exact t-tie is never culled by slab rounding */
-    float t0 = r.tmin, t1 = tmax * 1.00000036f;
+    float t0 = r.tmin, t1 = tmax * kHitSlack;
     for (int a = 0; a < 3; ++a) {
         float tn = (b.lo[a] - r.o[a]) * r.invd[a];
         float tf = (b.hi[a] - r.o[a]) * r.invd[a];
@@ -585,7 +589,7 @@ void trace(const orc_bvh &B, const crg_ray &ray, crg_hit &hit, bool &occl) {
     while (sp > 0) {
         --sp;
         const uint32_t x = stack[sp];
-        if (stack_t[sp] > best_t * 1.00000036f) continue;
+        if (stack_t[sp] > best_t * kHitSlack) continue;
         if (x & LEAF) {
             const uint32_t prim = B.order[x & ~LEAF];
             const float *v = &B.verts[(size_t)prim * 9];

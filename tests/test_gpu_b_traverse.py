@@ -136,3 +136,23 @@ def test_full_size_soup(ctx, orc):
     b = orc.Bvh(v)
     assert _same_hits(g[idx], b.closest(np.ascontiguousarray(rays[idx])))
     assert np.array_equal(ga[idx], b.any(np.ascontiguousarray(srays[idx])))
+
+
+@pytest.mark.parametrize("width,treelet", [(8, 0), (8, 1), (4, 1), (2, 0)])
+def test_coplanar_faces_match_brute_force(ctx, orc, width, treelet):
+    """Rays from inside the box scene's inner boxes toward the floor their bottom
+    faces lie on: the closest computed t among coplanar triangles, as the brute
+    force finds it, whatever the BVH."""
+    sc = scenes.box_scene()
+    r = np.random.default_rng(13)
+    n = 20000
+    rays = np.zeros(n, _abi.RAY_DTYPE)
+    centre = np.where(r.uniform(size=n)[:, None] < 0.5, [0.68, 0.0, 0.33], [0.32, 0.0, 0.67])
+    o = centre + np.stack([r.uniform(-0.1, 0.1, n), r.uniform(0.001, 0.2, n), r.uniform(-0.1, 0.1, n)], 1)
+    d = np.stack([r.uniform(-1, 1, n), r.uniform(-1, -0.05, n), r.uniform(-1, 1, n)], 1)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays["org"], rays["dir"], rays["tmin"], rays["tmax"] = o, d, 1e-5, np.inf
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(width, treelet)
+    g = s.intersect(rays)
+    s.close()
+    assert _same_hits(g, orc.closest_brute(sc["verts"], rays))

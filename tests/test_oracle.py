@@ -185,3 +185,28 @@ def test_faithful_vs_extended_expectation(orc):
     z = (m0 - m1) / np.sqrt(v0 + v1)
     assert np.mean(np.abs(z) > 3) <= 0.03
     assert abs(m0.mean() - m1.mean()) < 4 * np.sqrt(v0.sum() + v1.sum()) / m0.size
+
+
+def test_coplanar_faces_closest_matches_brute_force(orc):
+    """The box scene's inner boxes stand on the floor: their bottom faces are
+    coplanar with it, and a ray from inside a box meets both at nearly the same
+    t.  The BVH traversal must keep every box whose entry lies within the hit
+    slack of the best t, so it returns the brute-force closest computed t
+    (a floor triangle once lost to a box face here by 2.8e-6 relative)."""
+    from crender_gb300 import _abi
+
+    sc = scenes.box_scene()
+    r = np.random.default_rng(12)
+    n = 4000
+    rays = np.zeros(n, _abi.RAY_DTYPE)
+    centre = np.where(r.uniform(size=n)[:, None] < 0.5, [0.68, 0.0, 0.33], [0.32, 0.0, 0.67])
+    o = centre + np.stack([r.uniform(-0.1, 0.1, n), r.uniform(0.001, 0.2, n), r.uniform(-0.1, 0.1, n)], 1)
+    d = np.stack([r.uniform(-1, 1, n), r.uniform(-1, -0.05, n), r.uniform(-1, 1, n)], 1)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays["org"], rays["dir"], rays["tmin"], rays["tmax"] = o, d, 1e-5, np.inf
+    rays[0]["org"] = (0.354058266, 0.00953761488, 0.564555764)
+    rays[0]["dir"] = (-0.718778908, -0.331720859, 0.610997558)
+    got = orc.Bvh(sc["verts"], 8, 0, 3).closest(rays)
+    want = orc.closest_brute(sc["verts"], rays)
+    assert got[0]["prim"] == want[0]["prim"] == 0
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
