@@ -160,6 +160,11 @@ def cpu_render(scene, camera, st, rows, skybox=None):
     return (rows[1] - rows[0]) * st.width * st.spp, f["render_seconds"]
 
 
+def cpu_cores(workload):
+    """Host threads the CPU leg uses: the post-processing oracle is single-threaded."""
+    return 1 if workload == "post" else (os.cpu_count() or 1)
+
+
 def cpu_leg(workload):
     """Bounded CPU sample of the workload on all host cores (the oracle)."""
     from crender_gb300 import api, scenes
@@ -212,7 +217,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    cores = os.cpu_count() or 1
+    cores = cpu_cores(args.workload)
     vals, sample = [], ""
     for i in range(args.warmup + args.steps):
         v, sample = cpu_leg(args.workload)
@@ -728,7 +733,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
-        cpu = {"value": cv, "unit": unit, "cores": os.cpu_count(), "kind": "port", "sample": sample}
+        cpu = {"value": cv, "unit": unit, "cores": cpu_cores(args.workload), "kind": "port", "sample": sample}
     if rank == 0:
         line = {
             "metric": unit, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -259,6 +259,7 @@ ORC_SIGNATURES = [
     ("orc_post_process", C.c_int, [vp, vp, C.c_uint32, C.c_uint32, P(PostSettings)]),
     ("orc_scene_intersect", C.c_int, [P(OrcSceneDesc), vp, vp, vp, C.c_uint64]),
     ("orc_draft_render", C.c_int, [P(OrcSceneDesc), P(Camera), C.c_uint32, C.c_uint32, C.c_float, vp]),
+    ("orc_alias_table", None, [vp, C.c_uint32, vp, vp]),
     ("orc_camera_ray", None, [P(Camera), P(Settings), C.c_uint32, C.c_uint32, C.c_float, C.c_float, vp, vp]),
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),

@@ -14,10 +14,18 @@ import numpy as np
 from . import _abi, check, load
 from ._abi import ptr
 
+def _default_sun_direction():
+    """normalize(0.8, -1, 0) in float32 as glm (and the library) compute it: v * (1 / sqrt(dot(v, v)))."""
+    d = np.array([0.8, -1.0, 0.0], np.float32)
+    inv = np.float32(1.0) / np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2], dtype=np.float32)
+    return tuple(float(x) for x in d * inv)
+
+
+# cr::entity::sun (src/render/entities/components.h:23-29), bit-identical to crg_scene_set_sun(.., NULL)
 DEFAULT_SUN = dict(
     size=np.float32(3.14159265359) / np.float32(48.0),
     intensity=100.0,
-    direction=(0.8 / np.sqrt(1.64), -1.0 / np.sqrt(1.64), 0.0),
+    direction=_default_sun_direction(),
     colour=(1.0, 0.9, 0.7),
 )
 

@@ -148,6 +148,38 @@ void compute_areas(crg_scene *s, const float *verts) {
     for (uint32_t p = 0; p < s->ntri; ++p) s->tri_area[p] = tri_area_of(verts + (size_t)p * 9);
 }
 
+// Alias table (Walker 1977, built with Vose's 1991 two-worklist method in
+// double, worklists scanned in index order so the table is reproducible) of
+// the weights w: entry j = {prob_j, alias_j}; picking j = floor(u1 * n) and
+// keeping it when u2 < prob_j, else taking alias_j, selects entry k with
+// probability w_k / total in two loads instead of a binary search.
+std::vector<float> alias_table(const std::vector<double> &w, double total) {
+    const size_t n = w.size();
+    std::vector<double> q(n);
+    std::vector<uint32_t> small, large, alias(n);
+    std::vector<double> prob(n, 1.0);
+    for (size_t i = 0; i < n; ++i) {
+        q[i] = (w[i] * (double)n) / total;
+        alias[i] = (uint32_t)i;
+        (q[i] < 1.0 ? small : large).push_back((uint32_t)i);
+    }
+    while (!small.empty() && !large.empty()) {
+        const uint32_t l = small.back(), g = large.back();
+        small.pop_back();
+        large.pop_back();
+        prob[l] = q[l];
+        alias[l] = g;
+        q[g] = (q[g] + q[l]) - 1.0;
+        (q[g] < 1.0 ? small : large).push_back(g);
+    }
+    std::vector<float> out(2 * n);
+    for (size_t i = 0; i < n; ++i) {
+        out[2 * i] = (float)prob[i];
+        std::memcpy(&out[2 * i + 1], &alias[i], 4);
+    }
+    return out;
+}
+
 // Emissive triangles weighted by area x luminance of colour*emission (double
 // sums in primitive order; CDF and pdfs rounded to float once).
 crg_status prepare_lights(crg_scene *s) {
@@ -181,22 +213,17 @@ crg_status prepare_lights(crg_scene *s) {
     std::vector<float> mpdf(nmat, 0.0f);
     s->nlights = 0;
     if (total > 0.0) {
-        std::vector<float> cdf, pdf;
-        double cum = 0.0;
-        for (size_t j = 0; j < w.size(); ++j) {
-            cum += w[j];
-            cdf.push_back((float)(cum / total));
-            pdf.push_back((float)(lum[mat_idx[prim[j]]] / total));
-        }
-        cdf.back() = 1.0f;
+        std::vector<float> pdf;
+        for (size_t j = 0; j < w.size(); ++j) pdf.push_back((float)(lum[mat_idx[prim[j]]] / total));
+        const std::vector<float> alias = alias_table(w, total);
         for (uint32_t m = 0; m < nmat; ++m) mpdf[m] = (float)(lum[m] / total);
         s->nlights = (uint32_t)prim.size();
         crg_status rc;
         if ((rc = dev_alloc(s->ctx, s->light_prim, 4 * prim.size())) != CRG_OK) return rc;
-        if ((rc = dev_alloc(s->ctx, s->light_cdf, 4 * cdf.size())) != CRG_OK) return rc;
+        if ((rc = dev_alloc(s->ctx, s->light_alias, 4 * alias.size())) != CRG_OK) return rc;
         if ((rc = dev_alloc(s->ctx, s->light_pdf, 4 * pdf.size())) != CRG_OK) return rc;
         CRG_CUDA(s->ctx, cudaMemcpy(s->light_prim.ptr, prim.data(), 4 * prim.size(), cudaMemcpyHostToDevice));
-        CRG_CUDA(s->ctx, cudaMemcpy(s->light_cdf.ptr, cdf.data(), 4 * cdf.size(), cudaMemcpyHostToDevice));
+        CRG_CUDA(s->ctx, cudaMemcpy(s->light_alias.ptr, alias.data(), 4 * alias.size(), cudaMemcpyHostToDevice));
         CRG_CUDA(s->ctx, cudaMemcpy(s->light_pdf.ptr, pdf.data(), 4 * pdf.size(), cudaMemcpyHostToDevice));
         if (s->ninst) {
             if ((rc = dev_alloc(s->ctx, s->light_inst, 4 * inst.size())) != CRG_OK) return rc;
@@ -305,7 +332,7 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
 
 void scene_free(crg_scene *s) {
     if (!s) return;
-    DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_cdf, &s->light_pdf, &s->mat_light_pdf,
+    DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_alias, &s->light_pdf, &s->mat_light_pdf,
                       &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead,
                       &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst};
     for (DevBuf *b : bufs) dev_free(*b);

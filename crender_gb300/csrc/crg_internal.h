@@ -52,10 +52,10 @@ struct crg_scene {
     std::vector<double> inst_area; // world area of triangle p under instance j at [j * ntri + p]
     DevBuf inst;       // float4[6 * ninst]
     DevBuf light_inst; // uint32 per emitter entry (instanced scenes)
-    // emissive triangles (power-weighted CDF)
+    // emissive triangles (power-weighted alias table)
     uint32_t nlights = 0;
     std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table
-    DevBuf light_prim, light_cdf, light_pdf, mat_light_pdf;
+    DevBuf light_prim, light_alias, light_pdf, mat_light_pdf; // light_alias: float2 {prob, alias bits}
     // environment / sun
     DevBuf sky;
     uint32_t sky_w = 0, sky_h = 0;

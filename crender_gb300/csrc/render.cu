@@ -53,7 +53,7 @@ using namespace rc;
 namespace {
 
 template <int W, int MODE, bool CNT>
-__global__ void __launch_bounds__(128) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
+__global__ void __launch_bounds__(128, 4) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
     PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
@@ -159,7 +159,7 @@ SceneDev scene_dev(const crg_scene *s) {
     S.mat_idx = (const uint32_t *)s->mat_idx.ptr;
     S.mats = (const crg_material *)s->mats.ptr;
     S.light_prim = (const uint32_t *)s->light_prim.ptr;
-    S.light_cdf = (const float *)s->light_cdf.ptr;
+    S.light_alias = (const float2 *)s->light_alias.ptr;
     S.light_pdf = (const float *)s->light_pdf.ptr;
     S.mat_light_pdf = (const float *)s->mat_light_pdf.ptr;
     S.verts = (const float *)s->verts.ptr;

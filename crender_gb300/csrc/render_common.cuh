@@ -22,7 +22,7 @@ struct SceneDev {
     const uint32_t *mat_idx;
     const crg_material *mats;
     const uint32_t *light_prim;
-    const float *light_cdf;
+    const float2 *light_alias; // per emitter entry {prob, alias bits}
     const float *light_pdf;
     const float *mat_light_pdf;
     const float4 *sky;
@@ -514,14 +514,13 @@ __device__ __forceinline__ float fresnel_dielectric(float ci, float eta, float &
 __device__ __forceinline__ v3 to_local(const onb &F, v3 w) { return mk(dot(w, F.t), dot(w, F.b), dot(w, F.n)); }
 __device__ __forceinline__ v3 from_local(const onb &F, v3 l) { return add(add(mul(F.t, l.x), mul(F.b, l.y)), mul(F.n, l.z)); }
 
-__device__ __forceinline__ uint32_t pick_light(const SceneDev &S, float u) {
-    uint32_t lo = 0, hi = S.nlights - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (u < __ldg(&S.light_cdf[mid])) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo;
+// Emitter entry with probability proportional to power: the alias table's
+// column floor(u1 * n), kept when u2 < its probability, else its alias.
+__device__ __forceinline__ uint32_t pick_light(const SceneDev &S, float u1, float u2) {
+    uint32_t j = (uint32_t)(u1 * (float)S.nlights);
+    if (j >= S.nlights) j = S.nlights - 1;
+    const float2 e = __ldg(&S.light_alias[j]);
+    return u2 < e.x ? j : __float_as_uint(e.y);
 }
 
 // Emissive-triangle NEE at p: fills nr (kind 1) with the shadow ray and the
@@ -530,7 +529,7 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
                             const onb &F, v3 wol, float alpha, NeeReq &nr, uint32_t mat = 0, float refl = 1.0f) {
     nr.kind = 0;
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
-    const uint32_t j = pick_light(S, g.x);
+    const uint32_t j = pick_light(S, g.x, g.w);
     const uint32_t prim = __ldg(&S.light_prim[j]);
     v3 a, b, c;
     prim_verts(S, prim, a, b, c);

@@ -219,7 +219,7 @@ __device__ __forceinline__ void warp_count(bool want, unsigned int *count) {
 // Contributions reach L in the same order in every form: emission of bounce
 // i, its NEE, then bounce i + 1.
 template <int W, int FUSE, bool CNT>
-__global__ void __launch_bounds__(256) k_wf_shade(Wf w) {
+__global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
     unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
 
 // Extend with per-lane ray refill (dyn_traverse): the same hits as k_wf_extend.
 template <int W, bool CNT>
-__global__ void __launch_bounds__(256) k_wf_extend_dyn(Wf w) {
+__global__ void __launch_bounds__(256, 4) k_wf_extend_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
     const uint32_t *in = q_in(w, *c);
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) k_wf_extend_dyn(Wf w) {
 // are all emitter tests (any hit below tmax); sun requests (faithful
 // estimator with the sun on) go through k_wf_shadow.
 template <int W, bool CNT>
-__global__ void __launch_bounds__(256) k_wf_shadow_dyn(Wf w) {
+__global__ void __launch_bounds__(256, 4) k_wf_shadow_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->sh_count;
     TravStats st{0, 0};
@@ -567,17 +567,47 @@ struct Workspace {
 
 size_t align_up(size_t x) { return (x + 255) / 256 * 256; }
 
+// Persistent grids: each per-bounce kernel fills every SM with as many of its
+// own blocks as fit (the traversal kernels need fewer registers than shading,
+// so they get more warps to hide memory latency); work is fetched atomically,
+// so any grid size is correct.
+struct Grids {
+    uint32_t ext, shade, shadow;
+};
+
+template <class K>
+uint32_t resident_grid(K kernel, uint32_t block, int sms) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)block, 0) != cudaSuccess) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+    }
+    return (uint32_t)(std::max(sms, 1) * std::max(per_sm, 1));
+}
+
+template <int W, int FUSE, bool CNT>
+Grids bounce_grids(const Wf &wf, uint32_t block, int sms) {
+    Grids g{0, 0, 0};
+    if (FUSE <= 1)
+        g.ext = wf.refill ? resident_grid(k_wf_extend_dyn<W, CNT>, block, sms) : resident_grid(k_wf_extend<W, CNT>, block, sms);
+    g.shade = resident_grid(k_wf_shade<W, FUSE, CNT>, block, sms);
+    if (FUSE == 0)
+        g.shadow = wf.refill_sh ? resident_grid(k_wf_shadow_dyn<W, CNT>, block, sms)
+                                : resident_grid(k_wf_shadow<W, CNT>, block, sms);
+    return g;
+}
+
 // The per-bounce kernels of one loop iteration for a fusion level.
 template <int W, int FUSE, bool CNT>
-void launch_bounce(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
+void launch_bounce(const Wf &wf, const Grids &g, uint32_t block, cudaStream_t st) {
     if (FUSE <= 1) {
-        if (wf.refill) k_wf_extend_dyn<W, CNT><<<grid, block, 0, st>>>(wf);
-        else k_wf_extend<W, CNT><<<grid, block, 0, st>>>(wf);
+        if (wf.refill) k_wf_extend_dyn<W, CNT><<<g.ext, block, 0, st>>>(wf);
+        else k_wf_extend<W, CNT><<<g.ext, block, 0, st>>>(wf);
     }
-    k_wf_shade<W, FUSE, CNT><<<grid, block, 0, st>>>(wf);
+    k_wf_shade<W, FUSE, CNT><<<g.shade, block, 0, st>>>(wf);
     if (FUSE == 0) {
-        if (wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<grid, block, 0, st>>>(wf);
-        else k_wf_shadow<W, CNT><<<grid, block, 0, st>>>(wf);
+        if (wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<g.shadow, block, 0, st>>>(wf);
+        else k_wf_shadow<W, CNT><<<g.shadow, block, 0, st>>>(wf);
     }
 }
 
@@ -585,12 +615,13 @@ void launch_bounce(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st)
 // done flag every 8 iterations (for profilers that cannot see into graphs
 // with conditional nodes, and for runtimes without them).
 template <int W, int FUSE, bool CNT>
-crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st) {
+crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &bg, uint32_t block, uint32_t max_iters,
+                    cudaStream_t st) {
     unsigned int *done_h = nullptr;
     CRG_CUDA(ctx, cudaHostAlloc(&done_h, sizeof(unsigned int), cudaHostAllocDefault));
     crg_status rc = CRG_OK;
     for (uint32_t it = 0; it < max_iters + 8; ++it) {
-        launch_bounce<W, FUSE, CNT>(wf, grid, block, st);
+        launch_bounce<W, FUSE, CNT>(wf, bg, block, st);
         k_wf_control<<<1, 32, 0, st>>>(wf, 0, 0);
         k_wf_resolve<<<grid, 256, 0, st>>>(wf);
         k_wf_generate<<<grid, 256, 0, st>>>(wf, 0);
@@ -617,7 +648,8 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
     k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
     k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
     CRG_CUDA(ctx, cudaGetLastError());
-    if (host_loop) return run_host<W, FUSE, CNT>(ctx, wf, grid, block, max_iters, st);
+    const Grids bg = bounce_grids<W, FUSE, CNT>(wf, block, ctx->sm_count);
+    if (host_loop) return run_host<W, FUSE, CNT>(ctx, wf, grid, bg, block, max_iters, st);
     // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -650,7 +682,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
             rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
             break;
         }
-        launch_bounce<W, FUSE, CNT>(wf, grid, block, cap);
+        launch_bounce<W, FUSE, CNT>(wf, bg, block, cap);
         k_wf_control<<<1, 32, 0, cap>>>(wf, handle, 1);
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);

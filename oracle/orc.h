@@ -115,6 +115,9 @@ int orc_scene_intersect(const orc_scene_desc *scene, const crg_ray *rays, crg_hi
 int orc_draft_render(const orc_scene_desc *scene, const crg_camera *cam, uint32_t w, uint32_t h, float aspect,
                      float *rgba);
 
+/* The emitter alias table of weights w[n] (for unit tests). */
+void orc_alias_table(const double *w, uint32_t n, float *prob, uint32_t *alias);
+
 /* Camera ray of pixel (px, py) with jitter (jx, jy) (for unit tests). */
 void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px, uint32_t py, float jx,
                     float jy, float *org, float *dir);

@@ -116,7 +116,8 @@ struct Scene {
     float sun_cos = 1, sun_pdf = 0;
     /* emissive triangles (extended mode) */
     std::vector<uint32_t> light_prim;
-    std::vector<float> light_cdf, light_pdf;
+    std::vector<float> light_prob, light_pdf; /* alias table: probability and alias per entry */
+    std::vector<uint32_t> light_alias;
     std::vector<float> mat_light_pdf;
     /* texture coordinates and textures */
     const float *uvs = nullptr;
@@ -537,14 +538,13 @@ float fresnel_dielectric(float ci, float eta, float *st2_out) {
 v3 to_local(const onb &F, v3 w) { return mk(dot(w, F.t), dot(w, F.b), dot(w, F.n)); }
 v3 from_local(const onb &F, v3 l) { return add(add(mul(F.t, l.x), mul(F.b, l.y)), mul(F.n, l.z)); }
 
-uint32_t pick_light(const Scene &S, float u) {
-    uint32_t lo = 0, hi = (uint32_t)S.light_cdf.size() - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (u < S.light_cdf[mid]) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo;
+/* Walker's alias method: column floor(u1 * n), kept when u2 < its
+ * probability, else its alias. */
+uint32_t pick_light(const Scene &S, float u1, float u2) {
+    const uint32_t n = (uint32_t)S.light_prim.size();
+    uint32_t j = (uint32_t)(u1 * (float)n);
+    if (j >= n) j = n - 1;
+    return u2 < S.light_prob[j] ? j : S.light_alias[j];
 }
 
 /* Emissive-triangle NEE; bsdf 0 = Lambert (albedo), 1 = GGX (F0, alpha, frame, wol). */
@@ -552,7 +552,7 @@ v3 nee(Ctx &C, uint32_t i, v3 p, v3 n, v3 T, int bsdf, v3 albedo, const onb &F, 
        Tape *tape = nullptr, uint32_t bsdf_mat = 0, float refl = 1.0f) {
     const Scene &S = *C.S;
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.set->seed);
-    const uint32_t j = pick_light(S, g.x);
+    const uint32_t j = pick_light(S, g.x, g.w);
     const uint32_t prim = S.light_prim[j];
     v3 a, b, c;
     tri_verts(S, prim, a, b, c);
@@ -745,6 +745,32 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
     return L;
 }
 
+/* Alias table of the weights w (Walker 1977; Vose 1991's two worklists in
+ * double, scanned in index order so the table is reproducible). */
+void build_alias(const std::vector<double> &w, double total, std::vector<float> &prob_out,
+                 std::vector<uint32_t> &alias) {
+    const size_t n = w.size();
+    std::vector<double> q(n), prob(n, 1.0);
+    std::vector<uint32_t> small, large;
+    alias.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        q[i] = (w[i] * (double)n) / total;
+        alias[i] = (uint32_t)i;
+        (q[i] < 1.0 ? small : large).push_back((uint32_t)i);
+    }
+    while (!small.empty() && !large.empty()) {
+        const uint32_t l = small.back(), g = large.back();
+        small.pop_back();
+        large.pop_back();
+        prob[l] = q[l];
+        alias[l] = g;
+        q[g] = (q[g] + q[l]) - 1.0;
+        (q[g] < 1.0 ? small : large).push_back(g);
+    }
+    prob_out.assign(n, 0.0f);
+    for (size_t i = 0; i < n; ++i) prob_out[i] = (float)prob[i];
+}
+
 /* Inverse of an affine 4x4 (column-major) in double, rounded once to rows
  * [A^-1 | -A^-1 t], followed by the forward rows [A | t] as given. */
 void inverse_rows(const float *x, float rows[24]) {
@@ -854,13 +880,8 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
         S.light_prim.clear();
         return;
     }
-    double cum = 0.0;
-    for (size_t j = 0; j < w.size(); ++j) {
-        cum += w[j];
-        S.light_cdf.push_back((float)(cum / total));
-        S.light_pdf.push_back((float)(lum[D.mat_idx[S.light_prim[j]]] / total));
-    }
-    S.light_cdf.back() = 1.0f;
+    for (size_t j = 0; j < w.size(); ++j) S.light_pdf.push_back((float)(lum[D.mat_idx[S.light_prim[j]]] / total));
+    build_alias(w, total, S.light_prob, S.light_alias);
     for (uint32_t m = 0; m < D.nmat; ++m) S.mat_light_pdf[m] = (float)(lum[m] / total);
 }
 
@@ -1078,6 +1099,19 @@ int orc_draft_render(const orc_scene_desc *desc, const crg_camera *cam, uint32_t
         }
     orc_bvh_free(bvh);
     return CRG_OK;
+}
+
+void orc_alias_table(const double *w, uint32_t n, float *prob, uint32_t *alias) {
+    std::vector<double> ww(w, w + n);
+    double total = 0.0;
+    for (uint32_t i = 0; i < n; ++i) total += w[i];
+    std::vector<float> p;
+    std::vector<uint32_t> a;
+    build_alias(ww, total, p, a);
+    for (uint32_t i = 0; i < n; ++i) {
+        prob[i] = p[i];
+        alias[i] = a[i];
+    }
 }
 
 int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,

@@ -30,7 +30,7 @@ def test_obj_model_renders_like_host_expansion(ctx, tmp_path):
     verts = pos[vi].reshape(-1, 9)
     mats = scenes.material_table([{"colour": tuple(c)} for c in col])
     s = api.Scene(ctx, verts, mi, mats).build(8, 1)
-    s.set_sun(True)
+    ctx.check(ctx.lib.crg_scene_set_sun(s.h, 1, None))  # the library's default sun, as the adapter uses it
     cam = dict(position=(0.0, 0.5, -3.0), rotation=(0.0, 0.0, 0.0), fov=60.0, mode=0, scale=1.0)
     f = api.Film(ctx, W, H)
     api.render(s, cam, api.make_settings(W, H, spp, 6, 0, 0, 1, W / H), f)

@@ -210,3 +210,20 @@ def test_coplanar_faces_closest_matches_brute_force(orc):
     want = orc.closest_brute(sc["verts"], rays)
     assert got[0]["prim"] == want[0]["prim"] == 0
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_alias_table_selects_in_proportion_to_power(orc):
+    """The emitter alias table (Walker's method, Vose's construction): column j
+    kept with probability prob_j, else its alias; every entry's total selection
+    probability equals its weight's share."""
+    from crender_gb300 import _abi
+
+    for n, seed in ((1, 0), (2, 1), (1280, 2), (5000, 3)):
+        w = np.random.default_rng(seed).gamma(0.5, 1.0, n) + 1e-9
+        prob = np.zeros(n, np.float32)
+        alias = np.zeros(n, np.uint32)
+        orc.lib().orc_alias_table(_abi.ptr(w), n, _abi.ptr(prob), _abi.ptr(alias))
+        p = prob.astype(np.float64) / n
+        np.add.at(p, alias, (1.0 - prob.astype(np.float64)) / n)
+        assert np.allclose(p, w / w.sum(), rtol=1e-5, atol=1e-12)
+        assert np.all((prob >= 0) & (prob <= 1)) and np.all(alias < n)
