@@ -128,6 +128,28 @@ def post_image(w, h):
     return img
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) from ncu captures on a GB300:
+#   one wavefront frame, per sample: box scene 512x512x64 1,720 B; displaced scene
+#   1920x1080x16 (path pool 4,194,304) 1,097 B;
+#   k_intersect on the soup, per launch of 16,777,216 closest-hit rays: 923.3 MB.
+TRAFFIC_PER_SAMPLE = {"box": 1720.0, "displaced": 1097.0}
+TRAFFIC_SOUP_LAUNCH = 923.3e6
+
+
+def traffic_estimate(workload, out, units):
+    """DRAM traffic per step from the ncu captures above, or None; the batch is
+    scaled per scene by its samples (the per-sample traffic of a frame grows in
+    proportion to its samples once the path pool exceeds L2)."""
+    if workload == "soup":
+        return TRAFFIC_SOUP_LAUNCH, "ncu capture of the same launch"
+    if workload == "batch" and "scene_samples" in out:
+        t = sum(TRAFFIC_PER_SAMPLE[k] * v for k, v in out["scene_samples"].items())
+        return t, "per-sample traffic of one wavefront frame of each scene (ncu), scaled by the batch's samples per scene"
+    if workload in ("box", "displaced") and out.get("form") == "wavefront":
+        return TRAFFIC_PER_SAMPLE[workload] * units, "per-sample traffic of one wavefront frame (ncu), times the samples"
+    return None, None
+
+
 def workload_config(w):
     if w == "post":
         return {"workload": "post-processing of a 3840x2160 RGBA32F image: bloom threshold + 10 separable 15-tap "
@@ -477,6 +499,8 @@ def main():
                                              v["width"] / v["height"])) for i, (si, cam, v) in enumerate(vdefs)]
         films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
         units = sum(st.width * st.height * st.spp for _, _, st in views)
+        out["scene_samples"] = {name: sum(st.width * st.height * st.spp for si, _, st in views if si == k)
+                                for k, name in enumerate(("box", "displaced"))}
 
         # autotuner (untimed): BVH width, stage fusion, refill, fetch, block size, path pool
         t0 = time.perf_counter()
@@ -730,6 +754,7 @@ def main():
         # test in shade, 1 fused) + control, resolve, generate, generated
         fuse = out.get("autotune", {}).get("opts", {}).get("fuse", 1) or 1
         launches = args.steps * (3 + (4 + (3, 2, 1)[fuse - 1]) * int(out["work"]["iterations"]))
+    traffic, traffic_src = traffic_estimate(args.workload, out, units)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
@@ -740,7 +765,7 @@ def main():
             "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args.workload),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": kernel, "peak_kind": peak_kind,
+                         "traffic": traffic, "traffic_source": traffic_src, "kernel": kernel, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": int(algo)},
             "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches, **out,
         }
