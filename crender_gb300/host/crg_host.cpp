@@ -162,6 +162,13 @@ void scene::add_model(const model_data &m) {
     dirty_ = true;
 }
 
+void scene::set_instances(const std::vector<std::array<float, 16>> &transforms) {
+    std::lock_guard<std::mutex> g(mutex_);
+    instances_ = transforms;
+    if (scene_) check(crg_scene_set_instances(scene_, instances_.empty() ? nullptr : instances_[0].data(),
+                                              (uint32_t)instances_.size()));
+}
+
 void scene::set_skybox(image &&sky) {
     std::lock_guard<std::mutex> g(mutex_);
     skybox_ = std::move(sky);
@@ -222,6 +229,8 @@ void scene::commit() {
         s = crg_scene_set_textures(fresh, (uint32_t)px.size(), px.data(), w.data(), h.data());
     }
     if (s == CRG_OK) s = crg_scene_build(fresh, &opts_, nullptr);
+    if (s == CRG_OK && !instances_.empty())
+        s = crg_scene_set_instances(fresh, instances_[0].data(), (uint32_t)instances_.size());
     if (s == CRG_OK && skybox_)
         s = crg_scene_set_skybox(fresh, skybox_->data(), (uint32_t)skybox_->width(), (uint32_t)skybox_->height(),
                                  sky_rot_.x, sky_rot_.y);
@@ -512,6 +521,91 @@ std::vector<float> renderer::current_sums() {
     std::vector<float> out(res_x_ * res_y_ * 3);
     check(crg_film_download(film_, out.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr));
     return out;
+}
+
+// ------------------------------------------------------------------ post_processor
+post_processor::post_processor(scene *owner, bool faithful) : scene_(owner), faithful_(faithful) {
+    if (!owner) throw error(CRG_ERR_INVALID_ARG, "post_processor: null scene");
+}
+
+post_processor::~post_processor() {
+    if (d_src_) crg_device_free(scene_->context(), d_src_);
+    if (d_dst_) crg_device_free(scene_->context(), d_dst_);
+}
+
+image post_processor::process(const image &img) {
+    if (!img.valid()) throw error(CRG_ERR_INVALID_ARG, "post_processor: empty image");
+    crg_context *ctx = scene_->context();
+    const size_t bytes = img.width() * img.height() * 16;
+    if (bytes > bytes_) {
+        if (d_src_) crg_device_free(ctx, d_src_);
+        if (d_dst_) crg_device_free(ctx, d_dst_);
+        d_src_ = d_dst_ = nullptr;
+        bytes_ = 0;
+        void *a = nullptr, *b = nullptr;
+        crg_status s = crg_device_alloc(ctx, bytes, &a);
+        if (s == CRG_OK) s = crg_device_alloc(ctx, bytes, &b);
+        if (s != CRG_OK) {
+            if (a) crg_device_free(ctx, a);
+            raise(ctx, s, "post_processor");
+        }
+        d_src_ = (float *)a;
+        d_dst_ = (float *)b;
+        bytes_ = bytes;
+    }
+    crg_post_settings ps;
+    crg_post_settings_default(&ps);
+    ps.bloom = bloom_.enabled;
+    ps.bloom_threshold = bloom_.threshold;
+    ps.bloom_strength = bloom_.strength;
+    ps.gray_scale = gray_.enabled;
+    ps.tonemapping = tone_.enabled;
+    ps.tonemap_type = tone_.type;
+    ps.exposure = tone_.exposure;
+    ps.gamma = tone_.gamma_correction;
+    ps.mode = faithful_ ? CRG_POST_FAITHFUL : CRG_POST_FULL;
+    image out(img.width(), img.height());
+    crg_status s = crg_memcpy_h2d(ctx, d_src_, img.data(), bytes, nullptr);
+    if (s == CRG_OK) s = crg_post_process(ctx, d_src_, d_dst_, (uint32_t)img.width(), (uint32_t)img.height(), &ps, nullptr);
+    if (s == CRG_OK) s = crg_memcpy_d2h(ctx, out.data(), d_dst_, bytes, nullptr);
+    if (s == CRG_OK) s = crg_stream_sync(ctx, nullptr);
+    if (s != CRG_OK) raise(ctx, s, "post_processor::process");
+    return out;
+}
+
+// ------------------------------------------------------------------ draft_renderer
+draft_renderer::draft_renderer(scene *s, uint64_t res_x, uint64_t res_y) : scene_(s), res_x_(0), res_y_(0) {
+    if (!s) throw error(CRG_ERR_INVALID_ARG, "draft_renderer: null scene");
+    set_resolution(res_x, res_y);
+}
+
+draft_renderer::~draft_renderer() {
+    if (d_rgba_) crg_device_free(scene_->context(), d_rgba_);
+}
+
+void draft_renderer::set_resolution(uint64_t res_x, uint64_t res_y) {
+    if (res_x == 0 || res_y == 0) throw error(CRG_ERR_INVALID_ARG, "draft_renderer: empty resolution");
+    if (d_rgba_) crg_device_free(scene_->context(), d_rgba_);
+    d_rgba_ = nullptr;
+    void *p = nullptr;
+    const crg_status s = crg_device_alloc(scene_->context(), res_x * res_y * 16, &p);
+    if (s != CRG_OK) raise(scene_->context(), s, "draft_renderer");
+    d_rgba_ = (float *)p;
+    res_x_ = res_x;
+    res_y_ = res_y;
+    out_ = image(res_x, res_y);
+}
+
+image *draft_renderer::render() {
+    crg_scene *sc = scene_->handle();
+    const crg_camera cam = scene_->camera()->to_crg();
+    crg_context *ctx = scene_->context();
+    crg_status s = crg_draft_render(sc, &cam, (uint32_t)res_x_, (uint32_t)res_y_, (float)res_x_ / (float)res_y_,
+                                    d_rgba_, nullptr);
+    if (s == CRG_OK) s = crg_memcpy_d2h(ctx, out_.data(), d_rgba_, res_x_ * res_y_ * 16, nullptr);
+    if (s == CRG_OK) s = crg_stream_sync(ctx, nullptr);
+    if (s != CRG_OK) raise(ctx, s, "draft_renderer::render");
+    return &out_;
 }
 
 } // namespace crg::host

@@ -19,6 +19,7 @@
 // use it; link libcrg_host.so and libcrg.so.
 #pragma once
 
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <limits>
@@ -177,6 +178,10 @@ public:
     bool is_sun_enabled() const noexcept { return sun_enabled_; }
     // BVH options used by the next commit (default: width 8, treelets on).
     void set_build_options(const crg_build_opts &opts);
+    // Instance transforms (cr::entity::instances::transforms, model.cpp:99-126),
+    // 16 floats each, column-major as glm::mat4; applied to every model of
+    // this scene (crg_scene_set_instances).  Empty = the models as added.
+    void set_instances(const std::vector<std::array<float, 16>> &transforms);
 
     // ABI handles (the scene is committed first).
     crg_context *context() noexcept { return ctx_; }
@@ -200,6 +205,7 @@ private:
     std::vector<uint32_t> mat_idx_;
     std::vector<material_information> materials_;
     std::optional<image> skybox_;
+    std::vector<std::array<float, 16>> instances_;
     vec2 sky_rot_;
     bool sun_enabled_ = true;
     crg_sun sun_{};
@@ -283,6 +289,65 @@ private:
     bool run_ = true, paused_ = false, idle_ = false;
     std::string thread_error_;
     std::thread thread_;
+};
+
+// cr::post_processor (src/render/post/post_processor.h:10-62) over
+// crg_post_process: the same settings structs and process(image) -> image,
+// with the GL compute passes run as CUDA kernels on the scene's device.
+class post_processor {
+public:
+    struct bloom_settings {
+        bool enabled = false;
+        float threshold = 0.7f;
+        float strength = 1.0f;
+    };
+    struct gray_scale_settings {
+        bool enabled = false;
+    };
+    struct tonemapping_settings {
+        bool enabled = false;
+        int type = 0;
+        float exposure = 1.f;
+        float gamma_correction = 2.2f;
+    };
+    // Runs on the context of `owner` (its device); `faithful` reproduces the
+    // reference's 8x8-dispatch coverage and brightness indexing (crg.h).
+    explicit post_processor(scene *owner, bool faithful = true);
+    ~post_processor();
+    post_processor(const post_processor &) = delete;
+    post_processor &operator=(const post_processor &) = delete;
+    image process(const image &img);
+    void submit_bloom_settings(const bloom_settings &s) { bloom_ = s; }
+    void submit_gray_scale_settings(const gray_scale_settings &s) { gray_ = s; }
+    void submit_tonemapping_settings(const tonemapping_settings &s) { tone_ = s; }
+
+private:
+    scene *scene_;
+    bool faithful_;
+    bloom_settings bloom_;
+    gray_scale_settings gray_;
+    tonemapping_settings tone_;
+    float *d_src_ = nullptr, *d_dst_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// cr::draft_renderer (src/render/draft/draft_renderer.h) over crg_draft_render:
+// the unlit preview of the scene from its camera, as an RGBA image in the
+// film's pixel layout.
+class draft_renderer {
+public:
+    draft_renderer(scene *s, uint64_t res_x, uint64_t res_y);
+    ~draft_renderer();
+    draft_renderer(const draft_renderer &) = delete;
+    draft_renderer &operator=(const draft_renderer &) = delete;
+    void set_resolution(uint64_t res_x, uint64_t res_y);
+    image *render();
+
+private:
+    scene *scene_;
+    uint64_t res_x_, res_y_;
+    float *d_rgba_ = nullptr;
+    image out_;
 };
 
 } // namespace crg::host

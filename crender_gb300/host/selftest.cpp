@@ -9,6 +9,7 @@
 //      (triangles [0, nsplit) and [nsplit, ntri) go in as two models, indexed)
 // out: u64 spp1; float sums1[W*H*3]; u64 spp2; float sums2[W*H*3];
 //      u64 total_rays; per ray: u32 prim, float distance, float normal[3]
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -110,9 +111,77 @@ int obj_render(const char *file, const char *out, uint32_t W, uint32_t H, uint32
     return 0;
 }
 
+// crg_host_selftest extras <in> <out>: the same input as the main mode; drives
+// draft_renderer, post_processor (bloom + Reinhard on a FULL-coverage
+// processor) on the progress image of a short render, and scene::set_instances.
+// out: float draft[W*H*4]; float progress[W*H*4]; float post[W*H*4];
+//      per ray: u32 prim, float distance (two instances: identity and +0.25 in x)
+int extras(const char *in, const char *out_path) {
+    FILE *f = std::fopen(in, "rb");
+    if (!f) return 2;
+    uint32_t h[10];
+    if (!rd(f, h, 10) || h[0] != 0x54475243u) return 2;
+    const uint32_t ntri = h[1], nmat = h[2], W = h[3], H = h[4], spp = h[5], bounces = h[6], mode = h[7], nrays = h[8];
+    std::vector<float> verts((size_t)ntri * 9);
+    std::vector<uint32_t> mat_idx(ntri);
+    std::vector<crg_material> mats(nmat);
+    crg_camera cam;
+    std::vector<crg_ray> rays(nrays);
+    if (!rd(f, verts.data(), verts.size()) || !rd(f, mat_idx.data(), ntri) || !rd(f, mats.data(), nmat) ||
+        !rd(f, &cam, 1) || !rd(f, rays.data(), nrays))
+        return 2;
+    std::fclose(f);
+    try {
+        scene sc(0);
+        sc.add_model(make_model(verts, mat_idx, mats, 0, ntri));
+        sc.set_sun_enabled(false);
+        camera *c = sc.camera();
+        c->fov = cam.fov;
+        c->rotate(vec3{cam.rotation[0], cam.rotation[1], cam.rotation[2]});
+        c->position = vec3{cam.position[0], cam.position[1], cam.position[2]};
+        draft_renderer dr(&sc, W, H);
+        const image draft = *dr.render();
+        renderer::options o;
+        o.mode = mode;
+        o.target_spp = spp;
+        renderer r(W, H, bounces, &sc, o);
+        if (!r.wait_for_target(120.0)) return 1;
+        const image progress = *r.current_progress();
+        post_processor pp(&sc, false);
+        pp.submit_bloom_settings({true, 0.6f, 0.8f});
+        pp.submit_tonemapping_settings({true, 1, 1.2f, 2.2f});
+        const image post = pp.process(progress);
+        std::array<float, 16> id{}, moved{};
+        for (int k = 0; k < 4; ++k) id[5 * k] = moved[5 * k] = 1.0f;
+        moved[12] = 0.25f;
+        sc.set_instances({id, moved});
+        std::vector<ray> rr(nrays);
+        for (uint32_t i = 0; i < nrays; ++i)
+            rr[i] = ray{vec3{rays[i].org[0], rays[i].org[1], rays[i].org[2]},
+                        vec3{rays[i].dir[0], rays[i].dir[1], rays[i].dir[2]}};
+        const std::vector<intersection_record> recs = sc.cast_rays(rr);
+        FILE *g = std::fopen(out_path, "wb");
+        if (!g) return 2;
+        wr(g, draft.data(), (size_t)W * H * 4);
+        wr(g, progress.data(), (size_t)W * H * 4);
+        wr(g, post.data(), (size_t)W * H * 4);
+        for (const intersection_record &rec : recs) {
+            const uint32_t prim = rec.material ? rec.prim_id : CRG_INVALID_PRIM;
+            wr(g, &prim, 1);
+            wr(g, &rec.distance, 1);
+        }
+        std::fclose(g);
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "selftest: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char **argv) {
+    if (argc == 4 && std::strcmp(argv[1], "extras") == 0) return extras(argv[2], argv[3]);
     if (argc == 4 && std::strcmp(argv[1], "obj") == 0) return obj_parse(argv[2], argv[3]);
     if (argc == 7 && std::strcmp(argv[1], "objrender") == 0)
         return obj_render(argv[2], argv[3], (uint32_t)std::atoi(argv[4]), (uint32_t)std::atoi(argv[5]),

@@ -77,3 +77,52 @@ def test_adapter_matches_abi(ctx, tmp_path, mode):
     finally:
         film.close()
         scene.close()
+
+
+def test_adapter_draft_post_instances(ctx, tmp_path):
+    """crg::host::draft_renderer, post_processor and scene::set_instances (the
+    cr::draft_renderer / cr::post_processor / instances interfaces) against
+    direct ABI calls."""
+    sc = scenes.box_scene()
+    W, H, spp, bounces = 48, 40, 4, 6
+    rays = _rays(512, 5)
+    cam = api.make_camera(sc["camera"])
+    hdr = np.array([0x54475243, len(sc["mat_idx"]), len(sc["mats"]), W, H, spp, bounces, 1, len(rays), 36], np.uint32)
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(inp, "wb") as f:
+        for a in (hdr, sc["verts"].astype(np.float32), sc["mat_idx"].astype(np.uint32), sc["mats"]):
+            f.write(np.ascontiguousarray(a).tobytes())
+        f.write(bytes(cam))
+        f.write(rays.tobytes())
+    r = subprocess.run([EXE, "extras", str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    buf = open(out, "rb").read()
+    n4 = W * H * 4
+    draft = np.frombuffer(buf, np.float32, n4, 0)
+    progress = np.frombuffer(buf, np.float32, n4, n4 * 4)
+    post = np.frombuffer(buf, np.float32, n4, n4 * 8)
+    rec = np.frombuffer(buf, np.dtype([("prim", "<u4"), ("t", "<f4")]), len(rays), n4 * 12)
+
+    scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    img = api.DeviceBuffer(ctx, n4 * 4)
+    dst = api.DeviceBuffer(ctx, n4 * 4)
+    try:
+        api.draft_render(scene, sc["camera"], W, H, img, W / H)
+        assert np.array_equal(img.download(np.zeros(n4, np.float32)).view(np.uint32), draft.view(np.uint32))
+        img.upload(np.ascontiguousarray(progress))
+        ps = api.post_settings(bloom=1, bloom_threshold=0.6, bloom_strength=0.8, tonemapping=1, tonemap_type=1,
+                               exposure=1.2, gamma=2.2, mode=1)
+        api.post_process(ctx, img, dst, W, H, ps)
+        assert np.array_equal(dst.download(np.zeros(n4, np.float32)).view(np.uint32), post.view(np.uint32))
+        moved = np.eye(4, dtype=np.float32)
+        moved[0, 3] = 0.25
+        scene.set_instances(np.stack([np.eye(4, dtype=np.float32), moved]))
+        hits = scene.intersect(rays)
+        assert np.array_equal(rec["prim"], hits["prim"])
+        hit = hits["prim"] != 0xFFFFFFFF
+        assert hit.sum() > 200
+        assert np.array_equal(rec["t"][hit].view(np.uint32), hits["t"][hit].view(np.uint32))
+    finally:
+        img.free()
+        dst.free()
+        scene.close()
