@@ -435,6 +435,26 @@ def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
     return units, algo, "k_render + k_loss_l2 + k_adjoint (one forward/backward step)", 3 * args.steps, clk, ms
 
 
+def max_over_ranks(seconds, world, device):
+    """The slowest rank's timed-region length (replicas: every rank renders its own
+    copy of the workload), then a barrier so no rank leaves early."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def weak_scaling_value(units, steps, world, seconds):
+    """Whole-job throughput in millions of units per second: every rank processed
+    `units` per step."""
+    return units * steps * world / seconds / 1e6
+
+
 def wavefront_overrides(args):
     """Wavefront options given on the command line (host-driven loop, path pool size)."""
     o = {}
@@ -741,13 +761,8 @@ def main():
                       "d2h_bytes_per_step": int(n * 16), "ms_per_step": e2e_s * 1e3,
                       "path": "crg_memcpy_h2d (pinned rays) + crg_intersect_closest + crg_memcpy_d2h (pinned hits)"}
 
-    total_s = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-        torch.distributed.barrier()
-    value = units * args.steps * world / total_s / 1e6
+    total_s = max_over_ranks(sum(ms) / 1e3, world, "cuda")
+    value = weak_scaling_value(units, args.steps, world, total_s)
     achieved = algo / (total_s / args.steps) / 1e9
     if launches is None:
         # per frame: 3 prologue kernels + per device-loop iteration: the bounce kernels (3 split, 2 with the shadow
