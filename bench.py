@@ -113,6 +113,12 @@ def measured_peaks():
 
 
 POST = dict(width=3840, height=2160)
+# leaf sizes the autotuner tries per scene (bit mask of 1 << leaf_max)
+LEAVES = (1 << 1) | (1 << 2) | (1 << 3)
+# (width, treelet, leaf_max) fastest for the megakernel in a GB300 sweep of width {4, 8} x leaf {1, 2, 3}
+# x treelet rounds {3, 6}: box 616-623 Msamples/s at width 4 (592 at 8), displaced 655 at width 4 leaf 1
+# (579 at width 8 leaf 3)
+MEGA_BVH = {"box": (4, 1, 2), "displaced": (4, 1, 1)}
 
 
 def post_settings_full(api):
@@ -300,13 +306,16 @@ def time_to_rmse(ctx, api, scenes, timer, stream, target=1e-2):
     film.close()
     st = api.make_settings(512, 512, spp, 8, 3, 1, 1)
     f = api.Film(ctx, 512, 512)
+    s.build(*MEGA_BVH["box"], stream=stream)
     t_mega = timer.steps(lambda: (f.reset(stream), api.render(s, sc["camera"], st, f, stream)), 1, 1)[0]
-    tuned, width, _ = api.autotune_batch([s], [(0, sc["camera"], st)], sample_budget=1 << 27, widths=4 | 8, stream=stream)
+    tuned, width, _ = api.autotune_batch([s], [(0, sc["camera"], st)], sample_budget=1 << 27, widths=4 | 8, stream=stream,
+                                         leaves=LEAVES)
     t_wave = timer.steps(lambda: (f.reset(stream), ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], tuned, stream))), 1, 1)[0]
     f.close()
     s.close()
     return {"target_rmse": target, "spp": spp, "rmse": rmse, "reference": "FP64 16384-spp box image, independent seed",
             "megakernel_s": t_mega / 1e3, "wavefront_s": t_wave / 1e3,
+            "megakernel_bvh": dict(zip(("width", "treelet", "leaf_max"), MEGA_BVH["box"])),
             "wavefront_opts": dict(tuned, width=width), "note": "wavefront options from crg_autotune_batch (untimed)"}
 
 
@@ -353,7 +362,7 @@ def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
     work = scene.stats()
     scene.set_counting(False)
     units = 2 * W * W * SPP
-    algo = 2 * (work["nodes_visited"] * 80 + work["tris_tested"] * 48) + W * W * 12 * 4
+    algo = 2 * (work["nodes_visited"] * scene.info()["node_bytes"] + work["tris_tested"] * 48) + W * W * 12 * 4
     with ClockSampler(env_rank()[2]) as clk:
         ms = timer.steps(step, args.steps, args.warmup)
     f_ms = timer.steps(forward, 3, 1)
@@ -531,8 +540,9 @@ def main():
             out["autotune"] = {"skipped": True, "width": tuned_width, "opts": tuned}
         else:
             tuned, tuned_width, trials = api.autotune_batch([sb, sd], views, sample_budget=1 << 28, widths=4 | 8,
-                                                            stream=S)
+                                                            stream=S, leaves=LEAVES)
             out["autotune"] = {"seconds": time.perf_counter() - t0, "width": tuned_width, "opts": tuned,
+                               "leaf_max": {"box": sb.info()["leaf_max"], "displaced": sd.info()["leaf_max"]},
                                "trials": len(trials), "trial_batch_samples": 1 << 28,
                                "best_trial_msamples_per_s": max(t["msamples_per_s"] for t in trials)}
         tuned = dict(tuned, **wavefront_overrides(args))
@@ -554,17 +564,18 @@ def main():
         torch.cuda.synchronize()
         work = api.batch_stats(ctx)
         rays = work["segments"] + work["shadow_rays"]
-        algo = rays * 48 + work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
+        algo = rays * 48 + work["nodes_visited"] * sd.info()["node_bytes"] + work["tris_tested"] * 48 + units * 12
         with ClockSampler(local) as clk:
             ms = timer.steps(wave, args.steps, args.warmup)
-        if tuned_width != 8:  # the megakernel runs at its own best width (8)
-            sb.build(8, 1, stream=S)
-            sd.build(8, 1, stream=S)
+        wave_leaf = (sb.info()["leaf_max"], sd.info()["leaf_max"])
+        sb.build(*MEGA_BVH["box"], stream=S)  # the megakernel runs on its own best BVHs
+        sd.build(*MEGA_BVH["displaced"], stream=S)
         mega_ms = timer.steps(mega, 2, 1)
         out["megakernel"] = {"value": units / (sum(mega_ms) / len(mega_ms) / 1e3) / 1e6, "unit": unit,
                              "ms_per_step": sum(mega_ms) / len(mega_ms),
-                             "how": "same 64 views, one crg_render call per view (the drop-in), BVH width 8, "
-                                    "1 warm-up + 2 steps"}
+                             "bvh": {k: dict(zip(("width", "treelet", "leaf_max"), v)) for k, v in MEGA_BVH.items()},
+                             "how": "same 64 views, one crg_render call per view (the drop-in), on the BVH options "
+                                    "fastest for the megakernel in a sweep of width x leaf size; 1 warm-up + 2 steps"}
         out["work"] = {**work, "mrays_per_step": rays / 1e6}
         kernel = "wavefront frame: one graph launch (k_wf_extend / k_wf_shade / k_wf_shadow / control / resolve)"
         launches = None  # counted below from the iteration count
@@ -580,8 +591,8 @@ def main():
         d2h = sum(o.array.nbytes for o in outs)
 
         def e2e_step():
-            a = api.Scene(ctx, *[p.array for p in pins["box"]]).build(tuned_width, 1, stream=S)
-            b = api.Scene(ctx, *[p.array for p in pins["disp"]]).build(tuned_width, 1, stream=S)
+            a = api.Scene(ctx, *[p.array for p in pins["box"]]).build(tuned_width, 1, wave_leaf[0], stream=S)
+            b = api.Scene(ctx, *[p.array for p in pins["disp"]]).build(tuned_width, 1, wave_leaf[1], stream=S)
             b.set_skybox(disp["skybox"])
             for f in films:
                 f.reset(S)
@@ -611,7 +622,11 @@ def main():
         else:
             sc = scenes.displaced_scene()
             st = api.make_settings(1920, 1080, 16, 16, 3, 1, 1, 1920 / 1080)
-        scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+        # the megakernel on its own best BVH; the wavefront form on width 8 with the leaf size its tuner
+        # picks for each scene (box 3, displaced 1)
+        bvh = MEGA_BVH[args.workload] if args.form == "megakernel" else (8, 1, 3 if args.workload == "box" else 1)
+        scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(*bvh)
+        out["bvh"] = dict(zip(("width", "treelet", "leaf_max"), bvh))
         if "skybox" in sc:
             scene.set_skybox(sc["skybox"])
         film = api.Film(ctx, st.width, st.height)
@@ -643,7 +658,7 @@ def main():
             kernel = "wavefront frame: one graph launch"
             launches = args.steps * (3 + 7 * int(work["iterations"]))
         rays = work["segments"] + work["shadow_rays"]
-        algo = work["nodes_visited"] * 80 + work["tris_tested"] * 48 + units * 12
+        algo = work["nodes_visited"] * scene.info()["node_bytes"] + work["tris_tested"] * 48 + units * 12
         out["work"] = {**work, "mrays_per_step": rays / 1e6}
         out["form"] = args.form
         with ClockSampler(local) as clk:
@@ -655,7 +670,7 @@ def main():
         pv.array[...], pm.array[...], pmat.array[...] = sc["verts"], sc["mat_idx"], sc["mats"]
 
         def e2e_step():
-            s2 = api.Scene(ctx, pv.array, pm.array, pmat.array).build(8, 1, stream=S)
+            s2 = api.Scene(ctx, pv.array, pm.array, pmat.array).build(*bvh, stream=S)
             if "skybox" in sc:
                 s2.set_skybox(sc["skybox"])
             film.reset(S)
@@ -736,7 +751,7 @@ def main():
         ctx.check(lib.crg_intersect_closest_counted(scene.h, rb.ptr, hb.ptr, nb.ptr, tb.ptr, n, S))
         nodes = int(nb.download(np.zeros(n, np.uint32)).astype(np.int64).sum())
         tris = int(tb.download(np.zeros(n, np.uint32)).astype(np.int64).sum())
-        algo = n * 48 + nodes * 80 + tris * 48
+        algo = n * 48 + nodes * scene.info()["node_bytes"] + tris * 48
         out["work"] = {"nodes_visited": nodes, "tris_tested": tris}
         with ClockSampler(local) as clk:
             ms = timer.steps(step, args.steps, args.warmup)

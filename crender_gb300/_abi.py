@@ -75,6 +75,8 @@ class BvhInfo(C.Structure):
         ("n_tri_slots", C.c_uint32),
         ("depth", C.c_uint32),
         ("sah_cost", C.c_float),
+        ("leaf_max", C.c_uint32),
+        ("treelet", C.c_uint32),
     ]
 
 
@@ -89,7 +91,8 @@ class WavefrontOpts(C.Structure):
 
 
 class AutotuneOpts(C.Structure):
-    _fields_ = [("sample_budget", C.c_uint64), ("widths", C.c_uint32), ("reuse", C.c_uint32)]
+    _fields_ = [("sample_budget", C.c_uint64), ("widths", C.c_uint32), ("reuse", C.c_uint32), ("leaves", C.c_uint32),
+                ("pad_", C.c_uint32)]
 
 
 class AutotuneTrial(C.Structure):

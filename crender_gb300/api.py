@@ -309,8 +309,9 @@ OPT_FIELDS = ("path_pool", "chunk_samples", "block_size", "fetch", "max_iteratio
               "refill")
 
 
-def autotune_batch(scenes, views, sample_budget=0, widths=0, reuse=True, stream=None):
-    """crg_autotune_batch: returns (options dict for render_batch, BVH width, trials list)."""
+def autotune_batch(scenes, views, sample_budget=0, widths=0, reuse=True, stream=None, leaves=0):
+    """crg_autotune_batch: returns (options dict for render_batch, BVH width, trials list).
+    `leaves` is a bit mask of leaf sizes to try per scene (1 << 1 | 1 << 2 | 1 << 3)."""
     ctx = scenes[0].ctx
     sc = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
     vs = (_abi.View * len(views))()
@@ -318,7 +319,7 @@ def autotune_batch(scenes, views, sample_budget=0, widths=0, reuse=True, stream=
         vs[i].scene = si
         vs[i].camera = make_camera(cam)
         vs[i].settings = st
-    o = _abi.AutotuneOpts(int(sample_budget), int(widths), int(bool(reuse)))
+    o = _abi.AutotuneOpts(int(sample_budget), int(widths), int(bool(reuse)), int(leaves), 0)
     best, width, n = _abi.WavefrontOpts(), C.c_uint32(), C.c_uint32()
     cap = 64
     trials = (_abi.AutotuneTrial * cap)()

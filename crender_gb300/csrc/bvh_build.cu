@@ -862,6 +862,8 @@ extern "C" crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri,
         *info = crg_bvh_info{};
         info->ntri = n;
         info->width = o.width;
+        info->leaf_max = o.leaf_max;
+        info->treelet = o.treelet;
         info->node_bytes = node_bytes;
         info->n_bvh2_nodes = n >= 2 ? n - 1 : 0;
         info->n_tri_slots = n;

@@ -674,6 +674,8 @@ crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info) {
     info->n_tri_slots = scene->ntri;
     info->depth = scene->depth;
     info->sah_cost = scene->sah;
+    info->leaf_max = scene->opts.leaf_max;
+    info->treelet = scene->opts.treelet;
     return CRG_OK;
 }
 

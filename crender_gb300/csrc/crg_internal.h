@@ -25,6 +25,7 @@ struct crg_context {
     struct Tuned {
         crg_wavefront_opts opts;
         uint32_t width;
+        std::vector<uint32_t> leaf; // per scene
     };
     std::map<std::string, Tuned> tune_cache; // autotuner results by batch shape
 };

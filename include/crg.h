@@ -245,6 +245,8 @@ typedef struct crg_bvh_info {
     uint32_t n_tri_slots;    /* triangles in the wide-BVH triangle array */
     uint32_t depth;          /* wide-BVH depth (levels) */
     float sah_cost;          /* SAH cost of the binary tree (Ci=1.2, Ct=1) */
+    uint32_t leaf_max;       /* the build's crg_build_opts::leaf_max */
+    uint32_t treelet;        /* the build's crg_build_opts::treelet */
 } crg_bvh_info;
 crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info);
 /* Copies to host: bvh2 = float[n_bvh2_nodes*8] (lo.xyz,left, hi.xyz,right; child
@@ -469,7 +471,8 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
  * view's spp scaled down so the trial holds about sample_budget samples, into
  * scratch films) under candidate settings and keeps the fastest by device
  * time: BVH width (the scenes are rebuilt with their build options at each
- * width tried, and left built at the winner), stage fusion, per-lane refill,
+ * width tried, and left built at the winner), each scene's leaf size, stage
+ * fusion, per-lane refill,
  * queue fetch size, block size and path pool, searched one knob at a time
  * from the defaults.  Every candidate renders identical films, so the choice
  * only trades speed.  Results are cached in the context by batch shape. */
@@ -477,6 +480,10 @@ typedef struct crg_autotune_opts {
     uint64_t sample_budget; /* samples per trial batch (0 = 134,217,728) */
     uint32_t widths;        /* BVH widths to try, bit mask of 2 | 4 | 8 (0 = keep the scenes' width) */
     uint32_t reuse;         /* 1 = return the cached result for a batch of the same shape */
+    uint32_t leaves;        /* leaf sizes (crg_build_opts::leaf_max) to try for each scene on its own,
+                               bit mask of 1 << 1 | 1 << 2 | 1 << 3 (0 = keep the scenes' leaf sizes);
+                               the scenes are left built with the winners */
+    uint32_t pad_;
 } crg_autotune_opts;
 
 typedef struct crg_autotune_trial {

@@ -787,6 +787,8 @@ void orc_bvh_info(const orc_bvh *b, crg_bvh_info *info) {
     info->n_tri_slots = (uint32_t)(b->tris.size() / 12);
     info->depth = b->depth;
     info->sah_cost = b->sah;
+    info->leaf_max = b->opts.leaf_max;
+    info->treelet = b->opts.treelet;
 }
 
 void orc_bvh_download(const orc_bvh *b, float *bvh2, uint32_t *order, void *wide, float *tris) {

@@ -195,3 +195,33 @@ def test_autotune_picks_options_that_render_identically(ctx):
     finally:
         sa.close()
         sb.close()
+
+
+def test_autotune_leaf_sizes(ctx):
+    """With leaves set, the autotuner also picks each scene's leaf size, leaves
+    the scenes built with it, and renders identical films; a cached answer
+    rebuilds scenes whose leaf size has been changed since."""
+    a = _box_variant("plain")
+    b = _box_variant("materials")
+    sa = api.Scene(ctx, a["verts"], a["mat_idx"], a["mats"]).build(8, 1)
+    sb = api.Scene(ctx, b["verts"], b["mat_idx"], b["mats"]).build(8, 1)
+    views = [(0, a["camera"], api.make_settings(48, 48, 16, 8, 3, 1, 1)),
+             (1, b["camera"], api.make_settings(32, 32, 32, 8, 3, 1, 2))]
+    leaves = (1 << 1) | (1 << 2) | (1 << 3)
+    try:
+        opts, width, trials = api.autotune_batch([sa, sb], views, sample_budget=1 << 16, widths=8, leaves=leaves)
+        la, lb = sa.info()["leaf_max"], sb.info()["leaf_max"]
+        assert la in (1, 2, 3) and lb in (1, 2, 3)
+        assert len(trials) >= 1 + 2 + 2  # defaults, two more leaf sizes per scene
+        refs = [_mega(ctx, (sa, sb)[si], cam, st) for si, cam, st in views]
+        films = [api.Film(ctx, st.width, st.height, f64=True) for _, _, st in views]
+        ctx.check(api.render_batch([sa, sb], views, films, opts))
+        for f, r in zip(films, refs):
+            _same(f.download(f64=True), r)
+            f.close()
+        sa.build(8, 1, 3 if la != 3 else 1)
+        again, width2, trials2 = api.autotune_batch([sa, sb], views, sample_budget=1 << 16, widths=8, leaves=leaves)
+        assert again == opts and trials2 == [] and sa.info()["leaf_max"] == la
+    finally:
+        sa.close()
+        sb.close()
