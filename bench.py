@@ -705,17 +705,17 @@ def main():
         dst = api.DeviceBuffer(ctx, img.nbytes)
         ps = post_settings_full(api)
         units = W * H
-        # per pixel: 5 fused (horizontal, vertical) blur pairs each read 16 B and write 16 B (the first reads
-        # the source); the composite reads source + bloom and writes the output
-        algo = units * (5 * 32 + 48)
+        # per pixel: pass 0 reads the source and writes 16 B, passes 1-9 read and write 16 B each,
+        # the composite reads source + bloom and writes the output
+        algo = units * (10 * 32 + 48)
 
         def step():
             api.post_process(ctx, src, dst, W, H, ps, S)
 
         with ClockSampler(local) as clk:
             ms = timer.steps(step, args.steps, args.warmup)
-        kernel = "k_blur_pair x 5 + k_post_final (one crg_post_process call)"
-        launches = 6 * args.steps
+        kernel = "k_blur_h / k_blur_v x 10 + k_post_final (one crg_post_process call)"
+        launches = 11 * args.steps
         pin_in = api.PinnedArray(ctx, img.shape, np.float32)
         pin_out = api.PinnedArray(ctx, img.shape, np.float32)
         pin_in.array[...] = img

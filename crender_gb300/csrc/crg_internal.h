@@ -21,7 +21,6 @@ struct crg_context {
     int sm_count = 0;
     DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
     DevBuf post_ws; // post-process ping-pong images, grow-only
-    bool post_smem_set = false; // blur kernels allowed their dynamic shared memory on this device
     crg_render_stats batch_stats{};
     struct Tuned {
         crg_wavefront_opts opts;

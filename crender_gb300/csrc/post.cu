@@ -13,9 +13,10 @@
 // without contraction (-fmad=false), so results equal the oracle's CPU
 // restatement bit for bit except where powf is involved (tone-mapping gamma).
 //
-// The 10 blur passes run as 5 fused (horizontal, vertical) pairs on 32x32
-// tiles staged in shared memory: each pair reads its input and writes its
-// output once (16 + 16 bytes per pixel in HBM, the halo re-reads from L2).
+// Each pixel of a pass costs 16 bytes read + 16 bytes written in HBM/L2; the
+// 15-tap neighbourhoods are staged in shared memory (a row segment for the
+// horizontal pass, a column tile for the vertical one), so each texel is read
+// from global memory once per pass.
 #include <algorithm>
 #include <cstdint>
 
@@ -36,7 +37,9 @@ struct PostDims {
     float threshold;
 };
 
-constexpr int kHalo = 7; // taps on each side of the centre
+constexpr int kRowTile = 256;          // horizontal pass: pixels of a row per block
+constexpr int kColW = 32, kColH = 32;  // vertical pass: tile of columns x rows per block
+constexpr int kHalo = 7;
 
 // _brightness (post_processor.cpp:296-307) visits pixel (i % w, i / h) for
 // i < w*h.  Pixel (x, y) is visited iff some i = x + k*w lies in [y*h, y*h + h)
@@ -75,52 +78,52 @@ __device__ __forceinline__ float4 blur_taps(const float4 *s, int stride) {
     return make_float4(r, g, b, 1.0f);
 }
 
-// Two consecutive blur passes, horizontal then vertical, on a 32x32 output
-// tile: the input tile and a 7-texel halo are staged in shared memory, the
-// horizontal results for the tile's columns over 46 rows are kept in shared
-// memory, and only the vertical results are written.  Each pixel's two sums
-// are the same float operations in the same order as two separate passes, and
-// the horizontal results outside the covered region (or the image) are zero,
-// as the reference's cleared target texture is, so the output equals the
-// pass-by-pass sequence bit for bit with half the global traffic.
-// BRIGHT: the source is the un-thresholded image; the threshold is applied to
-// each staged texel (the first pass reads _brightness's output, never stored).
-constexpr int kTile = 32;
-constexpr int kIn = kTile + 2 * kHalo; // 46
-constexpr size_t kPairSmem = sizeof(float4) * (size_t)(kIn * kIn + kIn * kTile);
-
+// Horizontal pass.  BRIGHT: the source is the un-thresholded image and the
+// threshold is applied to each staged texel (the first pass reads _brightness's
+// output, which is never stored).  Pixels outside the covered region are
+// written as zero, as the reference clears its target before each dispatch.
 template <bool BRIGHT>
-__global__ void __launch_bounds__(256) k_blur_pair(const float4 *__restrict__ src, float4 *__restrict__ dst, PostDims p) {
-    extern __shared__ float4 sm[];
-    float4 *in = sm;              // [kIn][kIn]
-    float4 *hb = sm + kIn * kIn;  // [kIn][kTile]
-    const int x0 = (int)(blockIdx.x * kTile), y0 = (int)(blockIdx.y * kTile);
-    const int tid = (int)(threadIdx.y * 32 + threadIdx.x);
-    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int i = tid; i < kIn * kIn; i += 256) {
-        const int y = y0 + i / kIn - kHalo, x = x0 + i % kIn - kHalo;
-        float4 v = zero;
-        if (x >= 0 && x < (int)p.w && y >= 0 && y < (int)p.h) {
-            v = src[(size_t)y * p.w + x];
-            if (BRIGHT) v = bright(v, (uint32_t)x, (uint32_t)y, p);
+__global__ void __launch_bounds__(kRowTile) k_blur_h(const float4 *__restrict__ src, float4 *__restrict__ dst,
+                                                     PostDims p) {
+    __shared__ float4 row[kRowTile + 2 * kHalo];
+    const uint32_t y = blockIdx.y;
+    const int x0 = (int)(blockIdx.x * kRowTile);
+    const float4 *srow = src + (size_t)y * p.w;
+    for (int i = threadIdx.x; i < kRowTile + 2 * kHalo; i += kRowTile) {
+        const int x = x0 + i - kHalo;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (x >= 0 && x < (int)p.w) {
+            v = srow[x];
+            if (BRIGHT) v = bright(v, (uint32_t)x, y, p);
         }
-        in[i] = v;
+        row[i] = v;
     }
     __syncthreads();
-    for (int i = tid; i < kIn * kTile; i += 256) {
-        const int ry = i / kTile, cx = i % kTile;
-        const int y = y0 + ry - kHalo, x = x0 + cx;
-        float4 v = zero;
-        if (y >= 0 && y < (int)p.rh && x < (int)p.rw) v = blur_taps(&in[ry * kIn + cx + kHalo], 1);
-        hb[i] = v;
+    const uint32_t x = (uint32_t)x0 + threadIdx.x;
+    if (x >= p.w) return;
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (x < p.rw && y < p.rh) out = blur_taps(&row[threadIdx.x + kHalo], 1);
+    dst[(size_t)y * p.w + x] = out;
+}
+
+__global__ void __launch_bounds__(kColW * 8) k_blur_v(const float4 *__restrict__ src, float4 *__restrict__ dst,
+                                                      PostDims p) {
+    __shared__ float4 col[kColH + 2 * kHalo][kColW];
+    const uint32_t x = blockIdx.x * kColW + threadIdx.x;
+    const int y0 = (int)(blockIdx.y * kColH);
+    for (int r = threadIdx.y; r < kColH + 2 * kHalo; r += 8) {
+        const int y = y0 + r - kHalo;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (x < p.w && y >= 0 && y < (int)p.h) v = src[(size_t)y * p.w + x];
+        col[r][threadIdx.x] = v;
     }
     __syncthreads();
-    for (int i = tid; i < kTile * kTile; i += 256) {
-        const int ty = i / kTile, cx = i % kTile;
-        const uint32_t y = (uint32_t)(y0 + ty), x = (uint32_t)(x0 + cx);
-        if (x >= p.w || y >= p.h) continue;
-        float4 out = zero;
-        if (x < p.rw && y < p.rh) out = blur_taps(&hb[(ty + kHalo) * kTile + cx], kTile);
+    if (x >= p.w) return;
+    for (int k = threadIdx.y; k < kColH; k += 8) {
+        const uint32_t y = (uint32_t)(y0 + k);
+        if (y >= p.h) break;
+        float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (x < p.rw && y < p.rh) out = blur_taps(&col[k + kHalo][threadIdx.x], kColW);
         dst[(size_t)y * p.w + x] = out;
     }
 }
@@ -212,7 +215,7 @@ extern "C" crg_status crg_post_process(crg_context *ctx, const float *d_src, flo
                                        uint32_t height, const crg_post_settings *settings, crg_stream stream) {
     if (!ctx || !d_src || !d_dst || !settings) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
     if (width == 0 || height == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty image");
-    if (width > 65535u * kTile || height > 65535u * kTile) return set_error(ctx, CRG_ERR_INVALID_ARG, "image too large");
+    if (width > 65536u * kRowTile || height > 65535u) return set_error(ctx, CRG_ERR_INVALID_ARG, "image too large");
     if (d_src == d_dst) return set_error(ctx, CRG_ERR_INVALID_ARG, "source and destination alias");
     const crg_post_settings &s = *settings;
     if (s.mode > CRG_POST_FULL) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad post-process mode");
@@ -235,23 +238,20 @@ extern "C" crg_status crg_post_process(crg_context *ctx, const float *d_src, flo
     if (s.bloom) {
         crg_status rc = dev_alloc(ctx, ctx->post_ws, npix * 32);
         if (rc != CRG_OK) return rc;
-        float4 *ba = (float4 *)ctx->post_ws.ptr;
-        float4 *bb = ba + npix;
-        if (!ctx->post_smem_set) { // 57 KB of dynamic shared memory per block, above the 48 KB default
-            CRG_CUDA(ctx, cudaFuncSetAttribute(k_blur_pair<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem));
-            CRG_CUDA(ctx, cudaFuncSetAttribute(k_blur_pair<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem));
-            ctx->post_smem_set = true;
+        b0 = (float4 *)ctx->post_ws.ptr;
+        float4 *b1 = b0 + npix;
+        const dim3 gh((width + kRowTile - 1) / kRowTile, height);
+        const dim3 gv((width + kColW - 1) / kColW, (height + kColH - 1) / kColH);
+        // _blur (post_processor.cpp:246-294): pass i reads buffers[i % 2] and
+        // writes the other; even passes are horizontal; the result is buffers[0].
+        // buffers[0] starts as the thresholded image, applied inside pass 0.
+        k_blur_h<true><<<gh, kRowTile, 0, st>>>(src, b1, p);
+        for (int i = 1; i < 10; ++i) {
+            const float4 *from = (i % 2 == 0) ? b0 : b1;
+            float4 *to = (i % 2 == 0) ? b1 : b0;
+            if (i % 2 == 0) k_blur_h<false><<<gh, kRowTile, 0, st>>>(from, to, p);
+            else k_blur_v<<<gv, dim3(kColW, 8), 0, st>>>(from, to, p);
         }
-        const dim3 grid((width + kTile - 1) / kTile, (height + kTile - 1) / kTile), block(32, 8);
-        // _blur (post_processor.cpp:246-294): 10 passes, horizontal on even ones,
-        // here as 5 fused (horizontal, vertical) pairs ping-ponging between two
-        // images; the first pair thresholds its input (_brightness)
-        k_blur_pair<true><<<grid, block, kPairSmem, st>>>(src, ba, p);
-        for (int k = 1; k < 5; ++k) {
-            const bool odd = (k % 2) == 1;
-            k_blur_pair<false><<<grid, block, kPairSmem, st>>>(odd ? ba : bb, odd ? bb : ba, p);
-        }
-        b0 = ba; // pair 4 (even) writes ba
         CRG_CUDA(ctx, cudaGetLastError());
     }
     const unsigned blocks = (unsigned)std::min<size_t>((npix + 255) / 256, (size_t)std::max(ctx->sm_count, 1) * 8);
