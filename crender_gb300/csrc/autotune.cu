@@ -6,7 +6,7 @@
 // ~9% faster with one triangle per leaf slot, the 36-triangle box ~8% slower),
 // stage fusion {split, shadow-in-shade, one kernel per bounce},
 // per-lane refill {off, 4, 16}, warp fetch {32, 64}, block size {128, 256}
-// path pool {8M, 32M, 64M} and chunk {128M, 256M} samples.  Each candidate renders a reduced copy of the
+// path pool {8M, 32M, 64M, 128M} and chunk {128M, 256M} samples.  Each candidate renders a reduced copy of the
 // batch (spp scaled to a sample budget) into scratch films: one untimed run,
 // then one run timed with CUDA events on the caller's stream.
 #include <algorithm>
@@ -206,7 +206,7 @@ extern "C" crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nsce
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.block_size = v; }, {128u, 256u});
     // pools small enough for L2 (about 160 B per path) measured 35-45% slower on GB300 (fewer paths per
     // iteration, more iterations), so the sweep looks at large pools and chunks only
-    sweep([](crg_wavefront_opts &c, uint32_t v) { c.path_pool = v; }, {1u << 23, 1u << 25, 1u << 26});
+    sweep([](crg_wavefront_opts &c, uint32_t v) { c.path_pool = v; }, {1u << 23, 1u << 25, 1u << 26, 1u << 27});
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.chunk_samples = v; }, {1u << 27, 1u << 28});
 
     for (crg_film *f : films)
