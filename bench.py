@@ -535,7 +535,7 @@ def main():
         t0 = time.perf_counter()
         if args.no_autotune:
             # options the autotuner picks for this batch on a GB300 (fixed, so profiler runs launch no tuning graphs)
-            tuned, tuned_width = dict(path_pool=1 << 25, chunk_samples=1 << 27, block_size=256, fetch=64,
+            tuned, tuned_width = dict(path_pool=1 << 27, chunk_samples=1 << 27, block_size=256, fetch=64,
                                       max_iterations=0, count_work=0, host_loop=0, fuse=1, refill=16), 8
             out["autotune"] = {"skipped": True, "width": tuned_width, "opts": tuned}
         else:

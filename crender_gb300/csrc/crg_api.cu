@@ -896,9 +896,10 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         for (uint32_t u = 0; u < v; ++u)
             if (films[u] == films[v]) return set_error(ctx, CRG_ERR_INVALID_ARG, "films must be distinct");
     }
-    // defaults: 32M paths in flight (about 5 GB of path state), 128M-sample chunks (2 GB of
+    // defaults: up to 128M paths in flight (about 20 GB of path state for a batch that large; a
+    // frame never holds more paths than its largest chunk's samples), 128M-sample chunks (2 GB of
     // sample slots), split stages with per-lane refill in the traversal stages
-    crg_wavefront_opts o{1u << 25, 1u << 27, 128, 32, 0, 0, 0, 1, 16};
+    crg_wavefront_opts o{1u << 27, 1u << 27, 128, 32, 0, 0, 0, 1, 16};
     if (opts) {
         if (opts->path_pool) o.path_pool = opts->path_pool;
         if (opts->chunk_samples) o.chunk_samples = opts->chunk_samples;

@@ -433,7 +433,8 @@ typedef struct crg_view {
 /* Wavefront knobs (the autotuner's search space besides the BVH width).
  * Zero fields take the defaults. */
 typedef struct crg_wavefront_opts {
-    uint32_t path_pool;     /* paths in flight (default 33,554,432; at most the chunk's samples) */
+    uint32_t path_pool;     /* paths in flight (default 134,217,728; at most the chunk's samples;
+                               about 156 bytes of path state each) */
     uint32_t chunk_samples; /* samples resolved into the films per chunk (default 134,217,728) */
     uint32_t block_size;    /* threads per block of the persistent kernels: 64, 128 or 256 (default 128) */
     uint32_t fetch;         /* queue entries a warp takes per atomic, multiple of 32 (default 32) */
