@@ -6,7 +6,7 @@
 // ~9% faster with one triangle per leaf slot, the 36-triangle box ~8% slower),
 // stage fusion {split, shadow-in-shade, one kernel per bounce},
 // per-lane refill {off, 4, 16}, warp fetch {32, 64}, block size {128, 256}
-// path pool {32M, 64M, 128M, 256M} and chunk {128M, 256M, 512M} samples.  Each candidate renders a reduced copy of the
+// path pool {32M, 64M, 128M} (128M-sample chunks).  Each candidate renders a reduced copy of the
 // batch (spp scaled to a sample budget) into scratch films: one untimed run,
 // then one run timed with CUDA events on the caller's stream.
 #include <algorithm>
@@ -204,12 +204,12 @@ extern "C" crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nsce
     if (cur.fuse <= 2) sweep([](crg_wavefront_opts &c, uint32_t v) { c.refill = v; }, {kOff, 4u, 16u});
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.fetch = v; }, {32u, 64u});
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.block_size = v; }, {128u, 256u});
-    // Path pool: on a GB300 the batch renders faster with more paths in flight (32M -> 64M -> 128M paths:
-    // +12%, +9%; fewer, fuller iterations), while pools small enough to keep the path state (about 156 B
-    // per path) in L2 measured 35-45% slower.  A chunk never holds fewer samples than the pool.
-    sweep([](crg_wavefront_opts &c, uint32_t v) { c.path_pool = v; c.chunk_samples = std::max(c.chunk_samples, v); },
-          {1u << 25, 1u << 26, 1u << 27, 1u << 28});
-    sweep([](crg_wavefront_opts &c, uint32_t v) { c.chunk_samples = std::max(v, c.path_pool); }, {1u << 27, 1u << 28, 1u << 29});
+    // Path pool, up to the 128M-sample chunk: on a GB300 the 64-view batch renders faster with more paths
+    // in flight (32M -> 64M -> 128M paths: +12%, +9%; fewer, fuller iterations), while pools small enough
+    // to keep the path state (about 156 B per path) in L2 measured 35-45% slower.  Larger chunks are not
+    // searched: a reduced trial batch fits in one of them and rewards them (256M paths in 512M-sample
+    // chunks won the trials at 1203 Msamples/s but rendered the full batch at 1110 against 1192).
+    sweep([](crg_wavefront_opts &c, uint32_t v) { c.path_pool = v; }, {1u << 25, 1u << 26, 1u << 27});
 
     for (crg_film *f : films)
         if (f) crg_film_destroy(f);
