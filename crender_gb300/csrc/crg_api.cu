@@ -233,7 +233,7 @@ crg_status prepare_lights(crg_scene *s) {
     crg_status rc;
     if ((rc = dev_alloc(s->ctx, s->mat_light_pdf, 4 * (size_t)(nmat ? nmat : 1))) != CRG_OK) return rc;
     if (nmat) CRG_CUDA(s->ctx, cudaMemcpy(s->mat_light_pdf.ptr, mpdf.data(), 4 * nmat, cudaMemcpyHostToDevice));
-    return CRG_OK;
+    return build_light_records(s);
 }
 
 // Affine 4x4 (column-major, glm::mat4 layout) -> device rows {inverse, forward}.
@@ -334,7 +334,7 @@ void scene_free(crg_scene *s) {
     if (!s) return;
     DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_alias, &s->light_pdf, &s->mat_light_pdf,
                       &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead,
-                      &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst};
+                      &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst, &s->light_rec};
     for (DevBuf *b : bufs) dev_free(*b);
     delete s;
 }
@@ -620,7 +620,7 @@ crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float 
     dev_free(scene->texels);
     dev_free(scene->tex_info);
     scene->ntex = 0;
-    if (count == 0) return CRG_OK;
+    if (count == 0) return build_light_records(scene);
     crg_status rc;
     if ((rc = dev_alloc(ctx, scene->texels, 16 * total)) != CRG_OK) return rc;
     if ((rc = dev_alloc(ctx, scene->tex_info, 16 * (size_t)count)) != CRG_OK) return rc;
@@ -631,7 +631,7 @@ crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float 
     }
     CRG_CUDA(ctx, cudaMemcpy(scene->tex_info.ptr, info.data(), 16 * (size_t)count, cudaMemcpyHostToDevice));
     scene->ntex = count;
-    return CRG_OK;
+    return build_light_records(scene); // emitters' textured flags follow the texture count
 }
 
 crg_status crg_scene_set_instances(crg_scene *scene, const float *xforms, uint32_t ninst) {

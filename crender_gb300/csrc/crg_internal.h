@@ -57,6 +57,7 @@ struct crg_scene {
     uint32_t nlights = 0;
     std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table
     DevBuf light_prim, light_alias, light_pdf, mat_light_pdf; // light_alias: float2 {prob, alias bits}
+    DevBuf light_rec; // float4[4] per emitter entry: world corners, pdf, prim, material, radiance
     // environment / sun
     DevBuf sky;
     uint32_t sky_w = 0, sky_h = 0;
@@ -117,6 +118,7 @@ struct CamDev {
 CamDev camera_params(const crg_camera &c);
 crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &set, crg_film *film,
                          cudaStream_t stream);
+crg_status build_light_records(crg_scene *s);
 
 // draft.cu
 crg_status launch_draft(crg_scene *s, const CamDev &cam, uint32_t w, uint32_t h, float aspect, float *d_rgba,

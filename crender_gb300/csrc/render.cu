@@ -151,6 +151,46 @@ void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, con
 
 } // namespace
 
+namespace {
+// Emitter records (see SceneDev::light_rec), built once per emitter table with
+// the same device arithmetic the NEE sample would otherwise repeat per path.
+__global__ void k_light_records(SceneDev S, float4 *__restrict__ rec) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= S.nlights) return;
+    const uint32_t prim = S.light_prim[j];
+    v3 a, b, c;
+    prim_verts(S, prim, a, b, c);
+    if (S.ninst) {
+        const float4 *F = S.inst + 6 * (size_t)S.light_inst[j] + 3;
+        a = xf_point(F, a);
+        b = xf_point(F, b);
+        c = xf_point(F, c);
+    }
+    const uint32_t mi = S.mat_idx[prim];
+    const crg_material &m = S.mats[mi];
+    float4 *r = rec + 4 * (size_t)j;
+    r[0] = make_float4(a.x, a.y, a.z, S.light_pdf[j]);
+    r[1] = make_float4(b.x, b.y, b.z, __uint_as_float(prim));
+    r[2] = make_float4(c.x, c.y, c.z, __uint_as_float(mi));
+    r[3] = make_float4(m.colour[0] * m.emission, m.colour[1] * m.emission, m.colour[2] * m.emission,
+                       __uint_as_float(textured(S, m) ? 1u : 0u));
+}
+
+} // namespace
+
+// Builds the emitter records of a scene's current emitter table (call after the
+// table, the materials, the textures or the instances change).
+crg_status build_light_records(crg_scene *s) {
+    if (s->nlights == 0) return CRG_OK;
+    crg_status rc = dev_alloc(s->ctx, s->light_rec, 64 * (size_t)s->nlights);
+    if (rc != CRG_OK) return rc;
+    const SceneDev S = scene_dev(s);
+    k_light_records<<<(s->nlights + 127) / 128, 128>>>(S, (float4 *)s->light_rec.ptr);
+    CRG_CUDA(s->ctx, cudaGetLastError());
+    CRG_CUDA(s->ctx, cudaDeviceSynchronize());
+    return CRG_OK;
+}
+
 namespace rc {
 SceneDev scene_dev(const crg_scene *s) {
     SceneDev S{};
@@ -169,6 +209,7 @@ SceneDev scene_dev(const crg_scene *s) {
     S.ntex = s->texels.ptr ? s->ntex : 0;
     S.inst = (const float4 *)s->inst.ptr;
     S.light_inst = (const uint32_t *)s->light_inst.ptr;
+    S.light_rec = (const float4 *)s->light_rec.ptr;
     S.ninst = s->inst.ptr ? s->ninst : 0;
     S.nlights = s->nlights;
     S.ntri = s->ntri;

@@ -36,6 +36,9 @@ struct SceneDev {
     // transform; ninst = 0 means the mesh is used as is
     const float4 *inst;
     const uint32_t *light_inst; // instance of each emitter entry (instanced scenes)
+    // per emitter entry 4 float4: (v0, pdf), (v1, prim bits), (v2, material bits), (colour * emission,
+    // textured flag bits); v0..v2 in world space
+    const float4 *light_rec;
     uint32_t ninst;
     uint32_t nlights, ntri;
     uint32_t sky_w, sky_h;
@@ -530,15 +533,11 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
     nr.kind = 0;
     const f4 g = rand4(C.pix, C.sample, 2 + 2 * i, C.seed);
     const uint32_t j = pick_light(S, g.x, g.w);
-    const uint32_t prim = __ldg(&S.light_prim[j]);
-    v3 a, b, c;
-    prim_verts(S, prim, a, b, c);
-    if (S.ninst) {
-        const float4 *F = S.inst + 6 * (size_t)__ldg(&S.light_inst[j]) + 3;
-        a = xf_point(F, a);
-        b = xf_point(F, b);
-        c = xf_point(F, c);
-    }
+    // the emitter entry's record: world-space corners, pdf, primitive, material, radiance
+    const float4 r0 = __ldg(&S.light_rec[4 * (size_t)j + 0]), r1 = __ldg(&S.light_rec[4 * (size_t)j + 1]);
+    const float4 r2 = __ldg(&S.light_rec[4 * (size_t)j + 2]), r3 = __ldg(&S.light_rec[4 * (size_t)j + 3]);
+    const v3 a = mk(r0.x, r0.y, r0.z), b = mk(r1.x, r1.y, r1.z), c = mk(r2.x, r2.y, r2.z);
+    const uint32_t prim = __float_as_uint(r1.w), lmi = __float_as_uint(r2.w);
     const float su = sqrtf(g.y);
     const float b0 = 1.0f - su, b1 = su * (1.0f - g.z), b2 = su * g.z;
     const v3 pl = add(add(mul(a, b0), mul(b, b1)), mul(c, b2));
@@ -553,18 +552,15 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
     const v3 Ngl = normalize(cross(sub(b, a), sub(c, a)));
     const float cos_l = absf(dot(Ngl, wi));
     if (!(cos_l > 0.0f)) return;
-    const crg_material &lm = S.mats[__ldg(&S.mat_idx[prim])];
-    float lc0 = lm.colour[0], lc1 = lm.colour[1], lc2 = lm.colour[2];
-    if (textured(S, lm)) {
+    v3 Le = mk(r3.x, r3.y, r3.z); // colour * emission
+    if (__float_as_uint(r3.w)) {   // textured emitter: texture colour at the sampled point * emission
+        const crg_material &lm = S.mats[lmi];
         float tu, tv;
         interp_uv(S, prim, b1, b2, tu, tv);
         const float4 t = tex_lookup(S, lm.tex, tu, tv);
-        lc0 = t.x;
-        lc1 = t.y;
-        lc2 = t.z;
+        Le = mk(t.x * lm.emission, t.y * lm.emission, t.z * lm.emission);
     }
-    const v3 Le = mk(lc0 * lm.emission, lc1 * lm.emission, lc2 * lm.emission);
-    const float p_light = (__ldg(&S.light_pdf[j]) * d2) / cos_l;
+    const float p_light = (r0.w * d2) / cos_l;
     v3 f;
     float p_bsdf, cos_i;
     if (bsdf == 0) {
@@ -590,7 +586,7 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
     }
     const float w_mis = (p_light * p_light) / (p_light * p_light + p_bsdf * p_bsdf);
     nr.bsdf_mat = mat;
-    nr.light_mat = __ldg(&S.mat_idx[prim]);
+    nr.light_mat = lmi;
     nr.kind = 1;
     nr.o = po;
     nr.d = wi;
