@@ -491,6 +491,9 @@ def main():
                          "graphs with conditional nodes)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch: use the autotuner's usual pick instead of running it (profiler runs)")
+    ap.add_argument("--spp-div", type=int, default=1,
+                    help="batch: divide every view's spp by this (a smaller copy of the batch for profiler captures; "
+                         "the JSON line then names the reduced samples per step)")
     ap.add_argument("--path-pool", type=int, default=0,
                     help="wavefront: paths in flight (0 = the autotuned or default pool); smaller pools keep "
                          "profiler captures within a few GB of device memory")
@@ -524,8 +527,9 @@ def main():
         sd = api.Scene(ctx, disp["verts"], disp["mat_idx"], disp["mats"]).build(8, 1)
         sd.set_skybox(disp["skybox"])
         vdefs = scenes.batch_views()
-        views = [(si, cam, api.make_settings(v["width"], v["height"], v["spp"], v["max_bounces"], 3, 1, 1 + i,
-                                             v["width"] / v["height"])) for i, (si, cam, v) in enumerate(vdefs)]
+        div = max(1, args.spp_div)
+        views = [(si, cam, api.make_settings(v["width"], v["height"], max(1, v["spp"] // div), v["max_bounces"], 3, 1,
+                                             1 + i, v["width"] / v["height"])) for i, (si, cam, v) in enumerate(vdefs)]
         films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
         units = sum(st.width * st.height * st.spp for _, _, st in views)
         out["scene_samples"] = {name: sum(st.width * st.height * st.spp for si, _, st in views if si == k)
@@ -785,6 +789,11 @@ def main():
         fuse = out.get("autotune", {}).get("opts", {}).get("fuse", 1) or 1
         launches = args.steps * (3 + (4 + (3, 2, 1)[fuse - 1]) * int(out["work"]["iterations"]))
     traffic, traffic_src = traffic_estimate(args.workload, out, units)
+    config = workload_config(args.workload)
+    if args.workload == "batch":
+        config["samples_per_step"] = units
+        if args.spp_div > 1:
+            config["spp_div"] = args.spp_div
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
@@ -793,7 +802,7 @@ def main():
         line = {
             "metric": unit, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(args.workload),
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "traffic_source": traffic_src, "kernel": kernel, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": int(algo)},
