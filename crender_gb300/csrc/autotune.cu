@@ -5,7 +5,7 @@
 // options), each scene's leaf size {1, 2, 3} (a large displaced mesh renders
 // ~9% faster with one triangle per leaf slot, the 36-triangle box ~8% slower),
 // stage fusion {split, shadow-in-shade, one kernel per bounce},
-// per-lane refill {off, 4, 16}, warp fetch {32, 64}, block size {128, 256}
+// per-lane refill {off, 4, 8, 16, 24}, warp fetch {32, 64}, block size {128, 256}
 // path pool {32M, 64M, 128M} (128M-sample chunks).  Each candidate renders a reduced copy of the
 // batch (spp scaled to a sample budget) into scratch films: one untimed run,
 // then one run timed with CUDA events on the caller's stream.
@@ -201,7 +201,7 @@ extern "C" crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nsce
         }
     };
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.fuse = v; }, {1u, 2u, 3u});
-    if (cur.fuse <= 2) sweep([](crg_wavefront_opts &c, uint32_t v) { c.refill = v; }, {kOff, 4u, 16u});
+    if (cur.fuse <= 2) sweep([](crg_wavefront_opts &c, uint32_t v) { c.refill = v; }, {kOff, 4u, 8u, 16u, 24u});
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.fetch = v; }, {32u, 64u});
     sweep([](crg_wavefront_opts &c, uint32_t v) { c.block_size = v; }, {128u, 256u});
     // Path pool, up to the 128M-sample chunk: on a GB300 the 64-view batch renders faster with more paths
