@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import wide_bvh
+from golden import make_golden
 from crender_gb300 import _abi, api, scenes
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.npz")
@@ -46,6 +47,17 @@ def test_golden_fixtures_reproduce(orc):
         f = orc.render(sc, sc["camera"], api.make_settings(16, 16, 4, 8, rr, mode, 42))
         assert np.array_equal(f["sum"].view(np.uint32), g[f"box16_mode{mode}_sum"].view(np.uint32))
         assert np.array_equal(f["sum64"].view(np.uint64), g[f"box16_mode{mode}_sum64"].view(np.uint64))
+    tx, inst = scenes.textured_box(), scenes.instanced_box()
+    for mode in (0, 1):
+        st = api.make_settings(16, 12, 4, 8, 3, mode, 43, 16 / 12)
+        for name, s in (("textured16", tx), ("instanced16", inst)):
+            f = orc.render(s, s["camera"], st)
+            assert np.array_equal(f["sum"].view(np.uint32), g[f"{name}_mode{mode}_sum"].view(np.uint32)), name
+    d = orc.draft_render(tx, tx["camera"], 24, 16, 1.5)
+    assert np.array_equal(d.view(np.uint32), g["draft_textured_24x16"].view(np.uint32))
+    for name, kw in make_golden.POST_CASES.items():
+        p = orc.post_process(g["post_input"], api.post_settings(**kw))
+        assert np.array_equal(p.view(np.uint32), g[f"post_{name}"].view(np.uint32)), name
 
 
 def test_sincos2pi_accuracy(orc):
