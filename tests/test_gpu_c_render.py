@@ -128,3 +128,30 @@ def test_faithful_and_extended_agree_in_expectation(ctx):
     z = (m0 - m1) / np.sqrt(v0 + v1 + 1e-30)
     assert np.mean(np.abs(z) > 3) < 0.02
     assert abs(m0.mean() - m1.mean()) < 3 * np.sqrt(v0.sum() + v1.sum()) / m0.size + 1e-3 * m0.mean()
+
+
+@pytest.mark.parametrize("mode,rr", [(0, 0), (1, 3)])
+def test_reference_image_against_independent_cpu_render(ctx, orc, mode, rr):
+    """The FP64 16384-spp GPU image (the kind the time-to-RMSE measurement uses
+    as ground truth) against an independent CPU render of the same pixels: other
+    seed, 1024 spp, FP64 sums.  Per-pixel means agree within 3 standard errors
+    (combined) for all but the normal tail, so the GPU image is never validated
+    only against itself."""
+    sc = scenes.box_scene()
+    W, H = 16, 12
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    f = api.Film(ctx, W, H, f64=True)
+    api.render(s, sc["camera"], api.make_settings(W, H, 16384, 8, rr, mode, 900 + mode, W / H), f)
+    g = f.download(f64=True)
+    ng = f.spp
+    f.close()
+    s.close()
+    o = orc.render(sc, sc["camera"], api.make_settings(W, H, 1024, 8, rr, mode, 77 + mode, W / H))
+    no = o["spp"]
+    mg, mo = g["sum64"] / ng, o["sum64"] / no
+    vg = (g["sumsq64"] / ng - mg * mg) / (ng - 1)
+    vo = (o["sumsq64"] / no - mo * mo) / (no - 1)
+    z = (mg - mo) / np.sqrt(vg + vo + 1e-30)
+    assert mg.sum() > 0
+    assert np.mean(np.abs(z) > 3) <= 0.02
+    assert abs(mg.mean() - mo.mean()) < 4 * np.sqrt(vg.sum() + vo.sum()) / mg.size
