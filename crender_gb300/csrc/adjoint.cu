@@ -153,18 +153,22 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
         tape.dy = (double)adj[fidx * 3 + 1] * inv;
         tape.dz = (double)adj[fidx * 3 + 2] * inv;
         const bool live = tape.dx != 0.0 || tape.dy != 0.0 || tape.dz != 0.0;
-        for (uint32_t s = 0; live && s < set.spp; ++s) {
-            C.sample = s;
-            const f4 g0 = rand4(pix, s, 0, set.seed);
-            const float x = ((float)px + g0.x) / (float)Wd;
-            const float y = ((float)py + g0.y) / (float)Hd;
-            v3 o, d;
-            camera_ray(cam, x, y, set.aspect, o, d);
-            PathState ps;
-            path_start(ps, o, d);
-            Aov aov;
-            tape.begin();
-            for (uint32_t i = 0; i < set.max_bounces; ++i) {
+        // one loop over segments with path regeneration, as in the forward megakernel
+        PathState ps;
+        Aov aov;
+        uint32_t s = 0, i = 0;
+        while (live && s < set.spp) {
+            if (i == 0) {
+                C.sample = s;
+                const f4 g0 = rand4(pix, s, 0, set.seed);
+                const float x = ((float)px + g0.x) / (float)Wd;
+                const float y = ((float)py + g0.y) / (float)Hd;
+                v3 o, d;
+                camera_ray(cam, x, y, set.aspect, o, d);
+                path_start(ps, o, d);
+                tape.begin();
+            }
+            if (i < set.max_bounces) {
                 Hit h;
                 const bool found = closest<W, false>(S, ps.o, ps.d, INFINITY, h, C);
                 NeeReq nr;
@@ -174,9 +178,12 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
                     ps.L = add(ps.L, nr.c);
                     tape.nee(nr, nf);
                 }
-                if (!cont) break;
+                ++i;
+                if (cont && i < set.max_bounces) continue;
             }
             tape.end();
+            ++s;
+            i = 0;
         }
         tape.flush_emitter();
     }

@@ -67,19 +67,27 @@ __global__ void __launch_bounds__(128, 4) k_render(SceneDev S, CamDev cam, crg_s
             q64[0] = F.sumsq64[fidx * 3]; q64[1] = F.sumsq64[fidx * 3 + 1]; q64[2] = F.sumsq64[fidx * 3 + 2];
         }
         Aov aov;
-        for (uint32_t s = 0; s < set.spp; ++s) {
-            C.sample = (uint32_t)(spp0 + s);
-            const f4 g0 = rand4(pix, C.sample, 0, set.seed);
-            const float x = ((float)px + g0.x) / (float)Wd;
-            const float y = ((float)py + g0.y) / (float)Hd;
-            v3 o, d;
-            camera_ray(cam, x, y, set.aspect, o, d);
-            aov.albedo = mk(0, 0, 0);
-            aov.normal = mk(0, 0, 0);
-            aov.depth = 0.0f;
-            PathState ps;
-            path_start(ps, o, d);
-            for (uint32_t i = 0; i < set.max_bounces; ++i) {
+        PathState ps;
+        // Path regeneration (Novak, Havran and Dachsbacher 2010): one loop over
+        // segments, in which a lane whose path has ended starts its pixel's next
+        // sample, so a warp runs for the largest total segment count of its lanes
+        // instead of the longest path of every sample.  A pixel's samples still run
+        // and accumulate in order, so the film is unchanged.
+        uint32_t s = 0, i = 0;
+        while (s < set.spp) {
+            if (i == 0) {
+                C.sample = (uint32_t)(spp0 + s);
+                const f4 g0 = rand4(pix, C.sample, 0, set.seed);
+                const float x = ((float)px + g0.x) / (float)Wd;
+                const float y = ((float)py + g0.y) / (float)Hd;
+                v3 o, d;
+                camera_ray(cam, x, y, set.aspect, o, d);
+                aov.albedo = mk(0, 0, 0);
+                aov.normal = mk(0, 0, 0);
+                aov.depth = 0.0f;
+                path_start(ps, o, d);
+            }
+            if (i < set.max_bounces) {
                 Hit h;
                 C.segments++;
                 const bool found = closest<W, CNT>(S, ps.o, ps.d, INFINITY, h, C);
@@ -87,8 +95,11 @@ __global__ void __launch_bounds__(128, 4) k_render(SceneDev S, CamDev cam, crg_s
                 const bool cont = MODE == CRG_MODE_EXTENDED ? shade_extended(S, set, C, i, ps, found, h, aov, nr)
                                                             : shade_faithful(S, set, C, i, ps, found, h, aov, nr);
                 if (nr.kind != 0 && shadow_visible<W, CNT>(S, nr, C)) ps.L = add(ps.L, nr.c);
-                if (!cont) break;
+                ++i;
+                if (cont && i < set.max_bounces) continue;
             }
+            ++s;
+            i = 0;
             const v3 L = ps.L;
             acc[0] += L.x;
             acc[1] += L.y;
