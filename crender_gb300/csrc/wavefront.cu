@@ -776,7 +776,10 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
         V.sumsq64 = (double *)films[v]->sumsq64.ptr;
         total += (unsigned long long)V.npix * V.set.spp;
     }
-    if (total == 0) return CRG_OK;
+    if (total == 0) { // nothing to trace: films and their sample counts stay as they are
+        if (stats) *stats = crg_render_stats{};
+        return CRG_OK;
+    }
     const unsigned long long C = o.chunk_samples;
     std::vector<Segment> segs;
     std::vector<Chunk> chunks;

@@ -136,9 +136,11 @@ def render(scene: dict, camera: dict, settings: _abi.Settings, film: dict | None
 
     W, H = settings.width, settings.height
     if film is None:
+        # AOV images start at FLT_MAX, cr::image's clear value (src/objects/image.h:30-33), as the library's films do
+        big = np.finfo(np.float32).max
         film = dict(sum=np.zeros(W * H * 3, np.float32), sum64=np.zeros(W * H * 3), sumsq64=np.zeros(W * H * 3),
-                    albedo=np.zeros(W * H * 4, np.float32), normal=np.zeros(W * H * 4, np.float32),
-                    depth=np.zeros(W * H * 4, np.float32), spp=0, segments=0, shadow_rays=0)
+                    albedo=np.full(W * H * 4, big, np.float32), normal=np.full(W * H * 4, big, np.float32),
+                    depth=np.full(W * H * 4, big, np.float32), spp=0, segments=0, shadow_rays=0)
     d, keep = scene_desc(scene, **kw)
     f = _abi.OrcFilm()
     f.width, f.height = W, H

@@ -155,3 +155,25 @@ def test_reference_image_against_independent_cpu_render(ctx, orc, mode, rr):
     assert mg.sum() > 0
     assert np.mean(np.abs(z) > 3) <= 0.02
     assert abs(mg.mean() - mo.mean()) < 4 * np.sqrt(vg.sum() + vo.sum()) / mg.size
+
+
+@pytest.mark.parametrize("spp,max_bounces", [(4, 0), (3, 1), (0, 8), (5, 2)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_edge_settings(ctx, orc, spp, max_bounces, mode):
+    """Zero segments (every sample adds zero radiance and resets the AOVs), one
+    segment, zero samples (films untouched, AOVs keep the image clear value)
+    and two segments: the megakernel against the oracle, and the wavefront
+    form's sums (it writes no AOVs) against the same oracle film."""
+    sc = _box_variant("materials")
+    st = api.make_settings(12, 10, spp, max_bounces, 0, mode, 7, 1.2)
+    g, o = _render_both(ctx, orc, sc, st)
+    _assert_identical(g, o)
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build()
+    f = api.Film(ctx, 12, 10, f64=True, aov=True)
+    ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f]))
+    w = f.download(f64=True)
+    assert f.spp == o["spp"]
+    f.close()
+    s.close()
+    for k in ("sum", "sum64", "sumsq64"):
+        assert np.array_equal(w[k].view(np.uint8), o[k].view(np.uint8)), k
