@@ -53,7 +53,7 @@ using namespace rc;
 namespace {
 
 template <int W, int MODE, bool CNT>
-__global__ void __launch_bounds__(128, 4) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
+__global__ void __launch_bounds__(128, 5) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
     PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
