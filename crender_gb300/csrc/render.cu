@@ -52,8 +52,11 @@ using namespace rc;
 
 namespace {
 
-template <int W, int MODE, bool CNT>
-__global__ void __launch_bounds__(128, 5) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
+// MINB blocks of 128 threads per SM: 5 (96 registers, some spilled) when the grid fills the
+// GPU at that occupancy, else 4 (no spills: a grid below one wave gains nothing from the
+// extra warps and loses the spill traffic).
+template <int W, int MODE, bool CNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
     PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
@@ -145,19 +148,26 @@ __global__ void __launch_bounds__(128, 5) k_render(SceneDev S, CamDev cam, crg_s
     }
 }
 
+template <int W, int MINB>
+void launch_m(const SceneDev &S, const CamDev &cam, const crg_settings &set, const FilmDev &F, uint64_t spp0,
+              uint32_t blocks, cudaStream_t st) {
+    const uint32_t T = 128;
+    if (S.counters) {
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, true, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, true, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+    } else {
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, false, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, false, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+    }
+}
+
 template <int W>
 void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, const FilmDev &F, uint64_t spp0,
-              cudaStream_t st) {
-    const uint32_t T = 128;
+              int sm_count, cudaStream_t st) {
     const uint64_t npix = (uint64_t)set.width * set.height;
-    const uint32_t blocks = (uint32_t)((npix + T - 1) / T);
-    if (S.counters) {
-        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, true><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-        else k_render<W, CRG_MODE_FAITHFUL, true><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-    } else {
-        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, false><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-        else k_render<W, CRG_MODE_FAITHFUL, false><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-    }
+    const uint32_t blocks = (uint32_t)((npix + 127) / 128);
+    if ((uint64_t)blocks >= 5ull * (uint64_t)(sm_count > 0 ? sm_count : 1)) launch_m<W, 5>(S, cam, set, F, spp0, blocks, st);
+    else launch_m<W, 4>(S, cam, set, F, spp0, blocks, st);
 }
 
 } // namespace
@@ -255,9 +265,9 @@ crg_status launch_render(crg_scene *s, const CamDev &cam, const crg_settings &se
               film->height};
     if (s->ntri == 0) return set_error(s->ctx, CRG_ERR_INVALID_ARG, "crg_render: scene has no triangles");
     switch (s->width) {
-    case 2: launch_w<2>(S, cam, set, F, film->spp, st); break;
-    case 4: launch_w<4>(S, cam, set, F, film->spp, st); break;
-    default: launch_w<8>(S, cam, set, F, film->spp, st); break;
+    case 2: launch_w<2>(S, cam, set, F, film->spp, s->ctx->sm_count, st); break;
+    case 4: launch_w<4>(S, cam, set, F, film->spp, s->ctx->sm_count, st); break;
+    default: launch_w<8>(S, cam, set, F, film->spp, s->ctx->sm_count, st); break;
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(s->ctx, e, "k_render launch");
