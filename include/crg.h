@@ -35,7 +35,7 @@ typedef enum crg_status {
     CRG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
     CRG_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
     CRG_ERR_NOT_BUILT = 5,   /* query on a scene whose BVH is not built */
-    CRG_ERR_UNSUPPORTED = 6, /* option not available in this build */
+    CRG_ERR_UNSUPPORTED = 6, /* valid request the call does not support (e.g. the adjoint of a textured scene) */
     CRG_ERR_DEVICE = 7       /* a kernel reported an internal error word */
 } crg_status;
 
