@@ -181,11 +181,25 @@ def workload_config(w):
 
 
 # ---------------------------------------------------------------- CPU oracle leg
-def cpu_render(scene, camera, st, rows, skybox=None):
+def cpu_render(scene, camera, st, rows, skybox=None, nthreads=0):
     from oracle import orc
 
-    f = orc.render(scene, camera, st, rows=rows, skybox=skybox)
+    f = orc.render(scene, camera, st, nthreads=nthreads, rows=rows, skybox=skybox)
     return (rows[1] - rows[0]) * st.width * st.spp, f["render_seconds"]
+
+
+def cpu_reference_threads(workload):
+    """The box frame on the reference's default thread count, a quarter of the
+    hardware threads (src/main.cpp:5-6), beside the all-core figure."""
+    if workload not in ("box", "batch"):
+        return None
+    from crender_gb300 import api, scenes
+
+    threads = max(1, (os.cpu_count() or 1) // 4)
+    sc = scenes.box_scene()
+    n, dt = cpu_render(sc, sc["camera"], api.make_settings(**BOX), (0, 512), nthreads=threads)
+    return {"threads": threads, "value": n / dt / 1e6,
+            "sample": f"box full frame 512x512x64 ({n} samples, {dt:.1f} s)"}
 
 
 def cpu_cores(workload):
@@ -253,11 +267,15 @@ def run_reference(args):
             vals.append(v)
     value = statistics.median(vals)
     unit = {"soup": "Mrays/s", "post": "Mpixels/s"}.get(args.workload, "Msamples/s")
+    cpu = {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample}
+    quarter = cpu_reference_threads(args.workload)
+    if quarter:
+        cpu["reference_default_threads"] = quarter
     print(json.dumps({
         "impl": "reference", "metric": unit, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": workload_config(args.workload),
-        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU oracle: C++ restatement of CRender's estimator with an LBVH + watertight traversal standing in "
                 "for Embree 3, which cannot be built here; std::thread over all host cores",
@@ -798,6 +816,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, sample = cpu_leg(args.workload)
         cpu = {"value": cv, "unit": unit, "cores": cpu_cores(args.workload), "kind": "port", "sample": sample}
+        quarter = cpu_reference_threads(args.workload)
+        if quarter:
+            cpu["reference_default_threads"] = quarter
     if rank == 0:
         line = {
             "metric": unit, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
