@@ -18,7 +18,10 @@
 namespace crg {
 
 crg_status set_error(crg_context *ctx, crg_status s, const std::string &msg) {
-    if (ctx) ctx->last_error = msg;
+    if (ctx) {
+        std::lock_guard<std::mutex> lock(ctx->error_mutex);
+        ctx->last_error = msg;
+    }
     return s;
 }
 
@@ -392,7 +395,14 @@ crg_status crg_context_destroy(crg_context *ctx) {
     return CRG_OK;
 }
 
-const char *crg_last_error_string(const crg_context *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+const char *crg_last_error_string(const crg_context *ctx) {
+    if (!ctx) return "null context";
+    // a copy per calling thread: the context's message may be replaced by another thread's error
+    thread_local std::string copy;
+    std::lock_guard<std::mutex> lock(ctx->error_mutex);
+    copy = ctx->last_error;
+    return copy.c_str();
+}
 
 crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr) {
     if (!ctx || !dptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");

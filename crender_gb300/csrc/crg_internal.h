@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -17,7 +18,8 @@ struct DevBuf {
 
 struct crg_context {
     int device = 0;
-    std::string last_error;
+    std::string last_error;     // guarded by error_mutex: concurrent queries may fail at once
+    mutable std::mutex error_mutex;
     int sm_count = 0;
     DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
     DevBuf post_ws; // post-process ping-pong images, grow-only

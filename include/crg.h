@@ -142,7 +142,8 @@ typedef struct crg_film crg_film;
  * src/objects/thread_pool.cpp:3-24 is replaced by kernel launches). */
 crg_status crg_context_create(int device, crg_context **out);
 crg_status crg_context_destroy(crg_context *ctx);
-/* Last error message of this context (never NULL). */
+/* Last error message of this context (never NULL): a copy owned by the calling
+ * thread, valid until that thread calls crg_last_error_string again. */
 const char *crg_last_error_string(const crg_context *ctx);
 const char *crg_status_string(crg_status s);
 uint32_t crg_abi_version(void);
