@@ -779,6 +779,17 @@ def main():
             ms = timer.steps(step, args.steps, args.warmup)
         kernel = "k_intersect<8> (closest hit)"
         launches = args.steps
+        # any-hit leg: 16,777,216 shadow rays of the same generator (separate seed, tmax ~ U[0.1, 1])
+        sb = api.DeviceBuffer.from_array(ctx, scenes.soup_rays(n, 3, shadow=True))
+        ob = api.DeviceBuffer(ctx, 4 * n)
+        ms_any = timer.steps(lambda: ctx.check(lib.crg_intersect_any(scene.h, sb.ptr, ob.ptr, n, S)),
+                             args.steps, args.warmup)
+        occluded = int(ob.download(np.zeros(n, np.uint32)).astype(bool).sum())
+        out["any_hit"] = {"value": n / (sum(ms_any) / len(ms_any) / 1e3) / 1e6, "unit": "Mrays/s",
+                          "ms_per_step": sum(ms_any) / len(ms_any), "rays": n, "occluded_fraction": occluded / n,
+                          "kernel": "k_intersect_dyn<8> (any hit, per-lane refill)"}
+        sb.free()
+        ob.free()
         pr = api.PinnedArray(ctx, rays_h.shape, rays_h.dtype)
         pr.array[...] = rays_h
         ph = api.PinnedArray(ctx, (n * 16,), np.uint8)
