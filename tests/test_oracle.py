@@ -239,3 +239,52 @@ def test_alias_table_selects_in_proportion_to_power(orc):
         np.add.at(p, alias, (1.0 - prob.astype(np.float64)) / n)
         assert np.allclose(p, w / w.sum(), rtol=1e-5, atol=1e-12)
         assert np.all((prob >= 0) & (prob <= 1)) and np.all(alias < n)
+
+
+def _camera_f64(cam, x, y, aspect):
+    """FP64 restatement of cr::camera::get_ray and _update_cache
+    (src/render/camera.cpp:14-39, 54-68): M = T(position) Ry(rot.x) Rx(rot.y)
+    Rz(rot.z) (glm::rotate multiplies on the right); perspective rays leave the
+    position along normalize(M (u, v, 1/tan(fov/2), 0)); orthographic rays leave
+    M (s u, s v, 0, 1) along M's third column."""
+    ax, ay, az = np.radians(np.asarray(cam["rotation"], np.float64))
+    Ry = np.array([[np.cos(ax), 0, np.sin(ax)], [0, 1, 0], [-np.sin(ax), 0, np.cos(ax)]])
+    Rx = np.array([[1, 0, 0], [0, np.cos(ay), -np.sin(ay)], [0, np.sin(ay), np.cos(ay)]])
+    Rz = np.array([[np.cos(az), -np.sin(az), 0], [np.sin(az), np.cos(az), 0], [0, 0, 1]])
+    M = Ry @ Rx @ Rz
+    pos = np.asarray(cam["position"], np.float64)
+    if cam.get("mode", 0) == 1:
+        s = cam.get("scale", 1.0)
+        o = pos + M @ np.array([s * (2 * x - 1), s * (2 * y - 1), 0.0])
+        d = M[:, 2]
+    else:
+        w = 1.0 / np.tan(0.5 * np.radians(cam["fov"]))
+        o = pos
+        d = M @ np.array([(2 * x - 1) * aspect, 2 * y - 1, w])
+    return o, d / np.linalg.norm(d)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_camera_rays_match_restatement(orc, mode):
+    """The oracle's camera (basis formed in double, rounded once) against the
+    FP64 restatement, for random poses, fields of view, aspects and jitters."""
+    r = np.random.default_rng(5 + mode)
+    o, d = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    for _ in range(200):
+        cam = dict(position=tuple(r.uniform(-5, 5, 3)),
+                   rotation=(r.uniform(-180, 180), r.uniform(-90, 90), r.uniform(-180, 180)),
+                   fov=float(r.uniform(20, 120)), mode=mode, scale=float(r.uniform(0.2, 3)))
+        W, H = int(r.integers(1, 2000)), int(r.integers(1, 2000))
+        aspect = float(r.uniform(0.5, 2.0))
+        st = api.make_settings(W, H, 1, aspect=aspect)
+        px, py = int(r.integers(0, W)), int(r.integers(0, H))
+        jx, jy = np.float32(r.random()), np.float32(r.random())
+        orc.lib().orc_camera_ray(C.byref(api.make_camera(cam)), C.byref(st), px, py, float(jx), float(jy),
+                                 o.ctypes.data, d.ctypes.data)
+        x = float(np.float32(np.float32(px) + jx) / np.float32(W))
+        y = float(np.float32(np.float32(py) + jy) / np.float32(H))
+        o64, d64 = _camera_f64(cam, x, y, float(np.float32(aspect)))
+        pos = np.asarray(cam["position"], np.float32).astype(np.float64)
+        assert np.allclose(o, o64, rtol=0, atol=4e-6 * (1 + np.abs(pos).max() + 3 * cam["scale"]))
+        assert np.allclose(d, d64, rtol=0, atol=2e-6)
+        assert abs(np.linalg.norm(d.astype(np.float64)) - 1) < 1e-6
