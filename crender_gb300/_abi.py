@@ -267,6 +267,12 @@ ORC_SIGNATURES = [
     ("orc_sincos2pi", None, [C.c_float, P(C.c_float), P(C.c_float)]),
     ("orc_rand4", None, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     ("orc_morton3", C.c_uint32, [C.c_float, C.c_float, C.c_float]),
+    ("orc_sample_sphere", None, [C.c_float, C.c_float, vp]),
+    ("orc_build_local", None, [vp, vp, vp]),
+    ("orc_ggx_d", C.c_float, [C.c_float, C.c_float]),
+    ("orc_ggx_lambda", C.c_float, [vp, C.c_float]),
+    ("orc_sample_vndf", None, [vp, C.c_float, C.c_float, C.c_float, vp]),
+    ("orc_fresnel_dielectric", C.c_float, [C.c_float, C.c_float]),
 ]
 
 

@@ -125,6 +125,16 @@ void orc_camera_ray(const crg_camera *cam, const crg_settings *set, uint32_t px,
 void orc_sincos2pi(float u, float *s, float *c);
 void orc_rand4(uint32_t pixel, uint32_t sample, uint32_t group, uint32_t seed, float *out4);
 uint32_t orc_morton3(float x, float y, float z); /* x,y,z already in [0,1024) */
+/* Sampling helpers of the estimators (for distribution tests): uniform sphere
+ * (sampling.h:156-166), orthonormal frame around a unit normal (sampling.h:21-33),
+ * GGX D and Smith Lambda in the local frame (sampling.h:93-140), visible-normal
+ * sampling (Heitz 2018), exact unpolarised dielectric Fresnel (eta = n_i / n_t). */
+void orc_sample_sphere(float u1, float u2, float *out3);
+void orc_build_local(const float *n3, float *t3, float *b3);
+float orc_ggx_d(float nh, float alpha);
+float orc_ggx_lambda(const float *w3, float alpha);
+void orc_sample_vndf(const float *wo3, float alpha, float u1, float u2, float *h3);
+float orc_fresnel_dielectric(float ci, float eta);
 
 #ifdef __cplusplus
 }

@@ -1145,4 +1145,25 @@ int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit
     return CRG_OK;
 }
 
+/* Sampling helpers exported for known-answer and distribution tests. */
+void orc_sample_sphere(float u1, float u2, float *out3) {
+    const v3 v = sphere(u1, u2);
+    out3[0] = v.x; out3[1] = v.y; out3[2] = v.z;
+}
+void orc_build_local(const float *n3, float *t3, float *b3) {
+    const onb F = build_local(mk(n3[0], n3[1], n3[2]));
+    t3[0] = F.t.x; t3[1] = F.t.y; t3[2] = F.t.z;
+    b3[0] = F.b.x; b3[1] = F.b.y; b3[2] = F.b.z;
+}
+float orc_ggx_d(float nh, float alpha) { return ggx_D(nh, alpha); }
+float orc_ggx_lambda(const float *w3, float alpha) { return ggx_lambda(mk(w3[0], w3[1], w3[2]), alpha); }
+void orc_sample_vndf(const float *wo3, float alpha, float u1, float u2, float *h3) {
+    const v3 h = sample_vndf(mk(wo3[0], wo3[1], wo3[2]), alpha, u1, u2);
+    h3[0] = h.x; h3[1] = h.y; h3[2] = h.z;
+}
+float orc_fresnel_dielectric(float ci, float eta) {
+    float st2;
+    return fresnel_dielectric(ci, eta, &st2);
+}
+
 } /* extern "C" */
