@@ -855,6 +855,7 @@ crg_status crg_draft_render(crg_scene *scene, const crg_camera *camera, uint32_t
 crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_settings *settings, crg_film *film, crg_stream stream) {
     if (!scene || !camera || !settings || !film) return set_error(scene ? scene->ctx : nullptr, CRG_ERR_INVALID_ARG, "null argument");
     crg_context *ctx = scene->ctx;
+    if (film->ctx != ctx) return set_error(ctx, CRG_ERR_INVALID_ARG, "film and scene belong to different contexts");
     if (!scene->built) return set_error(ctx, CRG_ERR_NOT_BUILT, "scene not built");
     const crg_settings &s = *settings;
     if (s.width != film->width || s.height != film->height) return set_error(ctx, CRG_ERR_INVALID_ARG, "settings resolution differs from the film");
