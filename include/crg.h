@@ -148,7 +148,8 @@ const char *crg_last_error_string(const crg_context *ctx);
 const char *crg_status_string(crg_status s);
 uint32_t crg_abi_version(void);
 
-/* Device memory helpers for callers without their own allocator. */
+/* Device memory helpers for callers without their own allocator (no reference
+ * counterpart: the reference keeps everything in host memory). */
 crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr);
 crg_status crg_device_free(crg_context *ctx, void *dptr);
 crg_status crg_memcpy_h2d(crg_context *ctx, void *dst, const void *src, size_t bytes, crg_stream stream);
@@ -496,7 +497,8 @@ typedef struct crg_autotune_trial {
     uint32_t pad_;
 } crg_autotune_trial;
 
-/* Writes the best options to *best and the BVH width to *best_width (scenes
+/* No reference counterpart (the reference has no tunable launch shape).
+ * Writes the best options to *best and the BVH width to *best_width (scenes
  * are left built at it); up to trials_cap trials to `trials` (may be NULL)
  * and their count to *ntrials (may be NULL; 0 when the cache answered). */
 crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, uint32_t nviews,
@@ -507,7 +509,9 @@ crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nscenes, const 
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replaces the material table (same count, e.g. after an optimiser step)
- * without rebuilding the BVH; the emitter table is rebuilt. */
+ * without rebuilding the BVH; the emitter table is rebuilt.  The reference
+ * edits cr::material::information in place while the renderer is paused
+ * (src/render/material/material.h:31-41, renderer.cpp:185-192). */
 crg_status crg_scene_set_materials(crg_scene *scene, const crg_material *mats, uint32_t nmat);
 
 /* Backward half of a forward/backward pair whose forward half is crg_render
