@@ -80,6 +80,19 @@ class BvhInfo(C.Structure):
     ]
 
 
+class ModelInfo(C.Structure):
+    _fields_ = [
+        ("first_prim", C.c_uint32),
+        ("ntri", C.c_uint32),
+        ("node_base", C.c_uint32),
+        ("n_wide_nodes", C.c_uint32),
+        ("depth", C.c_uint32),
+        ("ninst", C.c_uint32),
+        ("built", C.c_uint32),
+        ("sah_cost", C.c_float),
+    ]
+
+
 class View(C.Structure):
     _fields_ = [("scene", C.c_uint32), ("pad_", C.c_uint32), ("camera", Camera), ("settings", Settings)]
 
@@ -158,6 +171,8 @@ CRG_SIGNATURES = [
     ("crg_last_error_string", C.c_char_p, [vp]),
     ("crg_status_string", C.c_char_p, [C.c_int]),
     ("crg_abi_version", C.c_uint32, []),
+    ("crg_debug_fail_allocation", C.c_int, [C.c_int64]),
+    ("crg_debug_allocation_stats", C.c_int, [P(C.c_uint64), P(C.c_uint32), P(C.c_int64)]),
     ("crg_device_alloc", C.c_int, [vp, C.c_size_t, P(vp)]),
     ("crg_device_free", C.c_int, [vp, vp]),
     ("crg_memcpy_h2d", C.c_int, [vp, vp, vp, C.c_size_t, c_stream]),
@@ -175,9 +190,16 @@ CRG_SIGNATURES = [
     ("crg_scene_set_sun", C.c_int, [vp, C.c_int, P(Sun)]),
     ("crg_scene_set_textures", C.c_int, [vp, C.c_uint32, P(vp), vp, vp]),
     ("crg_scene_set_instances", C.c_int, [vp, vp, C.c_uint32]),
+    ("crg_scene_add_model", C.c_int, [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, P(C.c_uint32)]),
+    ("crg_scene_add_model_indexed", C.c_int, [vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp,
+                                              C.c_uint32, P(C.c_uint32)]),
+    ("crg_scene_set_model_instances", C.c_int, [vp, C.c_uint32, vp, C.c_uint32]),
+    ("crg_scene_model_count", C.c_int, [vp, P(C.c_uint32)]),
+    ("crg_scene_model_info", C.c_int, [vp, C.c_uint32, P(ModelInfo)]),
     ("crg_scene_bvh_info", C.c_int, [vp, P(BvhInfo)]),
     ("crg_scene_bvh_download", C.c_int, [vp, vp, vp, vp, vp]),
     ("crg_build_bvh_noalloc", C.c_int, [vp, C.c_uint32, P(BuildOpts), vp, C.c_size_t, vp, vp, P(BvhInfo), c_stream]),
+    ("crg_noalloc_last_error", C.c_char_p, []),
     ("crg_intersect_closest", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_any", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_closest_counted", C.c_int, [vp, vp, vp, vp, vp, C.c_uint64, c_stream]),
@@ -227,6 +249,9 @@ class OrcSceneDesc(C.Structure):
         ("tex_h", vp),
         ("xforms", vp),
         ("ninst", C.c_uint32),
+        ("nmodels", C.c_uint32),
+        ("model_ntri", vp),
+        ("model_ninst", vp),
     ]
 
 
@@ -273,6 +298,9 @@ ORC_SIGNATURES = [
     ("orc_ggx_lambda", C.c_float, [vp, C.c_float]),
     ("orc_sample_vndf", None, [vp, C.c_float, C.c_float, C.c_float, vp]),
     ("orc_fresnel_dielectric", C.c_float, [C.c_float, C.c_float]),
+    ("orc_sun_sample", None, [P(Sun), vp, C.c_float, C.c_float, vp, vp, vp]),
+    ("orc_sun_visible", C.c_int, [P(Sun), vp]),
+    ("orc_cos_hemp", None, [C.c_float, C.c_float, vp]),
 ]
 
 

@@ -164,6 +164,68 @@ class Scene:
         x = np.ascontiguousarray(np.transpose(np.asarray(xforms, np.float32), (0, 2, 1)))
         self.ctx.check(self.ctx.lib.crg_scene_set_instances(self.h, ptr(x), len(x)))
 
+    def add_model(self, verts, mat_idx, mats, uvs=None) -> int:
+        """crg_scene_add_model: appends a model (its own BVH and instance list); mat_idx
+        indexes its own mats.  Returns the model's index."""
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+        mi = np.ascontiguousarray(mat_idx, np.uint32)
+        mt = np.ascontiguousarray(mats)
+        uv = None if uvs is None else np.ascontiguousarray(uvs, np.float32).reshape(-1, 6)
+        m = C.c_uint32()
+        self.ctx.check(self.ctx.lib.crg_scene_add_model(self.h, ptr(v), len(v), ptr(uv), ptr(mi), ptr(mt), len(mt),
+                                                        C.byref(m)))
+        self.ntri += len(v)
+        return m.value
+
+    def add_model_indexed(self, positions, vertex_indices, mat_idx, mats, texcoords=None, tex_indices=None) -> int:
+        """crg_scene_add_model_indexed: as from_indexed, for an appended model."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(vertex_indices, np.uint32).reshape(-1, 3)
+        mi = np.ascontiguousarray(mat_idx, np.uint32)
+        mt = np.ascontiguousarray(mats)
+        tc = None if texcoords is None else np.ascontiguousarray(texcoords, np.float32).reshape(-1, 2)
+        ti = None if tex_indices is None else np.ascontiguousarray(tex_indices, np.int32).reshape(-1, 3)
+        m = C.c_uint32()
+        self.ctx.check(self.ctx.lib.crg_scene_add_model_indexed(self.h, ptr(pos), len(pos), ptr(idx), len(idx), ptr(tc),
+                                                                0 if tc is None else len(tc), ptr(ti), ptr(mi), ptr(mt),
+                                                                len(mt), C.byref(m)))
+        self.ntri += len(idx)
+        return m.value
+
+    def set_model_instances(self, model: int, xforms):
+        """crg_scene_set_model_instances: one model's [n, 4, 4] row-major transforms
+        (None or empty = one identity instance)."""
+        if xforms is None or len(xforms) == 0:
+            self.ctx.check(self.ctx.lib.crg_scene_set_model_instances(self.h, model, None, 0))
+            return
+        x = np.ascontiguousarray(np.transpose(np.asarray(xforms, np.float32), (0, 2, 1)))
+        self.ctx.check(self.ctx.lib.crg_scene_set_model_instances(self.h, model, ptr(x), len(x)))
+
+    def model_count(self) -> int:
+        n = C.c_uint32()
+        self.ctx.check(self.ctx.lib.crg_scene_model_count(self.h, C.byref(n)))
+        return n.value
+
+    def model_info(self, model: int) -> dict:
+        i = _abi.ModelInfo()
+        self.ctx.check(self.ctx.lib.crg_scene_model_info(self.h, model, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    @classmethod
+    def from_models(cls, ctx: Context, scene: dict):
+        """A scene of several models from a dict made by scenes.merge_models: model 0
+        by crg_scene_create, the others by crg_scene_add_model, then each model's
+        instance list."""
+        ms = scene["models"]
+        uv0 = ms[0].get("uvs")
+        self = cls(ctx, ms[0]["verts"], ms[0]["mat_idx"], ms[0]["mats"], uvs=uv0)
+        for m in ms[1:]:
+            self.add_model(m["verts"], m["mat_idx"], m["mats"], uvs=m.get("uvs"))
+        for k, m in enumerate(ms):
+            if m.get("instances") is not None and len(m["instances"]):
+                self.set_model_instances(k, m["instances"])
+        return self
+
     def set_textures(self, textures):
         """crg_scene_set_textures: a list of RGBA32F [h, w, 4] arrays (empty list removes them)."""
         texs = [np.ascontiguousarray(t, np.float32) for t in textures]

@@ -123,7 +123,7 @@ struct GradTape {
     }
 };
 
-template <int W>
+template <int W, bool INST>
 __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_settings set, const float *__restrict__ adj,
                                                  double *__restrict__ g_col, double *__restrict__ g_em, uint32_t nmat,
                                                  uint32_t copies) {
@@ -170,11 +170,11 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
             }
             if (i < set.max_bounces) {
                 Hit h;
-                const bool found = closest<W, false>(S, ps.o, ps.d, INFINITY, h, C);
+                const bool found = closest<W, false, INST>(S, ps.o, ps.d, INFINITY, h, C);
                 NeeReq nr;
                 const uint32_t nf = tape.n;
                 const bool cont = shade_extended(S, set, C, i, ps, found, h, aov, nr, &tape);
-                if (nr.kind != 0 && shadow_visible<W, false>(S, nr, C)) {
+                if (nr.kind != 0 && shadow_visible<W, false, INST>(S, nr, C)) {
                     ps.L = add(ps.L, nr.c);
                     tape.nee(nr, nf);
                 }
@@ -245,9 +245,18 @@ crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &
     const uint32_t copies = per_copy * (T / 32) <= 48 * 1024 ? T / 32 : (per_copy <= 48 * 1024 ? 1 : 0);
     const size_t dyn = per_copy * copies;
     switch (s->width) {
-    case 2: k_adjoint<2><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
-    case 4: k_adjoint<4><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
-    default: k_adjoint<8><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies); break;
+    case 2:
+        if (S.ninst) k_adjoint<2, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        else k_adjoint<2, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        break;
+    case 4:
+        if (S.ninst) k_adjoint<4, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        else k_adjoint<4, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        break;
+    default:
+        if (S.ninst) k_adjoint<8, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        else k_adjoint<8, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        break;
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(s->ctx, e, "k_adjoint launch");

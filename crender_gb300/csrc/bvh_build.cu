@@ -442,8 +442,9 @@ __global__ void k_treelet(Tree T, uint32_t n, uint32_t *__restrict__ visits, uin
 // ----------------------------------------------------------------- collapse
 struct Collapse {
     Tree T;
-    const float *verts;
+    const float *verts;  // the BVH's own triangles (model-local indexing)
     uint32_t W, leaf_max, node_bytes;
+    uint32_t prim_base;  // added to the primitive index stored in a triangle slot (scene-global ids)
 };
 
 __global__ void k_collapse_count(Collapse C, const uint32_t *__restrict__ level, uint32_t L, uint32_t *__restrict__ ents,
@@ -615,7 +616,7 @@ __global__ void k_collapse_emit(Collapse C, const uint32_t *__restrict__ level, 
                         const uint32_t prim = C.T.order[y & ~LEAF];
                         const float *v = C.verts + (size_t)prim * 9;
                         float4 *t = tris + (size_t)(tbase + toff) * 3;
-                        t[0] = make_float4(v[0], v[1], v[2], __uint_as_float(prim));
+                        t[0] = make_float4(v[0], v[1], v[2], __uint_as_float(prim + C.prim_base));
                         t[1] = make_float4(v[3], v[4], v[5], 0.0f);
                         t[2] = make_float4(v[6], v[7], v[8], 0.0f);
                         toff++;
@@ -652,66 +653,106 @@ inline uint32_t grid_for(uint64_t n, uint32_t threads, uint32_t cap = 152 * 32) 
     return (uint32_t)g;
 }
 
+// Where a build's scratch arrays come from: stream-ordered allocations for
+// crg_scene_build, a fixed device array for crg_build_bvh_noalloc.  get()
+// returns a 256-byte aligned block, or nullptr when none is available.
+struct ScratchSource {
+    virtual void *get(size_t bytes) = 0;
+    virtual ~ScratchSource() = default;
+};
+
 // Scratch owned for the duration of one build (stream-ordered allocations).
-struct Scratch {
+struct AsyncScratch final : ScratchSource {
     cudaStream_t st;
     std::vector<void *> ptrs;
     cudaError_t err = cudaSuccess;
-    template <typename T> T *get(size_t count) {
+    explicit AsyncScratch(cudaStream_t s) : st(s) {}
+    void *get(size_t bytes) override {
         void *p = nullptr;
-        const cudaError_t e = cudaMallocAsync(&p, count * sizeof(T) + 16, st);
-        if (e != cudaSuccess) { err = e; return nullptr; }
+        if (fault_injected()) {
+            err = cudaErrorMemoryAllocation;
+            return nullptr;
+        }
+        const cudaError_t e = cudaMallocAsync(&p, bytes + 16, st);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            err = e;
+            return nullptr;
+        }
         ptrs.push_back(p);
-        return (T *)p;
+        return p;
     }
-    ~Scratch() {
+    ~AsyncScratch() override {
         for (void *p : ptrs) cudaFreeAsync(p, st);
     }
 };
 
-} // namespace
+// One BVH of n triangles written into a region of a scene's node arrays.
+struct BvhTarget {
+    const float *verts;  // float[n*9], the BVH's triangles
+    uint32_t n;
+    float4 *nbox;        // binary nodes float4[2*max(1, n-1)]; nullptr = take them from the scratch
+    uint32_t *order;     // uint32[n]: sorted primitive order (BVH-local indices)
+    uint8_t *wide;       // node array; this BVH's nodes start at node_base
+    float4 *tris;        // triangle slot array; this BVH's slots start at slot_base
+    uint32_t node_base, node_cap; // region of the node array reserved for this BVH
+    uint32_t slot_base, prim_base;
+};
 
-crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t st) {
-    crg_context *ctx = s->ctx;
-    const uint32_t n = s->ntri;
-    s->built = false;
-    s->opts = o;
-    s->width = o.width;
-    s->node_bytes = ((24 + 7 * o.width) + 15) / 16 * 16;
-    s->n_wide = 0;
-    s->depth = 0;
-    s->sah = 0.0f;
-    if (n == 0) {
-        s->built = true;
-        return CRG_OK;
-    }
+struct BvhResult {
+    uint32_t n_wide = 0, depth = 0;
+    float sah = 0.0f;
+};
+
+// The build pipeline of this file's header comment, for one BVH.  Synchronises
+// the stream once per wide-BVH level.  On failure *msg names the failing step.
+crg_status build_pipeline(const BvhTarget &t, const crg_build_opts &o, ScratchSource &src, cudaStream_t st,
+                          BvhResult &res, std::string *msg) {
+    const uint32_t n = t.n;
+    res = BvhResult{};
+    if (n == 0) return CRG_OK;
     const uint32_t nint = n >= 2 ? n - 1 : 1;
-    crg_status rc;
-    if ((rc = dev_alloc(ctx, s->bvh2, sizeof(float4) * 2 * nint)) != CRG_OK) return rc;
-    if ((rc = dev_alloc(ctx, s->order, sizeof(uint32_t) * n)) != CRG_OK) return rc;
-    if ((rc = dev_alloc(ctx, s->wide, (size_t)s->node_bytes * nint)) != CRG_OK) return rc;
-    if ((rc = dev_alloc(ctx, s->tris, sizeof(float4) * 3 * n)) != CRG_OK) return rc;
-
-    Scratch S{st};
-    float4 *tbox = S.get<float4>(2 * (size_t)n);
-    uint32_t *cb = S.get<uint32_t>(8);
-    uint32_t *k0 = S.get<uint32_t>(n), *v0 = S.get<uint32_t>(n), *k1 = S.get<uint32_t>(n), *v1 = (uint32_t *)s->order.ptr;
+    const uint32_t node_bytes = ((24 + 7 * o.width) + 15) / 16 * 16;
     const uint32_t nblk = (n + kSortTile - 1) / kSortTile;
-    uint32_t *hist = S.get<uint32_t>(256 * (size_t)nblk);
-    uint32_t *parent = S.get<uint32_t>(nint), *leaf_parent = S.get<uint32_t>(n), *count = S.get<uint32_t>(nint);
-    uint32_t *visits = S.get<uint32_t>(nint);
-    float *cost = S.get<float>(nint);
-    uint32_t *lvl0 = S.get<uint32_t>(n + 1), *lvl1 = S.get<uint32_t>(n + 1);
-    uint32_t *ents = S.get<uint32_t>(8 * (size_t)(n + 1)), *nent = S.get<uint32_t>(n + 1);
-    uint32_t *ic = S.get<uint32_t>(n + 1), *tc = S.get<uint32_t>(n + 1), *totals = S.get<uint32_t>(2);
-    if (S.err != cudaSuccess) return cuda_error(ctx, S.err, "cudaMallocAsync(build scratch)");
+    auto fail = [&](crg_status s, const std::string &m) {
+        if (msg) *msg = m;
+        return s;
+    };
+    auto cuda_fail = [&](cudaError_t e, const char *what) {
+        (void)cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? CRG_ERR_OOM : CRG_ERR_CUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e));
+    };
+#define BP_CHECK(call)                                                                                                 \
+    do {                                                                                                               \
+        const cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);                                                            \
+    } while (0)
+    auto take = [&](size_t bytes) { return src.get((bytes + 255) / 256 * 256); };
+    float4 *tbox = (float4 *)take(sizeof(float4) * 2 * (size_t)n);
+    float4 *nbox = t.nbox ? t.nbox : (float4 *)take(sizeof(float4) * 2 * (size_t)nint);
+    uint32_t *cb = (uint32_t *)take(sizeof(uint32_t) * 8);
+    uint32_t *k0 = (uint32_t *)take(sizeof(uint32_t) * n), *v0 = (uint32_t *)take(sizeof(uint32_t) * n);
+    uint32_t *k1 = (uint32_t *)take(sizeof(uint32_t) * n), *v1 = (uint32_t *)take(sizeof(uint32_t) * n);
+    uint32_t *hist = (uint32_t *)take(sizeof(uint32_t) * 256 * (size_t)nblk);
+    uint32_t *parent = (uint32_t *)take(sizeof(uint32_t) * nint), *leaf_parent = (uint32_t *)take(sizeof(uint32_t) * n);
+    uint32_t *count = (uint32_t *)take(sizeof(uint32_t) * nint), *visits = (uint32_t *)take(sizeof(uint32_t) * nint);
+    float *cost = (float *)take(sizeof(float) * nint);
+    uint32_t *lvl0 = (uint32_t *)take(sizeof(uint32_t) * (n + 1)), *lvl1 = (uint32_t *)take(sizeof(uint32_t) * (n + 1));
+    uint32_t *ents = (uint32_t *)take(sizeof(uint32_t) * 8 * (size_t)(n + 1));
+    uint32_t *nent = (uint32_t *)take(sizeof(uint32_t) * (n + 1)), *ic = (uint32_t *)take(sizeof(uint32_t) * (n + 1));
+    uint32_t *tc = (uint32_t *)take(sizeof(uint32_t) * (n + 1)), *totals = (uint32_t *)take(sizeof(uint32_t) * 2);
+    if (!tbox || !nbox || !cb || !k0 || !v0 || !k1 || !v1 || !hist || !parent || !leaf_parent || !count || !visits ||
+        !cost || !lvl0 || !lvl1 || !ents || !nent || !ic || !tc || !totals)
+        return fail(CRG_ERR_OOM, "BVH build: no room for the build's scratch arrays");
 
-    CRG_CUDA(ctx, cudaMemsetAsync(cb, 0xFF, 3 * sizeof(uint32_t), st));
-    CRG_CUDA(ctx, cudaMemsetAsync(cb + 3, 0x00, 3 * sizeof(uint32_t), st));
+    // centroid bounds start at the identities of min / max
+    BP_CHECK(cudaMemsetAsync(cb, 0xFF, 3 * sizeof(uint32_t), st));
+    BP_CHECK(cudaMemsetAsync(cb + 3, 0x00, 3 * sizeof(uint32_t), st));
     const uint32_t T = 256;
-    k_bounds<<<grid_for(n, T), T, 0, st>>>((const float *)s->verts.ptr, n, tbox, cb);
+    k_bounds<<<grid_for(n, T), T, 0, st>>>(t.verts, n, tbox, cb);
     k_morton<<<grid_for(n, T), T, 0, st>>>(tbox, n, cb, k0, v0);
-    // 4 passes: k0/v0 -> k1/v1 -> k0/v0 -> k1/v1 -> k0/v0 ... keep the final values in order
+    // 4 passes: k0/v0 -> k1/v1 -> k0/v0 -> k1/v1 -> k0/v0: the sorted data ends in k0 / v0
     {
         uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
         for (int pass = 0; pass < 4; ++pass) {
@@ -721,71 +762,161 @@ crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t st) {
             std::swap(ki, ko);
             std::swap(vi, vo);
         }
-        // after 4 passes the sorted data is back in k0 / v0
-        CRG_CUDA(ctx, cudaMemcpyAsync(s->order.ptr, v0, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+        BP_CHECK(cudaMemcpyAsync(t.order, v0, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
     }
-    const uint32_t *codes = k0;
-    float4 *nbox = (float4 *)s->bvh2.ptr;
-    Tree Tr{tbox, (const uint32_t *)s->order.ptr, nbox, parent, leaf_parent, count, cost};
+    Tree Tr{tbox, t.order, nbox, parent, leaf_parent, count, cost};
     if (n >= 2) {
-        k_karras<<<grid_for(n - 1, T), T, 0, st>>>(codes, (int)n, nbox, parent, leaf_parent);
-        CRG_CUDA(ctx, cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+        k_karras<<<grid_for(n - 1, T), T, 0, st>>>(k0, (int)n, nbox, parent, leaf_parent);
+        BP_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
         k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 0);
-        CRG_CUDA(ctx, cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+        BP_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
         k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
         if (o.treelet) {
             uint32_t gamma = 7;
             for (uint32_t round = 0; round < o.treelet_rounds; ++round) {
-                CRG_CUDA(ctx, cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+                BP_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
                 k_treelet<<<grid_for(n, 128), 128, 0, st>>>(Tr, n, visits, gamma);
                 gamma *= 2;
             }
-            CRG_CUDA(ctx, cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
+            BP_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
             k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
         }
     } else {
         k_fill<<<1, 32, 0, st>>>(leaf_parent, 1, NONE);
     }
-    CRG_CUDA(ctx, cudaGetLastError());
+    BP_CHECK(cudaGetLastError());
 
-    // level-by-level collapse
-    Collapse Cc{Tr, (const float *)s->verts.ptr, o.width, o.leaf_max, s->node_bytes};
-    const uint32_t root = n >= 2 ? 0u : LEAF;
-    k_fill<<<1, 32, 0, st>>>(lvl0, 1, root);
+    // level-by-level collapse into the target region
+    Collapse Cc{Tr, t.verts, o.width, o.leaf_max, node_bytes, t.prim_base};
+    k_fill<<<1, 32, 0, st>>>(lvl0, 1, n >= 2 ? 0u : LEAF);
     uint32_t L = 1, node_start = 0, next_start = 1, tri_start = 0, depth = 0;
     uint32_t *cur = lvl0, *nxt = lvl1;
     while (L > 0) {
         k_collapse_count<<<grid_for(L, 128), 128, 0, st>>>(Cc, cur, L, ents, nent, ic, tc);
         k_scan<<<1, 1024, 0, st>>>(ic, L, totals);
         k_scan<<<1, 1024, 0, st>>>(tc, L, totals + 1);
-        k_collapse_emit<<<grid_for(L, 64), 64, 0, st>>>(Cc, cur, L, ents, nent, ic, tc, node_start, next_start, tri_start,
-                                                       (uint8_t *)s->wide.ptr, (float4 *)s->tris.ptr, nxt);
+        k_collapse_emit<<<grid_for(L, 64), 64, 0, st>>>(Cc, cur, L, ents, nent, ic, tc, t.node_base + node_start,
+                                                       t.node_base + next_start, t.slot_base + tri_start, t.wide,
+                                                       t.tris, nxt);
         uint32_t h[2];
-        CRG_CUDA(ctx, cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, st));
-        CRG_CUDA(ctx, cudaStreamSynchronize(st));
-        CRG_CUDA(ctx, cudaGetLastError());
+        BP_CHECK(cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, st));
+        BP_CHECK(cudaStreamSynchronize(st));
+        BP_CHECK(cudaGetLastError());
         depth++;
         node_start = next_start;
         next_start += h[0];
         tri_start += h[1];
         L = h[0];
         std::swap(cur, nxt);
-        if (next_start > nint + 1) return set_error(ctx, CRG_ERR_DEVICE, "wide BVH node count exceeded capacity");
+        // the next level writes nodes [node_start, next_start): stop before it would leave the region
+        if (next_start > t.node_cap) return fail(CRG_ERR_DEVICE, "wide BVH node count exceeded capacity");
     }
-    s->n_wide = next_start;
-    s->depth = depth;
-    if (tri_start != n) return set_error(ctx, CRG_ERR_DEVICE, "wide BVH triangle count mismatch");
+    if (tri_start != n) return fail(CRG_ERR_DEVICE, "wide BVH triangle count mismatch");
+    res.n_wide = next_start;
+    res.depth = depth;
     if (n >= 2) {
-        float h[1];
-        float4 root_lo_hi[2];
-        CRG_CUDA(ctx, cudaMemcpyAsync(h, cost, sizeof(float), cudaMemcpyDeviceToHost, st));
-        CRG_CUDA(ctx, cudaMemcpyAsync(root_lo_hi, nbox, sizeof(root_lo_hi), cudaMemcpyDeviceToHost, st));
-        CRG_CUDA(ctx, cudaStreamSynchronize(st));
-        const float dx = root_lo_hi[1].x - root_lo_hi[0].x, dy = root_lo_hi[1].y - root_lo_hi[0].y,
-                    dz = root_lo_hi[1].z - root_lo_hi[0].z;
+        float c0 = 0.0f;
+        float4 r[2];
+        BP_CHECK(cudaMemcpyAsync(&c0, cost, sizeof(float), cudaMemcpyDeviceToHost, st));
+        BP_CHECK(cudaMemcpyAsync(r, nbox, sizeof(r), cudaMemcpyDeviceToHost, st));
+        BP_CHECK(cudaStreamSynchronize(st));
+        const float dx = r[1].x - r[0].x, dy = r[1].y - r[0].y, dz = r[1].z - r[0].z;
         const float ra = 2.0f * ((dx * dy + dy * dz) + dz * dx);
-        s->sah = ra > 0.0f ? h[0] / ra : 0.0f;
+        res.sah = ra > 0.0f ? c0 / ra : 0.0f;
     }
+#undef BP_CHECK
+    (void)node_bytes;
+    return CRG_OK;
+}
+
+// Grows b to `bytes`, keeping its first `keep` bytes (device to device).
+crg_status grow_keep(crg_context *ctx, DevBuf &b, size_t bytes, size_t keep, cudaStream_t st) {
+    if (b.ptr && b.bytes >= bytes) return CRG_OK;
+    DevBuf nb;
+    crg_status rc = dev_alloc(ctx, nb, bytes);
+    if (rc != CRG_OK) return rc;
+    if (b.ptr && keep) {
+        const cudaError_t e = cudaMemcpyAsync(nb.ptr, b.ptr, std::min(keep, b.bytes), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) (void)cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            dev_free(nb);
+            return cuda_error(ctx, e, "cudaMemcpyAsync(grow)");
+        }
+    }
+    dev_free(b);
+    b = nb;
+    return CRG_OK;
+}
+
+} // namespace
+
+crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t st) {
+    crg_context *ctx = s->ctx;
+    const bool same = s->opts.width == o.width && s->opts.treelet == o.treelet && s->opts.leaf_max == o.leaf_max &&
+                      s->opts.treelet_rounds == o.treelet_rounds;
+    if (!same)
+        for (crg_model_rec &m : s->models) m.built = false;
+    s->built = false;
+    s->opts = o;
+    s->width = o.width;
+    s->node_bytes = ((24 + 7 * o.width) + 15) / 16 * 16;
+    // node arrays: each model's region at node_base (fixed by the triangle counts)
+    uint32_t cap = 0;
+    for (const crg_model_rec &m : s->models) cap = std::max(cap, m.node_base + m.node_cap);
+    const uint32_t old_cap = s->node_cap;
+    const size_t keep_nodes = same ? old_cap : 0;
+    crg_status rc;
+    if (s->ntri > 0) {
+        if ((rc = grow_keep(ctx, s->bvh2, sizeof(float4) * 2 * (size_t)cap, sizeof(float4) * 2 * keep_nodes, st)) != CRG_OK)
+            return rc;
+        if ((rc = grow_keep(ctx, s->wide, (size_t)s->node_bytes * cap, (size_t)s->node_bytes * keep_nodes, st)) != CRG_OK)
+            return rc;
+        size_t kept_prims = 0;
+        for (const crg_model_rec &m : s->models)
+            if (m.built) kept_prims = std::max<size_t>(kept_prims, (size_t)m.first + m.ntri);
+        if ((rc = grow_keep(ctx, s->order, sizeof(uint32_t) * s->ntri, sizeof(uint32_t) * kept_prims, st)) != CRG_OK)
+            return rc;
+        if ((rc = grow_keep(ctx, s->tris, sizeof(float4) * 3 * s->ntri, sizeof(float4) * 3 * kept_prims, st)) != CRG_OK)
+            return rc;
+        if (cap > old_cap || !same) // unused node slots read as zero (deterministic downloads)
+            CRG_CUDA(ctx, cudaMemsetAsync((uint8_t *)s->wide.ptr + (size_t)s->node_bytes * keep_nodes, 0,
+                                          (size_t)s->node_bytes * (cap - keep_nodes), st));
+    }
+    s->node_cap = cap;
+    for (crg_model_rec &m : s->models) {
+        if (m.built) continue;
+        BvhTarget t{(const float *)s->verts.ptr + (size_t)m.first * 9,
+                    m.ntri,
+                    (float4 *)s->bvh2.ptr + 2 * (size_t)m.node_base,
+                    (uint32_t *)s->order.ptr + m.first,
+                    (uint8_t *)s->wide.ptr,
+                    (float4 *)s->tris.ptr,
+                    m.node_base,
+                    m.node_base + m.node_cap,
+                    m.first,
+                    m.first};
+        AsyncScratch src(st);
+        BvhResult res;
+        std::string msg;
+        rc = build_pipeline(t, o, src, st, res, &msg);
+        if (rc != CRG_OK) {
+            if (src.err != cudaSuccess) return cuda_error(ctx, src.err, "cudaMallocAsync(build scratch)");
+            return set_error(ctx, rc, msg);
+        }
+        m.n_wide = res.n_wide;
+        m.depth = res.depth;
+        m.sah = res.sah;
+        m.built = true;
+    }
+    // whole-scene figures: the single model's, or the sums / maxima over the models
+    s->n_wide = 0;
+    s->depth = 0;
+    s->sah = 0.0f;
+    for (const crg_model_rec &m : s->models) {
+        s->depth = std::max(s->depth, m.depth);
+        s->sah += m.sah;
+    }
+    s->n_wide = s->models.size() == 1 ? s->models[0].n_wide : cap;
     s->built = true;
     return CRG_OK;
 }
@@ -793,41 +924,40 @@ crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t st) {
 } // namespace crg
 
 // ----------------------------------------------------------------- build without allocation
-// crg_build_bvh_noalloc: the same pipeline as build_bvh for callers that may
-// not allocate device memory (see include/crg.h).  Its scratch lives in one
+// crg_build_bvh_noalloc: build_pipeline with its scratch carved from one
 // file-scope __device__ array sized for CRG_NOALLOC_MAX_TRIS triangles; every
 // GPU that loads this library holds it until the process exits.
 namespace crg {
 namespace {
 
 constexpr size_t kNaN = CRG_NOALLOC_MAX_TRIS; // max triangles
-constexpr size_t kNaN1 = kNaN + 1;
 constexpr size_t kNaBlk = (kNaN + kSortTile - 1) / kSortTile;
 constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
-// section sizes in bytes, each rounded to 256
-constexpr size_t kNaTbox = na_round(sizeof(float4) * 2 * kNaN);
-constexpr size_t kNaNbox = na_round(sizeof(float4) * 2 * kNaN);
-constexpr size_t kNaCb = na_round(sizeof(uint32_t) * 8);
-constexpr size_t kNaKey = na_round(sizeof(uint32_t) * kNaN);
-constexpr size_t kNaHist = na_round(sizeof(uint32_t) * 256 * kNaBlk);
-constexpr size_t kNaU32N = na_round(sizeof(uint32_t) * kNaN);
-constexpr size_t kNaU32N1 = na_round(sizeof(uint32_t) * kNaN1);
-constexpr size_t kNaEnts = na_round(sizeof(uint32_t) * 8 * kNaN1);
-constexpr size_t kNaTotals = na_round(sizeof(uint32_t) * 2);
-constexpr size_t kNaBytes = kNaTbox + kNaNbox + kNaCb + 4 * kNaKey + kNaHist + 5 * kNaU32N + 2 * kNaU32N1 + kNaEnts +
-                            3 * kNaU32N1 + kNaTotals;
+// the blocks build_pipeline takes for kNaN triangles, each rounded to 256 bytes
+constexpr size_t kNaBytes = 2 * na_round(sizeof(float4) * 2 * kNaN) +    // triangle boxes, binary nodes
+                            na_round(sizeof(uint32_t) * 8) +               // centroid bounds
+                            4 * na_round(sizeof(uint32_t) * kNaN) +        // sort keys and values
+                            na_round(sizeof(uint32_t) * 256 * kNaBlk) +    // digit histograms
+                            5 * na_round(sizeof(uint32_t) * kNaN) +        // parent, leaf parent, count, visits, cost
+                            2 * na_round(sizeof(uint32_t) * (kNaN + 1)) +  // collapse levels
+                            na_round(sizeof(uint32_t) * 8 * (kNaN + 1)) +  // collapse entries
+                            3 * na_round(sizeof(uint32_t) * (kNaN + 1)) +  // entry / internal / triangle counts
+                            na_round(sizeof(uint32_t) * 2);                // level totals
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 // Device address of g_noalloc_scratch per device, fetched once with that
-// device current (the host-side symbol is only a stand-in).
+// device current (in host code the symbol's name is only a stand-in).
 constexpr int kNaMaxDevices = 64;
 unsigned char *g_noalloc_ptr[kNaMaxDevices] = {nullptr};
 std::mutex g_noalloc_mutex;
 
 crg_status noalloc_scratch(unsigned char **out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return CRG_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) {
+        (void)cudaGetLastError();
+        return CRG_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
@@ -841,23 +971,55 @@ crg_status noalloc_scratch(unsigned char **out) {
     return CRG_OK;
 }
 
+// Bump allocation over the fixed array; never more than kNaBytes.
+struct FixedScratch final : ScratchSource {
+    unsigned char *base;
+    size_t used = 0;
+    explicit FixedScratch(unsigned char *b) : base(b) {}
+    void *get(size_t bytes) override {
+        if (bytes > kNaBytes - used) return nullptr;
+        void *p = base + used;
+        used += bytes;
+        return p;
+    }
+};
+
+// Message of this thread's last failed crg_build_bvh_noalloc call.
+thread_local std::string g_noalloc_error;
+
+crg_status noalloc_fail(crg_status s, const std::string &m) {
+    g_noalloc_error = m;
+    return s;
+}
+
 } // namespace
+
+void noalloc_prepare() {
+    unsigned char *p = nullptr;
+    (void)noalloc_scratch(&p);
+}
+
 } // namespace crg
+
+extern "C" const char *crg_noalloc_last_error(void) { return crg::g_noalloc_error.c_str(); }
 
 extern "C" crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri, const crg_build_opts *opts,
                                             void *d_wide, size_t wide_bytes, float *d_tris, uint32_t *d_order,
                                             crg_bvh_info *info, crg_stream stream) {
     using namespace crg;
+    g_noalloc_error.clear();
     crg_build_opts o{8, 0, 3, 3};
     if (opts) o = *opts;
     if (!((o.width == 2 || o.width == 4 || o.width == 8) && o.leaf_max >= 1 && o.leaf_max <= 3 && o.treelet_rounds <= 8))
-        return CRG_ERR_INVALID_ARG;
-    if (ntri > CRG_NOALLOC_MAX_TRIS) return CRG_ERR_INVALID_ARG;
+        return noalloc_fail(CRG_ERR_INVALID_ARG, "build options: width 2/4/8, leaf_max 1..3, treelet_rounds <= 8");
+    if (ntri > CRG_NOALLOC_MAX_TRIS)
+        return noalloc_fail(CRG_ERR_INVALID_ARG, "more triangles than CRG_NOALLOC_MAX_TRIS");
     const uint32_t n = ntri;
     const uint32_t node_bytes = ((24 + 7 * o.width) + 15) / 16 * 16;
     const uint32_t nint = n >= 2 ? n - 1 : 1;
-    if (n > 0 && (!d_verts || !d_wide || !d_tris || !d_order)) return CRG_ERR_INVALID_ARG;
-    if (n > 0 && wide_bytes < (size_t)node_bytes * nint) return CRG_ERR_INVALID_ARG;
+    if (n > 0 && (!d_verts || !d_wide || !d_tris || !d_order)) return noalloc_fail(CRG_ERR_INVALID_ARG, "null buffer");
+    if (n > 0 && wide_bytes < (size_t)node_bytes * nint)
+        return noalloc_fail(CRG_ERR_INVALID_ARG, "node buffer smaller than node_bytes * max(1, ntri - 1)");
     if (info) {
         *info = crg_bvh_info{};
         info->ntri = n;
@@ -870,111 +1032,26 @@ extern "C" crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri,
     }
     if (n == 0) return CRG_OK;
     unsigned char *base = nullptr;
-    if (noalloc_scratch(&base) != CRG_OK) return CRG_ERR_CUDA;
+    if (noalloc_scratch(&base) != CRG_OK) return noalloc_fail(CRG_ERR_CUDA, "cudaGetSymbolAddress(scratch array) failed");
+    // an error left pending by the caller's earlier work is not this call's
+    (void)cudaGetLastError();
     cudaStream_t st = (cudaStream_t)stream;
-    unsigned char *cur_p = base;
-    auto take = [&](size_t bytes) {
-        unsigned char *p = cur_p;
-        cur_p += bytes;
-        return p;
-    };
-    float4 *tbox = (float4 *)take(kNaTbox);
-    float4 *nbox = (float4 *)take(kNaNbox);
-    uint32_t *cb = (uint32_t *)take(kNaCb);
-    uint32_t *k0 = (uint32_t *)take(kNaKey), *v0 = (uint32_t *)take(kNaKey);
-    uint32_t *k1 = (uint32_t *)take(kNaKey), *v1 = (uint32_t *)take(kNaKey);
-    uint32_t *hist = (uint32_t *)take(kNaHist);
-    uint32_t *parent = (uint32_t *)take(kNaU32N), *leaf_parent = (uint32_t *)take(kNaU32N);
-    uint32_t *count = (uint32_t *)take(kNaU32N), *visits = (uint32_t *)take(kNaU32N);
-    float *cost = (float *)take(kNaU32N);
-    uint32_t *lvl0 = (uint32_t *)take(kNaU32N1), *lvl1 = (uint32_t *)take(kNaU32N1);
-    uint32_t *ents = (uint32_t *)take(kNaEnts);
-    uint32_t *nent = (uint32_t *)take(kNaU32N1), *ic = (uint32_t *)take(kNaU32N1), *tc = (uint32_t *)take(kNaU32N1);
-    uint32_t *totals = (uint32_t *)take(kNaTotals);
-
-#define NA_CHECK(call)                                                                                                 \
-    do {                                                                                                               \
-        if ((call) != cudaSuccess) {                                                                                   \
-            (void)cudaGetLastError();                                                                                  \
-            return CRG_ERR_CUDA;                                                                                       \
-        }                                                                                                              \
-    } while (0)
-    // state that must start at zero / at the identity of min/max
-    NA_CHECK(cudaMemsetAsync(cb, 0xFF, 3 * sizeof(uint32_t), st));
-    NA_CHECK(cudaMemsetAsync(cb + 3, 0x00, 3 * sizeof(uint32_t), st));
-    const uint32_t T = 256;
-    const uint32_t nblk = (n + kSortTile - 1) / kSortTile;
-    k_bounds<<<grid_for(n, T), T, 0, st>>>(d_verts, n, tbox, cb);
-    k_morton<<<grid_for(n, T), T, 0, st>>>(tbox, n, cb, k0, v0);
-    {
-        uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
-        for (int pass = 0; pass < 4; ++pass) {
-            k_hist<<<nblk, kSortThreads, 0, st>>>(ki, n, pass * 8, hist);
-            k_scan<<<1, 1024, 0, st>>>(hist, 256 * nblk, nullptr);
-            k_scatter<<<nblk, kSortThreads, 0, st>>>(ki, vi, n, pass * 8, hist, ko, vo);
-            std::swap(ki, ko);
-            std::swap(vi, vo);
-        }
-        NA_CHECK(cudaMemcpyAsync(d_order, v0, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
+    FixedScratch src(base);
+    BvhTarget t{d_verts, n, nullptr, d_order, (uint8_t *)d_wide, (float4 *)d_tris, 0, nint, 0, 0};
+    BvhResult res;
+    std::string msg;
+    const crg_status rc = build_pipeline(t, o, src, st, res, &msg);
+    if (rc != CRG_OK) {
+        // kernels queued before the failure may still use the shared array:
+        // let them finish so the caller's next call does not race with them
+        (void)cudaStreamSynchronize(st);
+        (void)cudaGetLastError();
+        return noalloc_fail(rc, msg);
     }
-    Tree Tr{tbox, d_order, nbox, parent, leaf_parent, count, cost};
-    if (n >= 2) {
-        k_karras<<<grid_for(n - 1, T), T, 0, st>>>(k0, (int)n, nbox, parent, leaf_parent);
-        NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
-        k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 0);
-        NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
-        k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
-        if (o.treelet) {
-            uint32_t gamma = 7;
-            for (uint32_t round = 0; round < o.treelet_rounds; ++round) {
-                NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
-                k_treelet<<<grid_for(n, 128), 128, 0, st>>>(Tr, n, visits, gamma);
-                gamma *= 2;
-            }
-            NA_CHECK(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * nint, st));
-            k_bottom_up<<<grid_for(n, T), T, 0, st>>>(Tr, n, visits, 1);
-        }
-    } else {
-        k_fill<<<1, 32, 0, st>>>(leaf_parent, 1, NONE);
-    }
-    NA_CHECK(cudaGetLastError());
-    Collapse Cc{Tr, d_verts, o.width, o.leaf_max, node_bytes};
-    k_fill<<<1, 32, 0, st>>>(lvl0, 1, n >= 2 ? 0u : LEAF);
-    uint32_t L = 1, node_start = 0, next_start = 1, tri_start = 0, depth = 0;
-    uint32_t *cur = lvl0, *nxt = lvl1;
-    while (L > 0) {
-        k_collapse_count<<<grid_for(L, 128), 128, 0, st>>>(Cc, cur, L, ents, nent, ic, tc);
-        k_scan<<<1, 1024, 0, st>>>(ic, L, totals);
-        k_scan<<<1, 1024, 0, st>>>(tc, L, totals + 1);
-        k_collapse_emit<<<grid_for(L, 64), 64, 0, st>>>(Cc, cur, L, ents, nent, ic, tc, node_start, next_start, tri_start,
-                                                       (uint8_t *)d_wide, (float4 *)d_tris, nxt);
-        uint32_t h[2];
-        NA_CHECK(cudaMemcpyAsync(h, totals, sizeof(h), cudaMemcpyDeviceToHost, st));
-        NA_CHECK(cudaStreamSynchronize(st));
-        NA_CHECK(cudaGetLastError());
-        depth++;
-        node_start = next_start;
-        next_start += h[0];
-        tri_start += h[1];
-        L = h[0];
-        std::swap(cur, nxt);
-        if (next_start > nint + 1) return CRG_ERR_DEVICE;
-    }
-    if (tri_start != n) return CRG_ERR_DEVICE;
     if (info) {
-        info->n_wide_nodes = next_start;
-        info->depth = depth;
-        if (n >= 2) {
-            float c0 = 0.0f;
-            float4 r[2];
-            NA_CHECK(cudaMemcpyAsync(&c0, cost, sizeof(float), cudaMemcpyDeviceToHost, st));
-            NA_CHECK(cudaMemcpyAsync(r, nbox, sizeof(r), cudaMemcpyDeviceToHost, st));
-            NA_CHECK(cudaStreamSynchronize(st));
-            const float dx = r[1].x - r[0].x, dy = r[1].y - r[0].y, dz = r[1].z - r[0].z;
-            const float ra = 2.0f * ((dx * dy + dy * dz) + dz * dx);
-            info->sah_cost = ra > 0.0f ? c0 / ra : 0.0f;
-        }
+        info->n_wide_nodes = res.n_wide;
+        info->depth = res.depth;
+        info->sah_cost = res.sah;
     }
-#undef NA_CHECK
     return CRG_OK;
 }

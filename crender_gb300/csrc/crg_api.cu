@@ -5,6 +5,8 @@
 // the host side only validates arguments, copies inputs, prepares the
 // emissive-triangle table and launches kernels.
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -16,6 +18,29 @@
 #include "crg_internal.h"
 
 namespace crg {
+
+namespace {
+// Countdown of the armed allocation fault: -1 = disarmed, else the number of
+// allocations still to succeed before one fails.
+std::atomic<int64_t> g_fault_countdown{-1};
+std::atomic<uint64_t> g_alloc_seen{0};
+std::atomic<uint32_t> g_fault_fired{0};
+} // namespace
+
+bool fault_injected() {
+    g_alloc_seen.fetch_add(1, std::memory_order_relaxed);
+    int64_t c = g_fault_countdown.load(std::memory_order_relaxed);
+    while (c >= 0) {
+        if (g_fault_countdown.compare_exchange_weak(c, c - 1, std::memory_order_relaxed)) {
+            if (c == 0) {
+                g_fault_fired.fetch_add(1, std::memory_order_relaxed);
+                return true;
+            }
+            return false;
+        }
+    }
+    return false;
+}
 
 crg_status set_error(crg_context *ctx, crg_status s, const std::string &msg) {
     if (ctx) {
@@ -34,6 +59,8 @@ crg_status dev_alloc(crg_context *ctx, DevBuf &b, size_t bytes) {
     if (b.ptr && b.bytes >= bytes) return CRG_OK;
     dev_free(b);
     if (bytes == 0) return CRG_OK;
+    if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "device allocation of " + std::to_string(bytes) +
+                                                                 " bytes failed (injected fault)");
     void *p = nullptr;
     const cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) {
@@ -199,20 +226,23 @@ crg_status prepare_lights(crg_scene *s) {
     std::vector<uint32_t> prim, inst;
     std::vector<double> w;
     double total = 0.0;
-    // entries in instance-major, primitive order; an instanced scene weighs
-    // each emitter copy by its world area
+    // entries in placement-major, primitive order; an instanced scene holds one
+    // copy of every emissive triangle of a placement's model, weighed by its world area
     const uint32_t ncopy = s->ninst ? s->ninst : 1;
-    for (uint32_t j = 0; j < ncopy; ++j)
-        for (uint32_t p = 0; p < s->ntri; ++p) {
+    for (uint32_t j = 0; j < ncopy; ++j) {
+        const uint32_t p0 = s->ninst ? s->models[s->place_model[j]].first : 0;
+        const uint32_t p1 = s->ninst ? p0 + s->models[s->place_model[j]].ntri : s->ntri;
+        for (uint32_t p = p0; p < p1; ++p) {
             const uint32_t m = mat_idx[p];
             if (!(lum[m] > 0.0)) continue;
-            const double area = s->ninst ? s->inst_area[(size_t)j * s->ntri + p] : s->tri_area[p];
+            const double area = s->ninst ? s->inst_area[s->inst_area_off[j] + (p - p0)] : s->tri_area[p];
             const double wt = area * lum[m];
             prim.push_back(p);
             inst.push_back(j);
             w.push_back(wt);
             total += wt;
         }
+    }
     std::vector<float> mpdf(nmat, 0.0f);
     s->nlights = 0;
     if (total > 0.0) {
@@ -277,12 +307,15 @@ bool instance_rows(const float *x, float rows[24]) {
     return true;
 }
 
-// World areas (double) of every triangle under every instance.
+// World areas (double) of every triangle of each placement's model under its transform.
 void instance_areas(crg_scene *s, const float *verts) {
-    s->inst_area.assign((size_t)s->ninst * s->ntri, 0.0);
+    s->inst_area.clear();
+    s->inst_area_off.assign(s->ninst, 0);
     for (uint32_t j = 0; j < s->ninst; ++j) {
         const float *x = &s->host_xf[16 * (size_t)j];
-        for (uint32_t p = 0; p < s->ntri; ++p) {
+        const crg_model_rec &md = s->models[s->place_model[j]];
+        s->inst_area_off[j] = s->inst_area.size();
+        for (uint32_t p = md.first; p < md.first + md.ntri; ++p) {
             double w[3][3];
             for (int k = 0; k < 3; ++k) {
                 const float *v = verts + (size_t)p * 9 + 3 * k;
@@ -296,9 +329,267 @@ void instance_areas(crg_scene *s, const float *verts) {
             }
             const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
                          cz = e1[0] * e2[1] - e1[1] * e2[0];
-            s->inst_area[(size_t)j * s->ntri + p] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+            s->inst_area.push_back(0.5 * std::sqrt(cx * cx + cy * cy + cz * cz));
         }
     }
+}
+
+// Object-space bounds of ntri de-indexed triangles (host float[ntri*9]).
+void mesh_box(const float *v, uint32_t ntri, float box[6]) {
+    for (int a = 0; a < 3; ++a) {
+        box[a] = INFINITY;
+        box[3 + a] = -INFINITY;
+    }
+    for (size_t i = 0; i < 9 * (size_t)ntri; ++i) {
+        const int a = (int)(i % 3);
+        box[a] = std::min(box[a], v[i]);
+        box[3 + a] = std::max(box[3 + a], v[i]);
+    }
+    if (ntri == 0)
+        for (int a = 0; a < 6; ++a) box[a] = 0.0f;
+}
+
+const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+// World box of a model's object box under a column-major affine transform,
+// from its 8 corners in double, widened outwards by 1e-5 of its size and of
+// its distance from the origin so that every rounded world point of a hit
+// lies inside it.
+void world_box(const float box[6], const float *x, double out[6]) {
+    for (int a = 0; a < 3; ++a) {
+        out[a] = INFINITY;
+        out[3 + a] = -INFINITY;
+    }
+    for (int c = 0; c < 8; ++c) {
+        const double p[3] = {box[(c & 1) ? 3 : 0], box[(c & 2) ? 4 : 1], box[(c & 4) ? 5 : 2]};
+        for (int r = 0; r < 3; ++r) {
+            const double w = (((double)x[r] * p[0] + (double)x[4 + r] * p[1]) + (double)x[8 + r] * p[2]) + (double)x[12 + r];
+            out[r] = std::min(out[r], w);
+            out[3 + r] = std::max(out[3 + r], w);
+        }
+    }
+    double mag = 0.0, ext = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        mag = std::max(mag, std::max(std::fabs(out[a]), std::fabs(out[3 + a])));
+        ext = std::max(ext, out[3 + a] - out[a]);
+    }
+    const double pad = 1e-5 * (mag + ext) + 1e-30;
+    for (int a = 0; a < 3; ++a) {
+        out[a] -= pad;
+        out[3 + a] += pad;
+    }
+}
+
+// Top-level tree over the placements' world boxes: a binary tree split at the
+// median placement along the widest axis of the box centres (ties by placement
+// index), nodes in pre-order.  Node i is 4 float4: {lo_a.xyz, ref_a},
+// {hi_a.xyz, ref_b}, {lo_b.xyz, 0}, {hi_b.xyz, 0}; a ref is a node index, or
+// kTlasLeaf | placement.  Boxes are rounded outwards to float.
+struct TlasBuilder {
+    const std::vector<std::array<double, 6>> &box;
+    std::vector<float> nodes; // 16 floats per node
+    std::array<double, 6> bounds(const std::vector<uint32_t> &ids, size_t b, size_t e) const {
+        std::array<double, 6> r{INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (size_t i = b; i < e; ++i)
+            for (int a = 0; a < 3; ++a) {
+                r[a] = std::min(r[a], box[ids[i]][a]);
+                r[3 + a] = std::max(r[3 + a], box[ids[i]][3 + a]);
+            }
+        return r;
+    }
+    static float down(double v) {
+        float f = (float)v;
+        if ((double)f > v) f = std::nextafter(f, -INFINITY);
+        return f;
+    }
+    static float up(double v) {
+        float f = (float)v;
+        if ((double)f < v) f = std::nextafter(f, INFINITY);
+        return f;
+    }
+    // returns the ref of the subtree over ids[b, e)
+    uint32_t build(std::vector<uint32_t> &ids, size_t b, size_t e) {
+        if (e - b == 1) return kTlasLeaf | ids[b];
+        const uint32_t me = (uint32_t)(nodes.size() / 16);
+        nodes.resize(nodes.size() + 16, 0.0f);
+        double clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (size_t i = b; i < e; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double c = 0.5 * (box[ids[i]][a] + box[ids[i]][3 + a]);
+                clo[a] = std::min(clo[a], c);
+                chi[a] = std::max(chi[a], c);
+            }
+        int ax = 0;
+        for (int a = 1; a < 3; ++a)
+            if (chi[a] - clo[a] > chi[ax] - clo[ax]) ax = a;
+        std::sort(ids.begin() + b, ids.begin() + e, [&](uint32_t p, uint32_t q) {
+            const double cp = box[p][ax] + box[p][3 + ax], cq = box[q][ax] + box[q][3 + ax];
+            return cp < cq || (cp == cq && p < q);
+        });
+        const size_t mid = b + (e - b) / 2;
+        const std::array<double, 6> la = bounds(ids, b, mid), lb = bounds(ids, mid, e);
+        const uint32_t ra = build(ids, b, mid);
+        const uint32_t rb = build(ids, mid, e);
+        float *n = &nodes[16 * (size_t)me];
+        for (int a = 0; a < 3; ++a) {
+            n[a] = down(la[a]);
+            n[4 + a] = up(la[3 + a]);
+            n[8 + a] = down(lb[a]);
+            n[12 + a] = up(lb[3 + a]);
+        }
+        std::memcpy(&n[3], &ra, 4);
+        std::memcpy(&n[7], &rb, 4);
+        return me;
+    }
+};
+
+// Rebuilds the placement list of a scene from its models' instance lists:
+// device transform rows, BVH roots, the top-level tree and the world areas of
+// emitter copies.  A scene of one model without a list has no placements.
+crg_status update_placements(crg_scene *s) {
+    crg_context *ctx = s->ctx;
+    const bool flat = s->models.size() == 1 && s->models[0].xf.empty();
+    s->ninst = 0;
+    s->host_xf.clear();
+    s->host_rows.clear();
+    s->place_model.clear();
+    s->inst_area.clear();
+    s->inst_area_off.clear();
+    s->tlas_root = 0;
+    s->tlas_nodes = 0;
+    dev_free(s->inst);
+    dev_free(s->inst_root);
+    dev_free(s->tlas);
+    dev_free(s->light_inst);
+    if (flat) return CRG_OK;
+    std::vector<uint32_t> roots;
+    std::vector<std::array<double, 6>> boxes;
+    for (uint32_t m = 0; m < (uint32_t)s->models.size(); ++m) {
+        const crg_model_rec &md = s->models[m];
+        const uint32_t count = md.xf.empty() ? 1u : (uint32_t)(md.xf.size() / 16);
+        for (uint32_t j = 0; j < count; ++j) {
+            const float *x = md.xf.empty() ? kIdentity : &md.xf[16 * (size_t)j];
+            float rows[24];
+            if (!instance_rows(x, rows)) return set_error(ctx, CRG_ERR_INVALID_ARG, "instance transform is not invertible");
+            s->host_xf.insert(s->host_xf.end(), x, x + 16);
+            s->host_rows.insert(s->host_rows.end(), rows, rows + 24);
+            s->place_model.push_back(m);
+            roots.push_back(md.node_base);
+            std::array<double, 6> wb;
+            world_box(md.box, x, wb.data());
+            boxes.push_back(wb);
+        }
+    }
+    const uint32_t np = (uint32_t)s->place_model.size();
+    if (np > (1u << 20)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 2^20 placements");
+    TlasBuilder tb{boxes, {}};
+    std::vector<uint32_t> ids(np);
+    for (uint32_t k = 0; k < np; ++k) ids[k] = k;
+    const uint32_t root = tb.build(ids, 0, np);
+    crg_status rc;
+    if ((rc = dev_alloc(ctx, s->inst, sizeof(float) * s->host_rows.size())) != CRG_OK) return rc;
+    if ((rc = dev_alloc(ctx, s->inst_root, sizeof(uint32_t) * np)) != CRG_OK) return rc;
+    if (!tb.nodes.empty() && (rc = dev_alloc(ctx, s->tlas, sizeof(float) * tb.nodes.size())) != CRG_OK) return rc;
+    CRG_CUDA(ctx, cudaMemcpy(s->inst.ptr, s->host_rows.data(), sizeof(float) * s->host_rows.size(), cudaMemcpyHostToDevice));
+    CRG_CUDA(ctx, cudaMemcpy(s->inst_root.ptr, roots.data(), sizeof(uint32_t) * np, cudaMemcpyHostToDevice));
+    if (!tb.nodes.empty())
+        CRG_CUDA(ctx, cudaMemcpy(s->tlas.ptr, tb.nodes.data(), sizeof(float) * tb.nodes.size(), cudaMemcpyHostToDevice));
+    s->tlas_root = root;
+    s->tlas_nodes = (uint32_t)(tb.nodes.size() / 16);
+    s->ninst = np;
+    // emitter copies are weighed by their world areas: the vertices come back to the host once
+    std::vector<float> hv((size_t)s->ntri * 9);
+    if (s->ntri) CRG_CUDA(ctx, cudaMemcpy(hv.data(), s->verts.ptr, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost));
+    instance_areas(s, hv.data());
+    return CRG_OK;
+}
+
+// Copies the first `keep` bytes of src into a fresh buffer of `bytes` bytes.
+crg_status copy_grow(crg_context *ctx, const DevBuf &src, size_t keep, size_t bytes, DevBuf &out) {
+    crg_status rc = dev_alloc(ctx, out, bytes);
+    if (rc != CRG_OK) return rc;
+    if (src.ptr && keep) CRG_CUDA(ctx, cudaMemcpy(out.ptr, src.ptr, keep, cudaMemcpyDeviceToDevice));
+    return CRG_OK;
+}
+
+// cr::registry::register_model (registry.cpp:51-97) for a scene that already
+// exists: the model's triangles are appended to the scene's arrays (its
+// material indices rebased onto the appended materials) and it gets its own
+// BVH region; only its BVH is built by the next crg_scene_build.  fill(d_verts,
+// d_uvs, box, areas) writes the model's de-indexed vertices (and texture
+// coordinates when d_uvs is not null), its object box and its triangle areas.
+// The scene is left unchanged when a step fails.
+template <class Fill>
+crg_status append_model(crg_scene *s, uint32_t ntri, const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
+                        uint32_t *model, Fill &&fill, bool model_uv) {
+    crg_context *ctx = s->ctx;
+    if (ntri > 0 && (!mat_idx || !mats || nmat == 0))
+        return set_error(ctx, CRG_ERR_INVALID_ARG, "triangles need mat_idx and a non-empty material table");
+    if ((uint64_t)s->ntri + ntri > (1u << 30)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 2^30 triangles");
+    if (s->models.size() >= (1u << 16)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 65536 models");
+    for (uint32_t p = 0; p < ntri; ++p)
+        if (mat_idx[p] >= nmat) return set_error(ctx, CRG_ERR_INVALID_ARG, "material index out of range");
+    for (uint32_t m = 0; m < nmat; ++m)
+        if (mats[m].shade_type > CRG_SHADE_GLASS) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad shade_type");
+    const uint32_t n0 = s->ntri, m0 = s->nmat, n1 = n0 + ntri, m1 = m0 + nmat;
+    const bool uv = s->uvs.ptr != nullptr || model_uv;
+    DevBuf verts, uvs, midx, dmats;
+    std::vector<uint32_t> shifted(mat_idx, mat_idx + ntri);
+    for (uint32_t &k : shifted) k += m0;
+    crg_model_rec rec;
+    rec.first = n0;
+    rec.ntri = ntri;
+    rec.node_base = 0;
+    for (const crg_model_rec &m : s->models) rec.node_base = std::max(rec.node_base, m.node_base + m.node_cap);
+    rec.node_cap = ntri >= 2 ? ntri - 1 : 1;
+    std::vector<double> areas;
+    crg_status rc = copy_grow(ctx, s->verts, sizeof(float) * 9 * (size_t)n0, sizeof(float) * 9 * (size_t)std::max(n1, 1u), verts);
+    if (rc == CRG_OK && uv) {
+        rc = copy_grow(ctx, s->uvs, s->uvs.ptr ? sizeof(float) * 6 * (size_t)n0 : 0, sizeof(float) * 6 * (size_t)std::max(n1, 1u), uvs);
+        if (rc == CRG_OK && !s->uvs.ptr && n0) {
+            const cudaError_t e = cudaMemset(uvs.ptr, 0, sizeof(float) * 6 * (size_t)n0);
+            if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemset(uvs)");
+        }
+    }
+    if (rc == CRG_OK) rc = copy_grow(ctx, s->mat_idx, sizeof(uint32_t) * n0, sizeof(uint32_t) * std::max(n1, 1u), midx);
+    if (rc == CRG_OK) rc = copy_grow(ctx, s->mats, sizeof(crg_material) * m0, sizeof(crg_material) * std::max(m1, 1u), dmats);
+    if (rc == CRG_OK && ntri) {
+        const cudaError_t e = cudaMemcpy((uint32_t *)midx.ptr + n0, shifted.data(), sizeof(uint32_t) * ntri, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(mat_idx)");
+    }
+    if (rc == CRG_OK && nmat) {
+        const cudaError_t e = cudaMemcpy((crg_material *)dmats.ptr + m0, mats, sizeof(crg_material) * nmat, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaMemcpy(materials)");
+    }
+    if (rc == CRG_OK) rc = fill((float *)verts.ptr + 9 * (size_t)n0, uv ? (float *)uvs.ptr + 6 * (size_t)n0 : nullptr, rec.box, areas);
+    if (rc != CRG_OK) {
+        dev_free(verts);
+        dev_free(uvs);
+        dev_free(midx);
+        dev_free(dmats);
+        return rc;
+    }
+    dev_free(s->verts);
+    s->verts = verts;
+    if (uv) {
+        dev_free(s->uvs);
+        s->uvs = uvs;
+    }
+    dev_free(s->mat_idx);
+    s->mat_idx = midx;
+    dev_free(s->mats);
+    s->mats = dmats;
+    s->host_mat_idx.insert(s->host_mat_idx.end(), shifted.begin(), shifted.end());
+    s->host_mats.insert(s->host_mats.end(), mats, mats + nmat);
+    s->tri_area.insert(s->tri_area.end(), areas.begin(), areas.end());
+    s->models.push_back(rec);
+    s->ntri = n1;
+    s->nmat = m1;
+    s->built = false;
+    if (model) *model = (uint32_t)(s->models.size() - 1);
+    rc = update_placements(s);
+    if (rc == CRG_OK) rc = prepare_lights(s);
+    return rc;
 }
 
 crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat,
@@ -311,13 +602,19 @@ crg_status scene_common(crg_context *ctx, uint32_t ntri, const uint32_t *mat_idx
         if (mat_idx[p] >= nmat) return set_error(ctx, CRG_ERR_INVALID_ARG, "material index out of range");
     for (uint32_t m = 0; m < nmat; ++m)
         if (mats[m].shade_type > CRG_SHADE_GLASS) return set_error(ctx, CRG_ERR_INVALID_ARG, "bad shade_type");
-    s = new (std::nothrow) crg_scene();
-    if (!s) return set_error(ctx, CRG_ERR_OOM, "host allocation failed");
+    s = fault_injected() ? nullptr : new (std::nothrow) crg_scene();
+    if (!s) return set_error(ctx, CRG_ERR_OOM, "host allocation of the scene failed");
     s->ctx = ctx;
     s->ntri = ntri;
     s->nmat = nmat;
     s->host_mats.assign(mats, mats + nmat);
     s->host_mat_idx.assign(mat_idx, mat_idx + ntri);
+    crg_model_rec m0;
+    m0.first = 0;
+    m0.ntri = ntri;
+    m0.node_base = 0;
+    m0.node_cap = ntri >= 2 ? ntri - 1 : 1;
+    s->models.push_back(m0);
     apply_sun(s, default_sun());
     s->sun_enabled = 0;
     crg_status rc;
@@ -337,7 +634,8 @@ void scene_free(crg_scene *s) {
     if (!s) return;
     DevBuf *bufs[] = {&s->verts, &s->mat_idx, &s->mats, &s->light_prim, &s->light_alias, &s->light_pdf, &s->mat_light_pdf,
                       &s->sky, &s->bvh2, &s->order, &s->wide, &s->tris, &s->err, &s->counters, &s->qhead,
-                      &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst, &s->light_rec};
+                      &s->uvs, &s->texels, &s->tex_info, &s->inst, &s->light_inst, &s->light_rec,
+                      &s->inst_root, &s->tlas};
     for (DevBuf *b : bufs) dev_free(*b);
     delete s;
 }
@@ -354,6 +652,18 @@ using namespace crg;
 extern "C" {
 
 uint32_t crg_abi_version(void) { return CRG_ABI_VERSION; }
+
+crg_status crg_debug_fail_allocation(int64_t nth) {
+    g_fault_countdown.store(nth < 0 ? -1 : nth, std::memory_order_relaxed);
+    return CRG_OK;
+}
+
+crg_status crg_debug_allocation_stats(uint64_t *allocations, uint32_t *injected, int64_t *armed) {
+    if (allocations) *allocations = g_alloc_seen.load(std::memory_order_relaxed);
+    if (injected) *injected = g_fault_fired.load(std::memory_order_relaxed);
+    if (armed) *armed = g_fault_countdown.load(std::memory_order_relaxed);
+    return CRG_OK;
+}
 
 const char *crg_status_string(crg_status s) {
     switch (s) {
@@ -379,10 +689,13 @@ crg_status crg_context_create(int device, crg_context **out) {
         return e != cudaSuccess ? CRG_ERR_CUDA : CRG_ERR_INVALID_ARG;
     }
     if ((e = cudaSetDevice(device)) != cudaSuccess) return CRG_ERR_CUDA;
-    crg_context *ctx = new (std::nothrow) crg_context();
+    crg_context *ctx = fault_injected() ? nullptr : new (std::nothrow) crg_context();
     if (!ctx) return CRG_ERR_OOM;
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    // crg_build_bvh_noalloc's scratch array: its module is loaded and its address
+    // looked up here, so that the no-allocation build itself loads nothing
+    noalloc_prepare();
     *out = ctx;
     return CRG_OK;
 }
@@ -408,6 +721,7 @@ crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr) {
     if (!ctx || !dptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
     *dptr = nullptr;
     if (bytes == 0) return CRG_OK;
+    if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "crg_device_alloc failed (injected fault)");
     CRG_CUDA(ctx, cudaMalloc(dptr, bytes));
     return CRG_OK;
 }
@@ -434,6 +748,7 @@ crg_status crg_host_alloc(crg_context *ctx, size_t bytes, void **hptr) {
     if (!ctx || !hptr) return set_error(ctx, CRG_ERR_INVALID_ARG, "null argument");
     *hptr = nullptr;
     if (bytes == 0) return CRG_OK;
+    if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "crg_host_alloc failed (injected fault)");
     CRG_CUDA(ctx, cudaHostAlloc(hptr, bytes, cudaHostAllocDefault));
     return CRG_OK;
 }
@@ -469,6 +784,7 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
     }
     if (rc == CRG_OK) {
         compute_areas(s, verts);
+        mesh_box(verts, ntri, s->models[0].box);
         rc = prepare_lights(s);
     }
     if (rc != CRG_OK) {
@@ -524,9 +840,18 @@ crg_status crg_scene_create_indexed(crg_context *ctx, const float *positions, ui
         // emitter areas from the same float positions the device copied
         float tv[9];
         s->tri_area.assign(ntri, 0.0);
+        float *box = s->models[0].box;
+        for (int a = 0; a < 3; ++a) {
+            box[a] = ntri ? INFINITY : 0.0f;
+            box[3 + a] = ntri ? -INFINITY : 0.0f;
+        }
         for (uint32_t p = 0; p < ntri; ++p) {
             for (int k = 0; k < 3; ++k)
-                for (int a = 0; a < 3; ++a) tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
+                for (int a = 0; a < 3; ++a) {
+                    tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
+                    box[a] = std::min(box[a], tv[3 * k + a]);
+                    box[3 + a] = std::max(box[3 + a], tv[3 * k + a]);
+                }
             s->tri_area[p] = tri_area_of(tv);
         }
         rc = prepare_lights(s);
@@ -560,6 +885,7 @@ crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint3
     }
     if (rc == CRG_OK) {
         compute_areas(s, hv.data());
+        mesh_box(hv.data(), ntri, s->models[0].box);
         rc = prepare_lights(s);
     }
     if (rc != CRG_OK) {
@@ -649,36 +975,139 @@ crg_status crg_scene_set_instances(crg_scene *scene, const float *xforms, uint32
     crg_context *ctx = scene->ctx;
     if (ninst > 0 && !xforms) return set_error(ctx, CRG_ERR_INVALID_ARG, "null transform array");
     if (ninst > (1u << 16)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 65536 instances");
-    std::vector<float> rows(24 * (size_t)ninst);
+    float rows[24];
     for (uint32_t j = 0; j < ninst; ++j)
-        if (!instance_rows(xforms + 16 * (size_t)j, &rows[24 * (size_t)j]))
+        if (!instance_rows(xforms + 16 * (size_t)j, rows))
             return set_error(ctx, CRG_ERR_INVALID_ARG, "instance transform is not an invertible affine matrix");
-    // emitter copies are weighed by their world areas: the vertices come back to the host once
-    std::vector<float> hv((size_t)scene->ntri * 9);
-    if (ninst && scene->ntri)
-        CRG_CUDA(ctx, cudaMemcpy(hv.data(), scene->verts.ptr, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost));
-    dev_free(scene->inst);
-    dev_free(scene->light_inst);
-    scene->ninst = 0;
-    scene->host_xf.assign(xforms, xforms + 16 * (size_t)ninst);
-    scene->host_rows = rows;
-    scene->inst_area.clear();
-    if (ninst) {
-        crg_status rc = dev_alloc(ctx, scene->inst, sizeof(float) * rows.size());
+    for (crg_model_rec &m : scene->models) m.xf.assign(xforms, xforms + 16 * (size_t)ninst);
+    crg_status rc = update_placements(scene);
+    if (rc == CRG_OK) rc = prepare_lights(scene);
+    return rc;
+}
+
+crg_status crg_scene_set_model_instances(crg_scene *scene, uint32_t model, const float *xforms, uint32_t ninst) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scene->ctx;
+    if (model >= scene->models.size()) return set_error(ctx, CRG_ERR_INVALID_ARG, "model index out of range");
+    if (ninst > 0 && !xforms) return set_error(ctx, CRG_ERR_INVALID_ARG, "null transform array");
+    if (ninst > (1u << 16)) return set_error(ctx, CRG_ERR_INVALID_ARG, "more than 65536 instances");
+    float rows[24];
+    for (uint32_t j = 0; j < ninst; ++j)
+        if (!instance_rows(xforms + 16 * (size_t)j, rows))
+            return set_error(ctx, CRG_ERR_INVALID_ARG, "instance transform is not an invertible affine matrix");
+    scene->models[model].xf.assign(xforms, xforms + 16 * (size_t)ninst);
+    crg_status rc = update_placements(scene);
+    if (rc == CRG_OK) rc = prepare_lights(scene);
+    return rc;
+}
+
+crg_status crg_scene_add_model(crg_scene *scene, const float *verts, uint32_t ntri, const float *uvs,
+                               const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat, uint32_t *model) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (ntri > 0 && !verts) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null vertex array");
+    return append_model(scene, ntri, mat_idx, mats, nmat, model,
+                        [&](float *d_verts, float *d_uvs, float *box, std::vector<double> &areas) {
+        cudaError_t e = cudaSuccess;
+        if (ntri) e = cudaMemcpy(d_verts, verts, sizeof(float) * 9 * (size_t)ntri, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && d_uvs && ntri) {
+            if (uvs) e = cudaMemcpy(d_uvs, uvs, sizeof(float) * 6 * (size_t)ntri, cudaMemcpyHostToDevice);
+            else e = cudaMemset(d_uvs, 0, sizeof(float) * 6 * (size_t)ntri);
+        }
+        if (e != cudaSuccess) return cuda_error(scene->ctx, e, "cudaMemcpy(model)");
+        areas.resize(ntri);
+        for (uint32_t p = 0; p < ntri; ++p) areas[p] = tri_area_of(verts + (size_t)p * 9);
+        mesh_box(verts, ntri, box);
+        return CRG_OK;
+    }, uvs != nullptr);
+}
+
+crg_status crg_scene_add_model_indexed(crg_scene *scene, const float *positions, uint32_t npos,
+                                       const uint32_t *vertex_indices, uint32_t ntri, const float *texcoords, uint32_t ntc,
+                                       const int32_t *tex_indices, const uint32_t *mat_idx, const crg_material *mats,
+                                       uint32_t nmat, uint32_t *model) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    crg_context *ctx = scene->ctx;
+    if (ntri > 0 && (!positions || !vertex_indices)) return set_error(ctx, CRG_ERR_INVALID_ARG, "null positions or indices");
+    if (ntc > 0 && !texcoords) return set_error(ctx, CRG_ERR_INVALID_ARG, "null texture coordinates");
+    for (size_t c = 0; c < 3 * (size_t)ntri; ++c)
+        if (vertex_indices[c] >= npos) return set_error(ctx, CRG_ERR_INVALID_ARG, "vertex index out of range");
+    const bool want_uv = tex_indices != nullptr;
+    return append_model(scene, ntri, mat_idx, mats, nmat, model,
+                        [&](float *d_verts, float *d_uvs, float *box, std::vector<double> &areas) {
+        if (ntri == 0) return CRG_OK;
+        const size_t nc = 3 * (size_t)ntri;
+        DevBuf dpos, didx, dtc, dti;
+        crg_status rc = dev_alloc(ctx, dpos, sizeof(float) * 3 * (size_t)npos);
+        if (rc == CRG_OK) rc = dev_alloc(ctx, didx, sizeof(uint32_t) * nc);
+        if (rc == CRG_OK && d_uvs && want_uv) rc = dev_alloc(ctx, dti, sizeof(int32_t) * nc);
+        if (rc == CRG_OK && d_uvs && want_uv && ntc) rc = dev_alloc(ctx, dtc, sizeof(float) * 2 * (size_t)ntc);
+        cudaError_t e = cudaSuccess;
+        if (rc == CRG_OK) e = cudaMemcpy(dpos.ptr, positions, sizeof(float) * 3 * (size_t)npos, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess) e = cudaMemcpy(didx.ptr, vertex_indices, sizeof(uint32_t) * nc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess && dti.ptr)
+            e = cudaMemcpy(dti.ptr, tex_indices, sizeof(int32_t) * nc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess && dtc.ptr)
+            e = cudaMemcpy(dtc.ptr, texcoords, sizeof(float) * 2 * (size_t)ntc, cudaMemcpyHostToDevice);
+        if (rc == CRG_OK && e == cudaSuccess) {
+            const unsigned blocks = (unsigned)std::min<size_t>((nc + 255) / 256, (size_t)std::max(ctx->sm_count, 1) * 8);
+            k_expand<<<blocks, 256>>>((const float *)dpos.ptr, (const uint32_t *)didx.ptr, (const float *)dtc.ptr,
+                                      (const int32_t *)dti.ptr, dtc.ptr ? ntc : 0, d_verts, d_uvs, nc);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        }
+        dev_free(dpos);
+        dev_free(didx);
+        dev_free(dtc);
+        dev_free(dti);
         if (rc != CRG_OK) return rc;
-        CRG_CUDA(ctx, cudaMemcpy(scene->inst.ptr, rows.data(), sizeof(float) * rows.size(), cudaMemcpyHostToDevice));
-        scene->ninst = ninst;
-        instance_areas(scene, hv.data());
-    }
-    return prepare_lights(scene);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "k_expand(model)");
+        float tv[9];
+        for (int a = 0; a < 3; ++a) {
+            box[a] = INFINITY;
+            box[3 + a] = -INFINITY;
+        }
+        for (uint32_t p = 0; p < ntri; ++p) {
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
+                    box[a] = std::min(box[a], tv[3 * k + a]);
+                    box[3 + a] = std::max(box[3 + a], tv[3 * k + a]);
+                }
+            areas.push_back(tri_area_of(tv));
+        }
+        return CRG_OK;
+    }, want_uv);
+}
+
+crg_status crg_scene_model_count(const crg_scene *scene, uint32_t *count) {
+    if (!scene || !count) return CRG_ERR_INVALID_ARG;
+    *count = (uint32_t)scene->models.size();
+    return CRG_OK;
+}
+
+crg_status crg_scene_model_info(const crg_scene *scene, uint32_t model, crg_model_info *info) {
+    if (!scene || !info) return CRG_ERR_INVALID_ARG;
+    if (model >= scene->models.size()) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "model index out of range");
+    const crg_model_rec &m = scene->models[model];
+    *info = crg_model_info{};
+    info->first_prim = m.first;
+    info->ntri = m.ntri;
+    info->node_base = m.node_base;
+    info->n_wide_nodes = m.built ? m.n_wide : 0;
+    info->depth = m.built ? m.depth : 0;
+    info->ninst = (uint32_t)(m.xf.size() / 16);
+    info->built = m.built ? 1u : 0u;
+    info->sah_cost = m.built ? m.sah : 0.0f;
+    return CRG_OK;
 }
 
 crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info) {
     if (!scene || !info) return CRG_ERR_INVALID_ARG;
     if (!scene->built) return CRG_ERR_NOT_BUILT;
+    const bool one = scene->models.size() == 1;
     info->ntri = scene->ntri;
     info->width = scene->width;
-    info->n_bvh2_nodes = scene->ntri >= 2 ? scene->ntri - 1 : 0;
+    info->n_bvh2_nodes = one ? (scene->ntri >= 2 ? scene->ntri - 1 : 0) : scene->node_cap;
     info->n_wide_nodes = scene->n_wide;
     info->node_bytes = scene->node_bytes;
     info->n_tri_slots = scene->ntri;
@@ -695,7 +1124,8 @@ crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t 
     crg_context *ctx = scene->ctx;
     const uint32_t n = scene->ntri;
     if (n == 0) return CRG_OK;
-    if (bvh2 && n >= 2) CRG_CUDA(ctx, cudaMemcpy(bvh2, scene->bvh2.ptr, sizeof(float) * 8 * (size_t)(n - 1), cudaMemcpyDeviceToHost));
+    const size_t n2 = scene->models.size() == 1 ? (n >= 2 ? n - 1 : 0) : scene->node_cap;
+    if (bvh2 && n2) CRG_CUDA(ctx, cudaMemcpy(bvh2, scene->bvh2.ptr, sizeof(float) * 8 * n2, cudaMemcpyDeviceToHost));
     if (order) CRG_CUDA(ctx, cudaMemcpy(order, scene->order.ptr, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
     if (wide) CRG_CUDA(ctx, cudaMemcpy(wide, scene->wide.ptr, (size_t)scene->node_bytes * scene->n_wide, cudaMemcpyDeviceToHost));
     if (tris) CRG_CUDA(ctx, cudaMemcpy(tris, scene->tris.ptr, sizeof(float) * 12 * (size_t)n, cudaMemcpyDeviceToHost));
@@ -741,8 +1171,8 @@ crg_status crg_film_create(crg_context *ctx, uint32_t width, uint32_t height, ui
     *out = nullptr;
     if (width == 0 || height == 0 || (uint64_t)width * height > (1ull << 31))
         return set_error(ctx, CRG_ERR_INVALID_ARG, "film size must be positive and at most 2^31 pixels");
-    crg_film *f = new (std::nothrow) crg_film();
-    if (!f) return set_error(ctx, CRG_ERR_OOM, "host allocation failed");
+    crg_film *f = fault_injected() ? nullptr : new (std::nothrow) crg_film();
+    if (!f) return set_error(ctx, CRG_ERR_OOM, "host allocation of the film failed");
     f->ctx = ctx;
     f->width = width;
     f->height = height;

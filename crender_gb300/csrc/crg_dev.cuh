@@ -241,9 +241,11 @@ struct Trav {
     bool occluded;
 };
 
-__device__ __forceinline__ void trav_init(Trav &T, const RayPre &r, float tmax) {
+// `root` is the node index of the BVH's root: 0 for a scene of one model, the
+// model's first node for a model of a multi-model scene.
+__device__ __forceinline__ void trav_init(Trav &T, const RayPre &r, float tmax, uint32_t root = 0u) {
     T.oct = (r.dx < 0.0f ? 4u : 0u) | (r.dy < 0.0f ? 2u : 0u) | (r.dz < 0.0f ? 1u : 0u);
-    T.ng = make_uint2(0u, (1u << (24 + (0u ^ T.oct))) | 1u); // the root as child code 0 of a virtual parent
+    T.ng = make_uint2(root, (1u << (24 + (0u ^ T.oct))) | 1u); // the root as child code 0 of a virtual parent
     T.tg = make_uint2(0u, 0u);
     T.sp = 0;
     T.best_t = tmax;
@@ -398,10 +400,10 @@ template <int W, bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                          const RayPre &r, float tmax, float &best_t, uint32_t &best_prim,
                                          uint32_t &best_slot, float &best_u, float &best_v, bool &occluded,
-                                         TravStats &st, uint32_t &err) {
+                                         TravStats &st, uint32_t &err, uint32_t root = 0u) {
     Trav T;
     uint2 stack[kStack];
-    trav_init(T, r, tmax);
+    trav_init(T, r, tmax, root);
     while (!trav_step<W, ANY, COUNT>(T, stack, nodes, tris, r, 1 << 30, st, err)) {
     }
     best_t = T.best_t;

@@ -32,6 +32,21 @@ struct crg_context {
     std::map<std::string, Tuned> tune_cache; // autotuner results by batch shape
 };
 
+// One model of a scene (cr::registry::register_model, src/render/entities/registry.cpp:51-97):
+// a contiguous range of the scene's primitives with its own BVH (BLAS) and its
+// own instance list (cr::entity::instances::transforms, components.h:18-21).
+struct crg_model_rec {
+    uint32_t first = 0, ntri = 0; // primitives [first, first + ntri) of the scene arrays
+    uint32_t node_base = 0;       // first node of its BVH in the scene's node arrays
+    uint32_t node_cap = 1;        // nodes reserved for it: max(1, ntri - 1)
+    bool built = false;           // its BVH is current for the scene's build options
+    uint32_t n_wide = 0, depth = 0;
+    float sah = 0.0f;
+    float box[6] = {0, 0, 0, 0, 0, 0}; // object-space bounds of its vertices (lo.xyz, hi.xyz)
+    std::vector<float> xf;        // 16 floats per instance as given; empty = one identity instance
+                                  // (the mesh as is when the scene has this one model only)
+};
+
 struct crg_scene {
     crg_context *ctx = nullptr;
     uint32_t ntri = 0;
@@ -47,14 +62,24 @@ struct crg_scene {
     DevBuf texels;    // float4 texels of all textures, concatenated
     DevBuf tex_info;  // uint4 per texture: {first texel (low 32 bits), first texel (high 32 bits), width, height}
     uint32_t ntex = 0;
-    // instances (cr::entity::instances::transforms): 4x4 column-major affine
-    // transforms as given, and per instance 6 float4 rows (inverse, forward)
+    // models (at least one; model 0 holds the triangles the scene was created with)
+    std::vector<crg_model_rec> models;
+    // placements: every (model, instance) pair in model order then instance
+    // order, the order in which cr::scene::cast_ray and cr::model::intersect
+    // visit them (scene.cpp:79-98, model.cpp:99-126).  ninst = 0 when the scene
+    // is one model without an instance list: the mesh is traced as is.
     uint32_t ninst = 0;
-    std::vector<float> host_xf;   // 16 floats per instance
-    std::vector<float> host_rows; // 24 floats per instance (the device layout)
-    std::vector<double> inst_area; // world area of triangle p under instance j at [j * ntri + p]
+    std::vector<float> host_xf;   // 16 floats per placement (identity for a model without a list)
+    std::vector<float> host_rows; // 24 floats per placement (the device layout)
+    std::vector<uint32_t> place_model; // model of each placement
+    std::vector<double> inst_area; // world area of each placement's triangles, placement-major
+    std::vector<size_t> inst_area_off; // first inst_area entry of each placement
     DevBuf inst;       // float4[6 * ninst]
-    DevBuf light_inst; // uint32 per emitter entry (instanced scenes)
+    DevBuf inst_root;  // uint32 per placement: node index of its model's BVH root
+    DevBuf tlas;       // float4[4] per top-level node over the placements' world boxes
+    uint32_t tlas_root = 0; // top-level root: node index, or kTlasLeaf | placement
+    uint32_t tlas_nodes = 0;
+    DevBuf light_inst; // uint32 per emitter entry (instanced scenes): its placement
     // emissive triangles (power-weighted alias table)
     uint32_t nlights = 0;
     std::vector<double> tri_area; // per-triangle area (host), for rebuilding the emitter table
@@ -73,10 +98,11 @@ struct crg_scene {
     crg_build_opts opts{8, 0, 3, 3};
     uint32_t width = 8, node_bytes = 80, n_wide = 0, depth = 0;
     float sah = 0.0f;
-    DevBuf bvh2;   // float4[2*(ntri-1)]
-    DevBuf order;  // uint32[ntri]
-    DevBuf wide;   // node_bytes * n_wide_capacity
-    DevBuf tris;   // float4[3*ntri]
+    uint32_t node_cap = 0; // sum of the models' node_cap: the node arrays' length
+    DevBuf bvh2;   // float4[2*node_cap]: each model's binary LBVH at 2 * node_base, model-local indices
+    DevBuf order;  // uint32[ntri]: each model's sorted primitive order at first, model-local indices
+    DevBuf wide;   // node_bytes * node_cap: each model's wide BVH at node_base (indices scene-global)
+    DevBuf tris;   // float4[3*ntri]: each model's triangle slots at first (primitive ids scene-global)
     DevBuf err;    // uint32 device error word
     DevBuf qhead;  // uint32 work counter of the persistent query kernels
     // statistics
@@ -97,13 +123,26 @@ struct crg_film {
 
 namespace crg {
 
+// Allocation fault injection (crg_debug_fail_allocation): true when the
+// allocation about to be made must fail as if the device or host were out of
+// memory.  Every allocation site of the library asks once per allocation.
+bool fault_injected();
+
 crg_status set_error(crg_context *ctx, crg_status s, const std::string &msg);
 crg_status cuda_error(crg_context *ctx, cudaError_t e, const char *what);
 crg_status dev_alloc(crg_context *ctx, DevBuf &b, size_t bytes);
 void dev_free(DevBuf &b);
 
 // bvh_build.cu
+// Builds the BVH of every model that is not built for options o (all of them
+// when o differs from the scene's current options).
 crg_status build_bvh(crg_scene *s, const crg_build_opts &o, cudaStream_t stream);
+// Looks the no-allocation build's scratch array up on the current device
+// (called once per context so that crg_build_bvh_noalloc never loads anything).
+void noalloc_prepare();
+
+// top-level tree over a scene's placements (crg_api.cu)
+constexpr uint32_t kTlasLeaf = 0x80000000u;
 
 // traverse.cu
 crg_status launch_intersect(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,

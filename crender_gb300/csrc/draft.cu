@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(128) k_draft(SceneDev S, CamDev cam, uint32_t 
     const float zn = cam.mode == CRG_CAMERA_ORTHOGRAPHIC ? 0.01f : 0.1f;
     PathCtx C{pix, 0, 0, 0, 0, 0, 0ull, 0ull};
     Hit h;
-    const bool found = cz > 0.0f && closest_t<W, false>(S, o, d, zn / cz, 10000.0f / cz, h, C);
+    const bool found = cz > 0.0f && closest_t<W, false, true>(S, o, d, zn / cz, 10000.0f / cz, h, C);
     float4 c;
     if (found) {
         const HitGeom g = hit_geom<false>(S, h, o, d);

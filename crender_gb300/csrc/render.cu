@@ -55,7 +55,9 @@ namespace {
 // MINB blocks of 128 threads per SM: 5 (96 registers, some spilled) when the grid fills the
 // GPU at that occupancy, else 4 (no spills: a grid below one wave gains nothing from the
 // extra warps and loses the spill traffic).
-template <int W, int MODE, bool CNT, int MINB>
+// INST: the scene is traced through its placements (models and instances);
+// kernels for plain one-mesh scenes are compiled without that code.
+template <int W, int MODE, bool CNT, int MINB, bool INST>
 __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, crg_settings set, FilmDev F, uint64_t spp0) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
@@ -93,11 +95,11 @@ __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, cr
             if (i < set.max_bounces) {
                 Hit h;
                 C.segments++;
-                const bool found = closest<W, CNT>(S, ps.o, ps.d, INFINITY, h, C);
+                const bool found = closest<W, CNT, INST>(S, ps.o, ps.d, INFINITY, h, C);
                 NeeReq nr;
                 const bool cont = MODE == CRG_MODE_EXTENDED ? shade_extended(S, set, C, i, ps, found, h, aov, nr)
                                                             : shade_faithful(S, set, C, i, ps, found, h, aov, nr);
-                if (nr.kind != 0 && shadow_visible<W, CNT>(S, nr, C)) ps.L = add(ps.L, nr.c);
+                if (nr.kind != 0 && shadow_visible<W, CNT, INST>(S, nr, C)) ps.L = add(ps.L, nr.c);
                 ++i;
                 if (cont && i < set.max_bounces) continue;
             }
@@ -148,16 +150,16 @@ __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, cr
     }
 }
 
-template <int W, int MINB>
+template <int W, int MINB, bool INST>
 void launch_m(const SceneDev &S, const CamDev &cam, const crg_settings &set, const FilmDev &F, uint64_t spp0,
               uint32_t blocks, cudaStream_t st) {
     const uint32_t T = 128;
     if (S.counters) {
-        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, true, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-        else k_render<W, CRG_MODE_FAITHFUL, true, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, true, MINB, INST><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, true, MINB, INST><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
     } else {
-        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, false, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
-        else k_render<W, CRG_MODE_FAITHFUL, false, MINB><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        if (set.mode == CRG_MODE_EXTENDED) k_render<W, CRG_MODE_EXTENDED, false, MINB, INST><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
+        else k_render<W, CRG_MODE_FAITHFUL, false, MINB, INST><<<blocks, T, 0, st>>>(S, cam, set, F, spp0);
     }
 }
 
@@ -166,8 +168,9 @@ void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, con
               int sm_count, cudaStream_t st) {
     const uint64_t npix = (uint64_t)set.width * set.height;
     const uint32_t blocks = (uint32_t)((npix + 127) / 128);
-    if ((uint64_t)blocks >= 5ull * (uint64_t)(sm_count > 0 ? sm_count : 1)) launch_m<W, 5>(S, cam, set, F, spp0, blocks, st);
-    else launch_m<W, 4>(S, cam, set, F, spp0, blocks, st);
+    if (S.ninst) launch_m<W, 4, true>(S, cam, set, F, spp0, blocks, st); // placements: one variant
+    else if ((uint64_t)blocks >= 5ull * (uint64_t)(sm_count > 0 ? sm_count : 1)) launch_m<W, 5, false>(S, cam, set, F, spp0, blocks, st);
+    else launch_m<W, 4, false>(S, cam, set, F, spp0, blocks, st);
 }
 
 } // namespace
@@ -229,6 +232,9 @@ SceneDev scene_dev(const crg_scene *s) {
     S.tex_info = (const uint4 *)s->tex_info.ptr;
     S.ntex = s->texels.ptr ? s->ntex : 0;
     S.inst = (const float4 *)s->inst.ptr;
+    S.inst_root = (const uint32_t *)s->inst_root.ptr;
+    S.tlas = (const float4 *)s->tlas.ptr;
+    S.tlas_root = s->tlas_root;
     S.light_inst = (const uint32_t *)s->light_inst.ptr;
     S.light_rec = (const float4 *)s->light_rec.ptr;
     S.ninst = s->inst.ptr ? s->ninst : 0;

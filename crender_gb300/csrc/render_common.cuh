@@ -35,6 +35,9 @@ struct SceneDev {
     // instance 6 float4 rows: the inverse (3 rows of [A | t]) then the forward
     // transform; ninst = 0 means the mesh is used as is
     const float4 *inst;
+    const uint32_t *inst_root;  // per placement: node index of its model's BVH root
+    const float4 *tlas;         // top-level tree over the placements (4 float4 per node)
+    uint32_t tlas_root;         // its root: a node index, or kTlasLeaf | placement
     const uint32_t *light_inst; // instance of each emitter entry (instanced scenes)
     // per emitter entry 4 float4: (v0, pdf), (v1, prim bits), (v2, material bits), (colour * emission,
     // textured flag bits); v0..v2 in world space
@@ -74,9 +77,9 @@ struct Hit {
 
 struct PathCtx;
 
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C);
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C);
 
 __device__ __forceinline__ void slot_verts(const SceneDev &S, uint32_t slot, v3 &a, v3 &b, v3 &c) {
@@ -201,39 +204,174 @@ __device__ __forceinline__ float vdist(v3 a, v3 b) {
 // of the reference's loop over instances.
 constexpr float kInstSlack = 1.0001f;
 
-// Closest hit with tmin < t (object space for instances, as the reference's
-// tnear) and world distance below tmax.
+// ------------------------------------------------------------------ top level
+// Placements are the (model, instance) pairs of a scene in the order
+// cr::scene::cast_ray and cr::model::intersect visit them (scene.cpp:79-98,
+// model.cpp:99-126).  A binary tree over their world boxes (built on the
+// host, 4 float4 per node: {lo_a, ref_a}, {hi_a, ref_b}, {lo_b, -}, {hi_b, -})
+// orders and prunes them; the result is the reference loop's: the smallest
+// world distance, ties to the earlier placement.  A subtree is skipped only
+// when its box entry lies beyond the best distance by more than a generous
+// margin (1e-3 relative plus 1e-3 of the origin's magnitude), far above the
+// rounding of the world points, so pruning never changes the answer.
+constexpr int kTlasStack = 48;
+
+struct TlasRay {
+    v3 o, inv;
+    float dl;     // |d|
+    float margin; // world-space widening of every box: 1e-4 of the origin's magnitude
+    float slack;  // absolute slack of the pruning test: 1e-3 of the origin's magnitude (at least 1e-3)
+    bool ahead;   // tmin >= 0: boxes wholly behind the origin cannot hold a hit
+};
+__device__ __forceinline__ TlasRay tlas_ray(v3 o, v3 d, float tmin) {
+    TlasRay t;
+    t.o = o;
+    const float tiny = 8.27180613e-25f; // 2^-80
+    t.inv = mk(1.0f / (fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x), 1.0f / (fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y),
+               1.0f / (fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z));
+    t.dl = sqrtf(dot(d, d));
+    const float om = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    t.margin = 1e-4f * om;
+    t.slack = 1e-3f * (om + 1.0f);
+    t.ahead = tmin >= 0.0f;
+    return t;
+}
+// Entry parameter of the ray into a box widened by the margin, or +inf when it
+// misses it (or, for tmin >= 0, when the box lies wholly behind the origin).
+__device__ __forceinline__ float tlas_entry(const TlasRay &t, float4 lo, float4 hi) {
+    const float m = t.margin;
+    const float x0 = ((lo.x - m) - t.o.x) * t.inv.x, x1 = ((hi.x + m) - t.o.x) * t.inv.x;
+    const float y0 = ((lo.y - m) - t.o.y) * t.inv.y, y1 = ((hi.y + m) - t.o.y) * t.inv.y;
+    const float z0 = ((lo.z - m) - t.o.z) * t.inv.z, z1 = ((hi.z + m) - t.o.z) * t.inv.z;
+    const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+    const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+    if (!(tn <= tf) || (t.ahead && tf < 0.0f)) return INFINITY;
+    return tn;
+}
+// True while a subtree entered at parameter `entry` may still hold a hit whose
+// world distance is at most `best`.
+__device__ __forceinline__ bool tlas_keep(const TlasRay &t, float entry, float best) {
+    return entry * t.dl <= best * 1.001f + t.slack;
+}
+
+// Visits the placements whose boxes the ray may reach, nearest box first;
+// visit(k) returns the current bound (best world distance) after placement k,
+// or a negative value to stop.  Returns false if the stack overflowed.
+template <class Visit>
+__device__ __forceinline__ bool tlas_walk(const SceneDev &S, const TlasRay &t, float bound, Visit &&visit) {
+    uint32_t ref = S.tlas_root;
+    uint32_t stack[kTlasStack];
+    float sent[kTlasStack];
+    int sp = 0;
+    bool ok = true;
+    for (;;) {
+        if (ref & kTlasLeaf) {
+            bound = visit(ref & ~kTlasLeaf);
+            if (bound < 0.0f) return ok;
+        } else {
+            const float4 *n = S.tlas + 4 * (size_t)ref;
+            const float4 la = __ldg(&n[0]), ha = __ldg(&n[1]), lb = __ldg(&n[2]), hb = __ldg(&n[3]);
+            const float ea = tlas_entry(t, la, ha), eb = tlas_entry(t, lb, hb);
+            const bool ka = ea < INFINITY && tlas_keep(t, ea, bound), kb = eb < INFINITY && tlas_keep(t, eb, bound);
+            const uint32_t ra = __float_as_uint(la.w), rb = __float_as_uint(ha.w);
+            if (ka && kb) {
+                const bool a_first = ea <= eb;
+                if (sp < kTlasStack) {
+                    stack[sp] = a_first ? rb : ra;
+                    sent[sp] = a_first ? eb : ea;
+                    sp++;
+                } else {
+                    ok = false;
+                }
+                ref = a_first ? ra : rb;
+                continue;
+            }
+            if (ka || kb) {
+                ref = ka ? ra : rb;
+                continue;
+            }
+        }
+        // pop the next subtree that may still hold a closer hit
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (tlas_keep(t, sent[sp], bound)) {
+                ref = stack[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) return ok;
+    }
+}
+
+// Closest hit over the placements (the reference's loops over models and
+// instances): h.t is the object-space parameter, h.inst the placement.
 template <int W, bool CNT>
+__device__ __forceinline__ void closest_placements(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, Hit &h,
+                                                TravStats &st, uint32_t &err) {
+    const TlasRay tr = tlas_ray(o, d, tmin);
+    float best = tmax;
+    h.prim = 0xFFFFFFFFu;
+    h.inst = kNoInst;
+    const bool ok = tlas_walk(S, tr, tmax, [&](uint32_t k) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, k, o, d, oo, od, len);
+        const float bound = best < INFINITY ? ((best * len) / tr.dl) * kInstSlack : INFINITY;
+        const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+        Hit hk;
+        bool occ;
+        traverse<W, false, CNT>(S.nodes, S.tris, r, bound, hk.t, hk.prim, hk.slot, hk.u, hk.v, occ, st, err,
+                                __ldg(&S.inst_root[k]));
+        if (hk.prim != 0xFFFFFFFFu) {
+            const float dist = vdist(inst_point(S, k, oo, od, hk.t), o);
+            if (dist < best || (dist == best && h.inst != kNoInst && k < h.inst)) {
+                best = dist;
+                h = hk;
+                h.inst = k;
+            }
+        }
+        return best;
+    });
+    if (!ok) err = 1u;
+}
+
+// Any hit over the placements: a placement's hit counts when its object-space
+// parameter is below tmax |inverse(T) d| / |d| (world distance below tmax).
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded_placements(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, TravStats &st,
+                                                 uint32_t &err) {
+    const TlasRay tr = tlas_ray(o, d, tmin);
+    bool occ = false;
+    const bool ok = tlas_walk(S, tr, tmax, [&](uint32_t k) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, k, o, d, oo, od, len);
+        const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+        float t, u, v;
+        uint32_t p, sl;
+        traverse<W, true, CNT>(S.nodes, S.tris, r, (tmax * len) / tr.dl, t, p, sl, u, v, occ, st, err,
+                               __ldg(&S.inst_root[k]));
+        return occ ? -1.0f : tmax;
+    });
+    if (!ok) err = 1u;
+    return occ;
+}
+
+// Closest hit with tmin < t (object space for instances, as the reference's
+// tnear) and world distance below tmax.  INST = false compiles the one-mesh
+// path only (kernels launched for scenes without placements).
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool closest_t(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, Hit &h, PathCtx &C) {
     bool occ;
     TravStats st{0, 0};
-    if (S.ninst == 0) {
+    if (!INST || S.ninst == 0) {
         const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
         traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
         h.inst = kNoInst;
     } else {
-        // model::intersect (model.cpp:99-126): every instance in order, closest
-        // world distance wins, ties to the earlier instance
-        const float dl = sqrtf(dot(d, d));
-        float best = tmax;
-        h.prim = 0xFFFFFFFFu;
-        h.inst = kNoInst;
-        for (uint32_t j = 0; j < S.ninst; ++j) {
-            v3 oo, od;
-            float len;
-            inst_ray(S, j, o, d, oo, od, len);
-            const float bound = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
-            const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
-            Hit hj;
-            traverse<W, false, CNT>(S.nodes, S.tris, r, bound, hj.t, hj.prim, hj.slot, hj.u, hj.v, occ, st, C.err);
-            if (hj.prim == 0xFFFFFFFFu) continue;
-            const float dist = vdist(inst_point(S, j, oo, od, hj.t), o);
-            if (dist < best) {
-                best = dist;
-                h = hj;
-                h.inst = j;
-            }
-        }
+        closest_placements<W, CNT>(S, o, d, tmin, tmax, h, st, C.err);
     }
     if (CNT) {
         C.nodes += st.nodes;
@@ -242,31 +380,24 @@ __device__ __forceinline__ bool closest_t(const SceneDev &S, v3 o, v3 d, float t
     return h.prim != 0xFFFFFFFFu;
 }
 
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool closest(const SceneDev &S, v3 o, v3 d, float tmax, Hit &h, PathCtx &C) {
-    return closest_t<W, CNT>(S, o, d, 1e-5f, tmax, h, C);
+    return closest_t<W, CNT, INST>(S, o, d, 1e-5f, tmax, h, C);
 }
 
-// Any hit with tmin < t < tmax.  Instanced: any instance with a hit whose
+// Any hit with tmin < t < tmax.  Instanced: any placement with a hit whose
 // object-space parameter is below tmax * |inverse(T) d| / |d|.
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool occluded_t(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, PathCtx &C) {
     float t, u, v;
     uint32_t p, sl;
     bool occ = false;
     TravStats st{0, 0};
-    if (S.ninst == 0) {
+    if (!INST || S.ninst == 0) {
         const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
         traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
     } else {
-        const float dl = sqrtf(dot(d, d));
-        for (uint32_t j = 0; j < S.ninst && !occ; ++j) {
-            v3 oo, od;
-            float len;
-            inst_ray(S, j, o, d, oo, od, len);
-            const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
-            traverse<W, true, CNT>(S.nodes, S.tris, r, (tmax * len) / dl, t, p, sl, u, v, occ, st, C.err);
-        }
+        occ = occluded_placements<W, CNT>(S, o, d, tmin, tmax, st, C.err);
     }
     if (CNT) {
         C.nodes += st.nodes;
@@ -275,9 +406,9 @@ __device__ __forceinline__ bool occluded_t(const SceneDev &S, v3 o, v3 d, float 
     return occ;
 }
 
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool occluded(const SceneDev &S, v3 o, v3 d, float tmax, PathCtx &C) {
-    return occluded_t<W, CNT>(S, o, d, 1e-5f, tmax, C);
+    return occluded_t<W, CNT, INST>(S, o, d, 1e-5f, tmax, C);
 }
 
 // Geometry of a closest hit of the ray (o, d): world point, geometric normal,
@@ -720,17 +851,17 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
 
 // The shadow test a NeeReq asks for: kind 1 = any hit below tmax; kind 2 =
 // closest hits stepping 0.1 past alpha-zero surfaces (renderer.cpp:330-345).
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool shadow_visible(const SceneDev &S, const NeeReq &nr, PathCtx &C) {
     if (nr.kind == 1) {
         C.shadow++;
-        return !occluded<W, CNT>(S, nr.o, nr.d, nr.tmax, C);
+        return !occluded<W, CNT, INST>(S, nr.o, nr.d, nr.tmax, C);
     }
     v3 so = nr.o;
     for (;;) {
         Hit sh;
         C.shadow++;
-        if (!closest<W, CNT>(S, so, nr.d, INFINITY, sh, C)) return true;
+        if (!closest<W, CNT, INST>(S, so, nr.d, INFINITY, sh, C)) return true;
         const HitGeom hg = hit_geom<false>(S, sh, so, nr.d);
         if (hit_colour(S, S.mats[__ldg(&S.mat_idx[sh.prim])], sh.prim, sh.slot, hg.ro, hg.rd).w != 0.0f) return false;
         so = add(hg.p, mul(nr.d, 0.1f));

@@ -27,10 +27,10 @@ __global__ void __launch_bounds__(128) k_intersect_inst(rc::SceneDev S, const fl
     const v3 o = mk(r0.x, r0.y, r0.z), d = mk(r1.x, r1.y, r1.z);
     rc::PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
     if (ANY) {
-        occluded[i] = rc::occluded_t<W, false>(S, o, d, r0.w, r1.w, C) ? 1u : 0u;
+        occluded[i] = rc::occluded_t<W, false, true>(S, o, d, r0.w, r1.w, C) ? 1u : 0u;
     } else {
         rc::Hit h;
-        if (rc::closest_t<W, false>(S, o, d, r0.w, r1.w, h, C)) {
+        if (rc::closest_t<W, false, true>(S, o, d, r0.w, r1.w, h, C)) {
             v3 oo, od;
             float len;
             rc::inst_ray(S, h.inst, o, d, oo, od, len);

@@ -172,7 +172,7 @@ __device__ __forceinline__ void finish_and_refill(const Wf &w, Ctrl *c, bool fin
     warp_push(refill, slot, q_out(w, *c), &c->out_count);
 }
 
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
     unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             const float4 o = w.o[slot], d = w.d[slot];
             PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
             Hit h;
-            const bool found = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
+            const bool found = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
             w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), pack_found(found, h.inst));
             if (C.err) atomicOr(&c->error, 1u);
             if (CNT) {
@@ -218,7 +218,7 @@ __device__ __forceinline__ void warp_count(bool want, unsigned int *count) {
 // FUSE 2: closest hit + shade + shadow test (one kernel per bounce)
 // Contributions reach L in the same order in every form: emission of bounce
 // i, its NEE, then bounce i + 1.
-template <int W, int FUSE, bool CNT>
+template <int W, int FUSE, bool CNT, bool INST>
 __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
     unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 float4 h4;
                 if (FUSE >= 2) {
                     Hit hh;
-                    const bool f = closest<W, CNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
+                    const bool f = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
                     h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), pack_found(f, hh.inst));
                 } else {
                     h4 = w.hit[slot];
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
                 shadow = nr.kind != 0;
-                if (FUSE >= 1 && shadow && shadow_visible<W, CNT>(S, nr, C)) ps.L = add(ps.L, nr.c);
+                if (FUSE >= 1 && shadow && shadow_visible<W, CNT, INST>(S, nr, C)) ps.L = add(ps.L, nr.c);
                 if (C.err) atomicOr(&c->error, 1u);
                 if (CNT) {
                     nodes += C.nodes;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
     }
 }
 
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
     unsigned long long nodes = 0, tris = 0;
     Ctrl *c = w.ctrl;
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
                 nr.kind = __float_as_uint(sd.w);
                 PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
                 Lv = w.L[slot];
-                if (shadow_visible<W, CNT>(S, nr, C)) {
+                if (shadow_visible<W, CNT, INST>(S, nr, C)) {
                     const v3 L = add(mk(Lv.x, Lv.y, Lv.z), nr.c);
                     Lv = make_float4(L.x, L.y, L.z, 0.0f);
                     w.L[slot] = Lv;
@@ -585,43 +585,47 @@ uint32_t resident_grid(K kernel, uint32_t block, int sms) {
     return (uint32_t)(std::max(sms, 1) * std::max(per_sm, 1));
 }
 
-template <int W, int FUSE, bool CNT>
+// INST: kernels for batches with a scene traced through placements (the
+// split stages without per-lane refill, which resumes a traversal of one mesh).
+template <int W, int FUSE, bool CNT, bool INST>
 Grids bounce_grids(const Wf &wf, uint32_t block, int sms) {
     Grids g{0, 0, 0};
     if (FUSE <= 1)
-        g.ext = wf.refill ? resident_grid(k_wf_extend_dyn<W, CNT>, block, sms) : resident_grid(k_wf_extend<W, CNT>, block, sms);
-    g.shade = resident_grid(k_wf_shade<W, FUSE, CNT>, block, sms);
+        g.ext = (!INST && wf.refill) ? resident_grid(k_wf_extend_dyn<W, CNT>, block, sms)
+                                     : resident_grid(k_wf_extend<W, CNT, INST>, block, sms);
+    g.shade = resident_grid(k_wf_shade<W, FUSE, CNT, INST>, block, sms);
     if (FUSE == 0)
-        g.shadow = wf.refill_sh ? resident_grid(k_wf_shadow_dyn<W, CNT>, block, sms)
-                                : resident_grid(k_wf_shadow<W, CNT>, block, sms);
+        g.shadow = (!INST && wf.refill_sh) ? resident_grid(k_wf_shadow_dyn<W, CNT>, block, sms)
+                                           : resident_grid(k_wf_shadow<W, CNT, INST>, block, sms);
     return g;
 }
 
 // The per-bounce kernels of one loop iteration for a fusion level.
-template <int W, int FUSE, bool CNT>
+template <int W, int FUSE, bool CNT, bool INST>
 void launch_bounce(const Wf &wf, const Grids &g, uint32_t block, cudaStream_t st) {
     if (FUSE <= 1) {
-        if (wf.refill) k_wf_extend_dyn<W, CNT><<<g.ext, block, 0, st>>>(wf);
-        else k_wf_extend<W, CNT><<<g.ext, block, 0, st>>>(wf);
+        if (!INST && wf.refill) k_wf_extend_dyn<W, CNT><<<g.ext, block, 0, st>>>(wf);
+        else k_wf_extend<W, CNT, INST><<<g.ext, block, 0, st>>>(wf);
     }
-    k_wf_shade<W, FUSE, CNT><<<g.shade, block, 0, st>>>(wf);
+    k_wf_shade<W, FUSE, CNT, INST><<<g.shade, block, 0, st>>>(wf);
     if (FUSE == 0) {
-        if (wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<g.shadow, block, 0, st>>>(wf);
-        else k_wf_shadow<W, CNT><<<g.shadow, block, 0, st>>>(wf);
+        if (!INST && wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<g.shadow, block, 0, st>>>(wf);
+        else k_wf_shadow<W, CNT, INST><<<g.shadow, block, 0, st>>>(wf);
     }
 }
 
 // Host-driven loop: the same kernels launched from the host, which polls the
 // done flag every 8 iterations (for profilers that cannot see into graphs
 // with conditional nodes, and for runtimes without them).
-template <int W, int FUSE, bool CNT>
+template <int W, int FUSE, bool CNT, bool INST>
 crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &bg, uint32_t block, uint32_t max_iters,
                     cudaStream_t st) {
     unsigned int *done_h = nullptr;
+    if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "host-driven loop: pinned flag allocation failed (injected fault)");
     CRG_CUDA(ctx, cudaHostAlloc(&done_h, sizeof(unsigned int), cudaHostAllocDefault));
     crg_status rc = CRG_OK;
     for (uint32_t it = 0; it < max_iters + 8; ++it) {
-        launch_bounce<W, FUSE, CNT>(wf, bg, block, st);
+        launch_bounce<W, FUSE, CNT, INST>(wf, bg, block, st);
         k_wf_control<<<1, 32, 0, st>>>(wf, 0, 0);
         k_wf_resolve<<<grid, 256, 0, st>>>(wf);
         k_wf_generate<<<grid, 256, 0, st>>>(wf, 0);
@@ -640,7 +644,7 @@ crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &
     return rc;
 }
 
-template <int W, int FUSE, bool CNT>
+template <int W, int FUSE, bool CNT, bool INST>
 crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st,
                bool host_loop) {
     // prologue on the caller's stream
@@ -648,8 +652,8 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
     k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
     k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
     CRG_CUDA(ctx, cudaGetLastError());
-    const Grids bg = bounce_grids<W, FUSE, CNT>(wf, block, ctx->sm_count);
-    if (host_loop) return run_host<W, FUSE, CNT>(ctx, wf, grid, bg, block, max_iters, st);
+    const Grids bg = bounce_grids<W, FUSE, CNT, INST>(wf, block, ctx->sm_count);
+    if (host_loop) return run_host<W, FUSE, CNT, INST>(ctx, wf, grid, bg, block, max_iters, st);
     // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -682,7 +686,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
             rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
             break;
         }
-        launch_bounce<W, FUSE, CNT>(wf, bg, block, cap);
+        launch_bounce<W, FUSE, CNT, INST>(wf, bg, block, cap);
         k_wf_control<<<1, 32, 0, cap>>>(wf, handle, 1);
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
@@ -703,13 +707,13 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
 template <int W, int FUSE>
 int occupancy_of(int block) {
     int a = 0, b = 0, c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shade<W, FUSE, false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shade<W, FUSE, false, false>, block, 0);
     a = b;
-    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false>, block, 0) == cudaSuccess)
+    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
-    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false>, block, 0) == cudaSuccess)
+    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
@@ -732,24 +736,27 @@ int occupancy(uint32_t width, uint32_t fuse, int block) {
 }
 
 template <int W>
-crg_status dispatch_w(crg_context *ctx, const Wf &wf, uint32_t fuse, bool cnt, uint32_t grid, uint32_t block,
+crg_status dispatch_w(crg_context *ctx, const Wf &wf, uint32_t fuse, bool cnt, bool inst, uint32_t grid, uint32_t block,
                       uint32_t max_iters, cudaStream_t st, bool hl) {
+    if (inst) // batches with placements run the split stages
+        return cnt ? run<W, 0, true, true>(ctx, wf, grid, block, max_iters, st, hl)
+                   : run<W, 0, false, true>(ctx, wf, grid, block, max_iters, st, hl);
     switch (fuse * 2 + (cnt ? 1 : 0)) {
-    case 0: return run<W, 0, false>(ctx, wf, grid, block, max_iters, st, hl);
-    case 1: return run<W, 0, true>(ctx, wf, grid, block, max_iters, st, hl);
-    case 2: return run<W, 1, false>(ctx, wf, grid, block, max_iters, st, hl);
-    case 3: return run<W, 1, true>(ctx, wf, grid, block, max_iters, st, hl);
-    case 4: return run<W, 2, false>(ctx, wf, grid, block, max_iters, st, hl);
-    default: return run<W, 2, true>(ctx, wf, grid, block, max_iters, st, hl);
+    case 0: return run<W, 0, false, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 1: return run<W, 0, true, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 2: return run<W, 1, false, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 3: return run<W, 1, true, false>(ctx, wf, grid, block, max_iters, st, hl);
+    case 4: return run<W, 2, false, false>(ctx, wf, grid, block, max_iters, st, hl);
+    default: return run<W, 2, true, false>(ctx, wf, grid, block, max_iters, st, hl);
     }
 }
 
-crg_status dispatch(crg_context *ctx, const Wf &wf, uint32_t width, uint32_t fuse, bool cnt, uint32_t grid,
+crg_status dispatch(crg_context *ctx, const Wf &wf, uint32_t width, uint32_t fuse, bool cnt, bool inst, uint32_t grid,
                     uint32_t block, uint32_t max_iters, cudaStream_t st, bool hl) {
     switch (width) {
-    case 2: return dispatch_w<2>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
-    case 4: return dispatch_w<4>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
-    default: return dispatch_w<8>(ctx, wf, fuse, cnt, grid, block, max_iters, st, hl);
+    case 2: return dispatch_w<2>(ctx, wf, fuse, cnt, inst, grid, block, max_iters, st, hl);
+    case 4: return dispatch_w<4>(ctx, wf, fuse, cnt, inst, grid, block, max_iters, st, hl);
+    default: return dispatch_w<8>(ctx, wf, fuse, cnt, inst, grid, block, max_iters, st, hl);
     }
 }
 
@@ -871,7 +878,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     CRG_CUDA(ctx, cudaMemcpyAsync(d_sg, segs.data(), sizeof(Segment) * segs.size(), cudaMemcpyHostToDevice, st));
     CRG_CUDA(ctx, cudaMemcpyAsync(d_ch, chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, st));
     // persistent grid: resident blocks of the launched kernels on every SM
-    const uint32_t fuse = o.fuse ? o.fuse - 1 : 0; // fusion level 0..2
+    const uint32_t fuse = instanced ? 0u : (o.fuse ? o.fuse - 1 : 0); // fusion level 0..2 (split with placements)
     int per_sm = occupancy(width, fuse, (int)o.block_size);
     const uint32_t grid = (uint32_t)(std::max(ctx->sm_count, 1) * per_sm);
     // every chunk needs at most (samples / P + 1) refills of max_bounces + 1 iterations
@@ -882,7 +889,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
     if (o.max_iterations) max_iters = o.max_iterations;
     const bool cnt = o.count_work != 0, hl = o.host_loop != 0;
-    rc = dispatch(ctx, wf, width, fuse, cnt, grid, o.block_size, max_iters, st, hl);
+    rc = dispatch(ctx, wf, width, fuse, cnt, instanced, grid, o.block_size, max_iters, st, hl);
     if (rc != CRG_OK) return rc;
     Ctrl host{};
     CRG_CUDA(ctx, cudaMemcpyAsync(&host, wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));

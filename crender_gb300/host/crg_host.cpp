@@ -128,7 +128,7 @@ void scene::check(crg_status s) const {
     if (s != CRG_OK) raise(ctx_, s, "crg");
 }
 
-void scene::add_model(const model_data &m) {
+size_t scene::add_model(const model_data &m) {
     std::lock_guard<std::mutex> g(mutex_);
     const size_t ni = m.vertex_indices.size();
     if (ni % 3) throw error(CRG_ERR_INVALID_ARG, "add_model: vertex_indices is not a multiple of 3");
@@ -142,31 +142,53 @@ void scene::add_model(const model_data &m) {
         if (k >= m.materials.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: material index out of range");
     for (const material_information &mi : m.materials)
         if (mi.tex && *mi.tex >= m.textures.size()) throw error(CRG_ERR_INVALID_ARG, "add_model: texture index out of range");
-    // register_model (registry.cpp:51-97) keeps the model's own index space;
-    // here the indices are rebased onto the scene-wide arrays
-    const uint32_t pos_base = (uint32_t)(positions_.size() / 3), tc_base = (uint32_t)(texcoords_.size() / 2);
-    const uint32_t mat_base = (uint32_t)materials_.size(), tex_base = (uint32_t)textures_.size();
-    for (const vec3 &v : m.vertices) positions_.insert(positions_.end(), {v.x, v.y, v.z});
-    for (const vec2 &t : m.texture_coords) texcoords_.insert(texcoords_.end(), {t.x, t.y});
-    for (size_t i = 0; i < ni; ++i) {
-        vidx_.push_back(pos_base + m.vertex_indices[i]);
-        const uint32_t t = have_uv ? m.texture_indices[i] : 0xFFFFFFFFu;
-        tidx_.push_back(t < m.texture_coords.size() ? (int32_t)(tc_base + t) : -1);
-    }
-    for (size_t t = 0; t < ntri; ++t) mat_idx_.push_back(mat_base + m.material_indices[t]);
+    // register_model (registry.cpp:51-97) keeps the model's own index space; only
+    // texture indices are rebased onto the scene's texture list
+    model_rec r;
+    const uint32_t tex_base = (uint32_t)textures_.size();
+    for (const vec3 &v : m.vertices) r.positions.insert(r.positions.end(), {v.x, v.y, v.z});
+    for (const vec2 &t : m.texture_coords) r.texcoords.insert(r.texcoords.end(), {t.x, t.y});
+    r.vidx.assign(m.vertex_indices.begin(), m.vertex_indices.end());
+    if (have_uv)
+        for (size_t i = 0; i < ni; ++i) {
+            const uint32_t t = m.texture_indices[i];
+            r.tidx.push_back(t < m.texture_coords.size() ? (int32_t)t : -1);
+        }
+    r.mat_idx.assign(m.material_indices.begin(), m.material_indices.end());
     for (material_information mi : m.materials) {
         if (mi.tex) mi.tex = tex_base + *mi.tex;
-        materials_.push_back(mi);
+        r.materials.push_back(to_crg(mi));
+        r.infos.push_back(mi);
     }
+    first_.push_back(mat_idx_.size());
+    for (size_t t = 0; t < ntri; ++t) mat_idx_.push_back(m.material_indices[t]);
     textures_.insert(textures_.end(), m.textures.begin(), m.textures.end());
+    models_.push_back(std::move(r));
     dirty_ = true;
+    return models_.size() - 1;
 }
 
 void scene::set_instances(const std::vector<std::array<float, 16>> &transforms) {
     std::lock_guard<std::mutex> g(mutex_);
-    instances_ = transforms;
-    if (scene_) check(crg_scene_set_instances(scene_, instances_.empty() ? nullptr : instances_[0].data(),
-                                              (uint32_t)instances_.size()));
+    for (model_rec &r : models_) {
+        r.instances = transforms;
+        r.instances_dirty = false;
+    }
+    if (scene_) check(crg_scene_set_instances(scene_, transforms.empty() ? nullptr : transforms[0].data(),
+                                              (uint32_t)transforms.size()));
+}
+
+void scene::set_model_instances(size_t model, const std::vector<std::array<float, 16>> &transforms) {
+    std::lock_guard<std::mutex> g(mutex_);
+    if (model >= models_.size()) throw error(CRG_ERR_INVALID_ARG, "set_model_instances: no such model");
+    model_rec &r = models_[model];
+    r.instances = transforms;
+    r.instances_dirty = true;
+    if (scene_ && r.added) {
+        check(crg_scene_set_model_instances(scene_, (uint32_t)model, transforms.empty() ? nullptr : transforms[0].data(),
+                                            (uint32_t)transforms.size()));
+        r.instances_dirty = false;
+    }
 }
 
 void scene::set_skybox(image &&sky) {
@@ -210,15 +232,37 @@ vec3 scene::sample_skybox(float x, float y) const noexcept {
 
 void scene::commit() {
     if (!dirty_ && scene_) return;
-    if (mat_idx_.empty()) throw error(CRG_ERR_INVALID_ARG, "scene has no triangles");
-    std::vector<crg_material> mats(materials_.size());
-    for (size_t i = 0; i < mats.size(); ++i) mats[i] = to_crg(materials_[i]);
-    crg_scene *fresh = nullptr;
-    check(crg_scene_create_indexed(ctx_, positions_.data(), (uint32_t)(positions_.size() / 3), vidx_.data(),
-                                   (uint32_t)mat_idx_.size(), texcoords_.data(), (uint32_t)(texcoords_.size() / 2),
-                                   tidx_.data(), mat_idx_.data(), mats.data(), (uint32_t)mats.size(), &fresh));
+    if (models_.empty() || mat_idx_.empty()) throw error(CRG_ERR_INVALID_ARG, "scene has no triangles");
+    auto indexed = [](const model_rec &r, auto &&call) {
+        return call(r.positions.data(), (uint32_t)(r.positions.size() / 3), r.vidx.data(), (uint32_t)(r.vidx.size() / 3),
+                    r.texcoords.empty() ? nullptr : r.texcoords.data(), (uint32_t)(r.texcoords.size() / 2),
+                    r.tidx.empty() ? nullptr : r.tidx.data(), r.mat_idx.data(), r.materials.data(),
+                    (uint32_t)r.materials.size());
+    };
     crg_status s = CRG_OK;
-    if (!textures_.empty()) {
+    bool fresh = false;
+    if (!scene_) {
+        // model 0 creates the library scene (crg_scene_create_indexed)
+        crg_scene *sc = nullptr;
+        s = indexed(models_[0], [&](auto... a) { return crg_scene_create_indexed(ctx_, a..., &sc); });
+        if (s != CRG_OK) raise(ctx_, s, "scene commit");
+        scene_ = sc;
+        models_[0].added = true;
+        models_[0].instances_dirty = !models_[0].instances.empty();
+        textures_sent_ = 0;
+        fresh = true;
+    }
+    // every later model: appended with its own BVH region (crg_scene_add_model_indexed)
+    for (size_t k = 0; k < models_.size() && s == CRG_OK; ++k) {
+        model_rec &r = models_[k];
+        if (r.added) continue;
+        uint32_t idx = 0;
+        s = indexed(r, [&](auto... a) { return crg_scene_add_model_indexed(scene_, a..., &idx); });
+        if (s == CRG_OK && idx != k) s = CRG_ERR_INVALID_ARG;
+        r.added = s == CRG_OK;
+        r.instances_dirty = !r.instances.empty();
+    }
+    if (s == CRG_OK && textures_sent_ != textures_.size()) {
         std::vector<const float *> px;
         std::vector<uint32_t> w, h;
         for (const image &t : textures_) {
@@ -226,22 +270,30 @@ void scene::commit() {
             w.push_back((uint32_t)t.width());
             h.push_back((uint32_t)t.height());
         }
-        s = crg_scene_set_textures(fresh, (uint32_t)px.size(), px.data(), w.data(), h.data());
+        s = crg_scene_set_textures(scene_, (uint32_t)px.size(), px.data(), w.data(), h.data());
+        if (s == CRG_OK) textures_sent_ = textures_.size();
     }
-    if (s == CRG_OK) s = crg_scene_build(fresh, &opts_, nullptr);
-    if (s == CRG_OK && !instances_.empty())
-        s = crg_scene_set_instances(fresh, instances_[0].data(), (uint32_t)instances_.size());
-    if (s == CRG_OK && skybox_)
-        s = crg_scene_set_skybox(fresh, skybox_->data(), (uint32_t)skybox_->width(), (uint32_t)skybox_->height(),
+    for (size_t k = 0; k < models_.size() && s == CRG_OK; ++k) {
+        model_rec &r = models_[k];
+        if (!r.instances_dirty) continue;
+        s = crg_scene_set_model_instances(scene_, (uint32_t)k, r.instances.empty() ? nullptr : r.instances[0].data(),
+                                          (uint32_t)r.instances.size());
+        r.instances_dirty = false;
+    }
+    // only models without a BVH for these options are built
+    if (s == CRG_OK) s = crg_scene_build(scene_, &opts_, nullptr);
+    if (s == CRG_OK && fresh && skybox_)
+        s = crg_scene_set_skybox(scene_, skybox_->data(), (uint32_t)skybox_->width(), (uint32_t)skybox_->height(),
                                  sky_rot_.x, sky_rot_.y);
-    if (s == CRG_OK) s = crg_scene_set_sun(fresh, sun_enabled_ ? 1 : 0, sun_set_ ? &sun_ : nullptr);
+    if (s == CRG_OK && fresh) s = crg_scene_set_sun(scene_, sun_enabled_ ? 1 : 0, sun_set_ ? &sun_ : nullptr);
     if (s == CRG_OK) s = crg_stream_sync(ctx_, nullptr);
     if (s != CRG_OK) {
-        crg_scene_destroy(fresh);
+        // a failed commit leaves no half-made library scene behind: the next one starts over
+        crg_scene_destroy(scene_);
+        scene_ = nullptr;
+        for (model_rec &r : models_) r.added = false;
         raise(ctx_, s, "scene commit");
     }
-    if (scene_) crg_scene_destroy(scene_);
-    scene_ = fresh;
     dirty_ = false;
 }
 
@@ -281,21 +333,25 @@ std::vector<intersection_record> scene::cast_rays(const std::vector<ray> &rays) 
         if (h.prim == CRG_INVALID_PRIM) continue;
         rec.prim_id = h.prim;
         rec.distance = h.t;
-        rec.material = &materials_[mat_idx_[h.prim]];
+        // the model holding the triangle, and its index there
+        const size_t mdl = (size_t)(std::upper_bound(first_.begin(), first_.end(), (size_t)h.prim) - first_.begin()) - 1;
+        const model_rec &mr = models_[mdl];
+        const size_t p = h.prim - first_[mdl];
+        rec.material = &mr.infos[mr.mat_idx[p]];
         float v[9];
         for (int k = 0; k < 3; ++k)
-            for (int a = 0; a < 3; ++a) v[3 * k + a] = positions_[3 * (size_t)vidx_[3 * (size_t)h.prim + k] + a];
+            for (int a = 0; a < 3; ++a) v[3 * k + a] = mr.positions[3 * (size_t)mr.vidx[3 * p + k] + a];
         const double e1[3] = {(double)v[3] - v[0], (double)v[4] - v[1], (double)v[5] - v[2]};
         const double e2[3] = {(double)v[6] - v[0], (double)v[7] - v[1], (double)v[8] - v[2]};
         double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
         const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
         if (len > 0) rec.normal = {(float)(n[0] / len), (float)(n[1] / len), (float)(n[2] / len)};
         float uv[6] = {0, 0, 0, 0, 0, 0};
-        for (int k = 0; k < 3; ++k) {
-            const int32_t t = tidx_[3 * (size_t)h.prim + k];
+        for (int k = 0; k < 3 && !mr.tidx.empty(); ++k) {
+            const int32_t t = mr.tidx[3 * p + k];
             if (t >= 0) {
-                uv[2 * k] = texcoords_[2 * (size_t)t];
-                uv[2 * k + 1] = texcoords_[2 * (size_t)t + 1];
+                uv[2 * k] = mr.texcoords[2 * (size_t)t];
+                uv[2 * k + 1] = mr.texcoords[2 * (size_t)t + 1];
             }
         }
         const float w0 = 1.0f - h.u - h.v;

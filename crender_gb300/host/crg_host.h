@@ -161,9 +161,16 @@ public:
     scene(const scene &) = delete;
     scene &operator=(const scene &) = delete;
 
-    // De-indexes the model (registry.cpp:51-97) and appends it; the BVH is
-    // rebuilt at the next render or query (rtcCommitScene's role).
-    void add_model(const model_data &model);
+    // Registers the model (registry.cpp:51-97) as one more model of the
+    // library scene, with its own BVH and instance list; at the next render or
+    // query it is de-indexed on the device and only its BVH is built
+    // (rtcCommitScene's role).  Returns the model's index.
+    size_t add_model(const model_data &model);
+    // One model's instance transforms (its cr::entity::instances::transforms,
+    // edited per entity by the UI, src/ui/ui.h:1105-1193); empty = one
+    // identity instance, the registry's default (registry.cpp:73-74).
+    void set_model_instances(size_t model, const std::vector<std::array<float, 16>> &transforms);
+    size_t model_count() const noexcept { return models_.size(); }
     void set_skybox(image &&skybox);
     void set_skybox_rotation(const vec2 &rotation);
     void set_sun_enabled(bool value);
@@ -179,8 +186,8 @@ public:
     // BVH options used by the next commit (default: width 8, treelets on).
     void set_build_options(const crg_build_opts &opts);
     // Instance transforms (cr::entity::instances::transforms, model.cpp:99-126),
-    // 16 floats each, column-major as glm::mat4; applied to every model of
-    // this scene (crg_scene_set_instances).  Empty = the models as added.
+    // 16 floats each, column-major as glm::mat4; given to every model of this
+    // scene (crg_scene_set_instances).  Empty = the models as added.
     void set_instances(const std::vector<std::array<float, 16>> &transforms);
 
     // ABI handles (the scene is committed first).
@@ -195,17 +202,27 @@ private:
     crg_scene *scene_ = nullptr;
     bool dirty_ = true;
     crg_build_opts opts_{8, 1, 3, 3};
-    // models as added, indexed; expanded on the device at commit
-    // (crg_scene_create_indexed), so the host never holds the de-indexed copy
-    std::vector<float> positions_;  // 3 per vertex, all models
-    std::vector<uint32_t> vidx_;    // 3 per triangle, into positions_
-    std::vector<float> texcoords_;  // 2 per coordinate, all models
-    std::vector<int32_t> tidx_;     // 3 per triangle, into texcoords_ (-1 = none)
-    std::vector<image> textures_;   // all models' textures
-    std::vector<uint32_t> mat_idx_;
-    std::vector<material_information> materials_;
+    // one library model per add_model call, kept indexed: the library expands
+    // it on the device (crg_scene_create_indexed / crg_scene_add_model_indexed),
+    // so the host never holds the de-indexed copy
+    struct model_rec {
+        std::vector<float> positions;  // 3 per vertex
+        std::vector<uint32_t> vidx;    // 3 per triangle, into positions
+        std::vector<float> texcoords;  // 2 per coordinate
+        std::vector<int32_t> tidx;     // 3 per triangle, into texcoords (-1 = none); empty = no coordinates
+        std::vector<uint32_t> mat_idx; // into materials
+        std::vector<crg_material> materials; // textures rebased onto the scene's texture list
+        std::vector<material_information> infos; // the same, as cast_ray's records point to them
+        std::vector<std::array<float, 16>> instances;
+        bool added = false;            // present in the library scene
+        bool instances_dirty = false;
+    };
+    std::vector<model_rec> models_;
+    std::vector<uint32_t> mat_idx_;  // model-local material index per triangle, all models (triangle_count)
+    std::vector<size_t> first_;      // first scene triangle of each model
+    std::vector<image> textures_;    // all models' textures
+    size_t textures_sent_ = 0;
     std::optional<image> skybox_;
-    std::vector<std::array<float, 16>> instances_;
     vec2 sky_rot_;
     bool sun_enabled_ = true;
     crg_sun sun_{};

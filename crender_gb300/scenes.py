@@ -177,6 +177,64 @@ def instanced_box():
     return dict(sc, instances=inst, camera=camera)
 
 
+def merge_models(models, camera=None):
+    """A scene of several models (cr::registry entities, each with its own mesh,
+    materials and instance list): `models` is a list of dicts {verts, mat_idx,
+    mats[, uvs][, instances]} with model-local material indices.  Returns the
+    scene dict with the merged arrays the library holds after
+    crg_scene_add_model (primitives in model order, material indices rebased)
+    and the list itself under "models"."""
+    verts = np.concatenate([np.asarray(m["verts"], np.float32).reshape(-1, 9) for m in models])
+    mats = np.concatenate([np.asarray(m["mats"]) for m in models])
+    base = np.cumsum([0] + [len(m["mats"]) for m in models])
+    mat_idx = np.concatenate([np.asarray(m["mat_idx"], np.uint32) + np.uint32(base[k]) for k, m in enumerate(models)])
+    out = dict(verts=np.ascontiguousarray(verts), mat_idx=mat_idx.astype(np.uint32), mats=mats, models=list(models))
+    if any(m.get("uvs") is not None for m in models):
+        out["uvs"] = np.concatenate([np.asarray(m["uvs"], np.float32).reshape(-1, 6) if m.get("uvs") is not None
+                                     else np.zeros((len(np.asarray(m["verts"]).reshape(-1, 9)), 6), np.float32)
+                                     for m in models])
+    if camera is not None:
+        out["camera"] = camera
+    return out
+
+
+def multi_model_box(duplicate=False):
+    """Three models with their own instance lists (cr::entity::instances per
+    entity, components.h:18-21):
+      0  the box room (walls and the ceiling light), no list (one identity instance);
+      1  the short box with a metal, a glass and a Lambert material, three instances;
+      2  the tall box plus a small emissive quad on its top, two instances.
+    duplicate=True adds model 3, a second copy of model 1's mesh with one
+    identity instance, so some hits of different models tie exactly (the earlier
+    model must win)."""
+    sc = box_scene()
+    room = dict(verts=np.concatenate([sc["verts"][:10], sc["verts"][34:]]),
+                mat_idx=np.concatenate([sc["mat_idx"][:10], sc["mat_idx"][34:]]), mats=sc["mats"])
+    short = np.asarray(_box((0.3, 0.3, 0.3), (0.0, 0.0, 0.0), 0.0), np.float64).astype(np.float32)
+    m1 = dict(verts=short, mat_idx=np.array([0, 0, 1, 1, 2, 2, 0, 0, 1, 1, 2, 2], np.uint32),
+              mats=material_table([{"colour": (0.8, 0.6, 0.3, 1.0), "shade_type": SHADE_METAL, "roughness": 0.2},
+                                   {"colour": (0.9, 0.95, 1.0, 1.0), "shade_type": SHADE_GLASS, "ior": 1.5},
+                                   {"colour": (0.3, 0.5, 0.8, 1.0)}]),
+              instances=np.stack([affine((0.68, 0.0, 0.33), (0.0, -17.0, 0.0)),
+                                  affine((0.25, 0.0, 0.25), (0.0, 40.0, 0.0), (0.6, 0.5, 0.6)),
+                                  affine((0.75, 0.45, 0.7), (15.0, 10.0, 5.0), (0.4, 0.4, 0.4))]))
+    tall = _box((0.3, 0.6, 0.3), (0.0, 0.0, 0.0), 0.0)
+    y = 0.6 + 2e-3
+    lamp = _quad([(-0.05, y, -0.05), (0.05, y, -0.05), (0.05, y, 0.05), (-0.05, y, 0.05)], (0, 1, 0))
+    m2 = dict(verts=np.asarray(tall + lamp, np.float64).astype(np.float32),
+              mat_idx=np.array([0] * 12 + [1, 1], np.uint32),
+              mats=material_table([{"colour": (0.7, 0.7, 0.7, 1.0)},
+                                   {"colour": (1.0, 0.8, 0.6, 1.0), "emission": 6.0}]),
+              instances=np.stack([affine((0.32, 0.0, 0.67), (0.0, 17.0, 0.0)),
+                                  affine((0.85, 0.0, 0.8), (0.0, -30.0, 0.0), (0.5, 0.8, 0.5))]))
+    models = [room, m1, m2]
+    if duplicate:
+        models.append(dict(m1, instances=None))
+        models[1] = dict(m1, instances=np.concatenate([np.eye(4, dtype=np.float32)[None], m1["instances"]]))
+    camera = dict(position=(0.5, 0.5, -1.4), rotation=(0.0, 0.0, 0.0), fov=40.0, mode=0, scale=1.0)
+    return merge_models(models, camera)
+
+
 def soup(n=1 << 20, seed=1, sigma=0.01):
     """Random triangle soup: centroids U[0,1]^3, vertex offsets N(0, sigma^2) per axis."""
     rng = np.random.default_rng(seed)

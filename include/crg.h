@@ -148,6 +148,20 @@ const char *crg_last_error_string(const crg_context *ctx);
 const char *crg_status_string(crg_status s);
 uint32_t crg_abi_version(void);
 
+/* Allocation fault injection, for testing callers' error paths (no reference
+ * counterpart: the reference ends the process with cr::exit on any fatal
+ * error, src/util/exception.h:9-13).  After crg_debug_fail_allocation(n), the
+ * n-th next allocation the library makes (n = 0: the very next one), device or
+ * host, fails as if memory were exhausted: the call that made it returns
+ * CRG_ERR_OOM with a message naming the injected fault, frees what it had
+ * allocated, and leaves its context usable.  The fault fires once, then the
+ * hook disarms; n < 0 disarms it.  Process-wide and thread-safe; the GPU is
+ * never made to fault.  crg_debug_allocation_stats reports the allocations
+ * made since the library loaded, the faults fired, and the countdown (-1 =
+ * disarmed); any pointer may be NULL. */
+crg_status crg_debug_fail_allocation(int64_t nth);
+crg_status crg_debug_allocation_stats(uint64_t *allocations, uint32_t *injected, int64_t *armed);
+
 /* Device memory helpers for callers without their own allocator (no reference
  * counterpart: the reference keeps everything in host memory). */
 crg_status crg_device_alloc(crg_context *ctx, size_t bytes, void **dptr);
@@ -196,8 +210,11 @@ crg_status crg_scene_create_indexed(crg_context *ctx, const float *positions, ui
 crg_status crg_scene_destroy(crg_scene *scene);
 
 /* Builds the acceleration structure: LBVH (Morton codes, radix sort, Karras
- * hierarchy, optional treelet restructuring) collapsed to a compressed wide BVH.
- * Replaces rtcCommitScene (src/objects/model.cpp:94).  opts may be NULL. */
+ * hierarchy, optional treelet restructuring) collapsed to a compressed wide BVH,
+ * one per model (crg_scene_add_model).  Replaces rtcCommitScene
+ * (src/objects/model.cpp:94).  Only models whose BVH is missing or was built
+ * with other options are (re)built, so adding a model to a built scene builds
+ * that model alone.  opts may be NULL (defaults). */
 crg_status crg_scene_build(crg_scene *scene, const crg_build_opts *opts, crg_stream stream);
 
 /* Equirectangular skybox, host RGBA32F [h][w][4]; replaces cr::scene::set_skybox
@@ -220,8 +237,9 @@ crg_status crg_scene_set_sun(crg_scene *scene, int enabled, const crg_sun *sun);
 crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float *const *rgba,
                                   const uint32_t *widths, const uint32_t *heights);
 
-/* Instances of the scene's mesh: `ninst` affine 4x4 transforms, 16 floats
- * each, column-major as glm::mat4 stores them (last row 0 0 0 1).  Replaces
+/* Instances: `ninst` affine 4x4 transforms, 16 floats each, column-major as
+ * glm::mat4 stores them (last row 0 0 0 1), given to EVERY model of the scene
+ * (crg_scene_set_model_instances sets one model's list).  Replaces
  * cr::entity::instances::transforms and the per-instance loop of
  * cr::model::intersect (src/objects/model.cpp:99-126, registry.cpp:73-74):
  * a ray is transformed into each instance's object space (origin by
@@ -232,10 +250,60 @@ crg_status crg_scene_set_textures(crg_scene *scene, uint32_t count, const float 
  * the extended estimator shades with the world-space normal, and its emitter
  * table holds one copy of every emissive triangle per instance, weighed by
  * world area.  Inverses are formed once here (in double), not per ray.
- * ninst = 0 (the default) uses the mesh as is, without any transform.  The
- * BVH is not rebuilt.  Instanced batches run the wavefront form without
- * per-lane refill. */
+ * ninst = 0 on a scene of one model (the default) traces the mesh as is,
+ * without any transform.  The BVHs are not rebuilt.  Instanced batches run
+ * the wavefront form without per-lane refill. */
 crg_status crg_scene_set_instances(crg_scene *scene, const float *xforms, uint32_t ninst);
+
+/* ------------------------------------------------------------------ models
+ *
+ * A scene holds one or more models.  Each model is one entity of the
+ * reference's registry (cr::registry::register_model,
+ * src/render/entities/registry.cpp:51-97): its own triangles, its own BVH
+ * (the bottom level) and its own instance list (cr::entity::instances,
+ * src/render/entities/components.h:18-21).  Model 0 holds the triangles the
+ * scene was created with.  A scene of more than one model, or with an
+ * instance list, is traced through its PLACEMENTS, every (model, instance)
+ * pair in model order then instance order (a model without a list has one
+ * identity instance, the registry's default, registry.cpp:73-74); a top-level
+ * tree over their world boxes prunes them, and the answer is that of
+ * cr::scene::cast_ray's loop over entities around cr::model::intersect's loop
+ * over instances (scene.cpp:79-98, model.cpp:99-126): the hit of smallest
+ * world distance |T p - o|, ties to the earlier placement.  Primitive indices
+ * (crg_hit::prim, the material table) are scene-wide: a model's triangles
+ * follow those of the models added before it. */
+
+/* Appends a model, as cr::scene::add_model -> registry::register_model does:
+ * arguments as crg_scene_create (host arrays, copied); its material indices
+ * index its own `mats`, which are appended to the scene's material table.
+ * *model (may be NULL) receives the model's index.  The scene must be built
+ * again (only the new model's BVH is built). */
+crg_status crg_scene_add_model(crg_scene *scene, const float *verts, uint32_t ntri, const float *uvs,
+                               const uint32_t *mat_idx, const crg_material *mats, uint32_t nmat, uint32_t *model);
+/* Same from indexed geometry, expanded on the device (arguments as
+ * crg_scene_create_indexed). */
+crg_status crg_scene_add_model_indexed(crg_scene *scene, const float *positions, uint32_t npos,
+                                       const uint32_t *vertex_indices, uint32_t ntri, const float *texcoords, uint32_t ntc,
+                                       const int32_t *tex_indices, const uint32_t *mat_idx, const crg_material *mats,
+                                       uint32_t nmat, uint32_t *model);
+/* One model's instance list (transforms as crg_scene_set_instances); ninst = 0
+ * gives it one identity instance (the mesh as is when it is the scene's only
+ * model).  Replaces editing one entity's cr::entity::instances
+ * (src/ui/ui.h:1105-1193).  No BVH is rebuilt. */
+crg_status crg_scene_set_model_instances(crg_scene *scene, uint32_t model, const float *xforms, uint32_t ninst);
+crg_status crg_scene_model_count(const crg_scene *scene, uint32_t *count);
+
+typedef struct crg_model_info {
+    uint32_t first_prim;   /* the model's triangles are scene primitives [first_prim, first_prim + ntri) */
+    uint32_t ntri;
+    uint32_t node_base;    /* first node of its wide BVH in crg_scene_bvh_download's node array */
+    uint32_t n_wide_nodes; /* its wide nodes (0 until built) */
+    uint32_t depth;
+    uint32_t ninst;        /* transforms in its instance list (0 = one identity instance) */
+    uint32_t built;        /* 1 when its BVH is current */
+    float sah_cost;
+} crg_model_info;
+crg_status crg_scene_model_info(const crg_scene *scene, uint32_t model, crg_model_info *info);
 
 /* Introspection of the built structure (for parity checks against a CPU build). */
 typedef struct crg_bvh_info {
@@ -254,7 +322,12 @@ crg_status crg_scene_bvh_info(const crg_scene *scene, crg_bvh_info *info);
 /* Copies to host: bvh2 = float[n_bvh2_nodes*8] (lo.xyz,left, hi.xyz,right; child
  * ints stored as raw bits, leaves tagged with bit 31), order = uint32[ntri] sorted
  * primitive order, wide = bytes[n_wide_nodes*node_bytes], tris = float[n_tri_slots*12].
- * Any pointer may be NULL. */
+ * Any pointer may be NULL.  On a scene of several models the arrays hold every
+ * model's structure: model m's binary nodes at 2 * node_base (model-local
+ * indices), its order at first_prim (model-local indices), its wide nodes at
+ * node_base (child and triangle indices scene-wide, unused nodes zero) and its
+ * triangle slots at first_prim (primitive ids scene-wide); n_bvh2_nodes and
+ * n_wide_nodes then give the arrays' full length (crg_scene_model_info). */
 crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t *order, void *wide,
                                   float *tris);
 
@@ -263,12 +336,20 @@ crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t 
 /* Largest triangle count crg_build_bvh_noalloc accepts. */
 #define CRG_NOALLOC_MAX_TRIS 16384u
 
+/* Message of the calling thread's last failed crg_build_bvh_noalloc call
+ * ("" after a call that succeeded); that call has no context, so
+ * crg_last_error_string does not describe it.  Valid until the thread's next
+ * crg_build_bvh_noalloc call. */
+const char *crg_noalloc_last_error(void);
+
 /* Builds the same wide BVH as crg_scene_create + crg_scene_build, for callers
  * that cannot allocate device memory themselves: a host application whose own
  * pool owns the GPU's memory, or an interactive loop that must not pay the
  * device-wide synchronisation of cudaMalloc/cudaFree when a model is added.
- * This entry point calls no cudaMalloc, cudaFree or other allocating routine.
- * It has no counterpart in the reference.
+ * This entry point calls no cudaMalloc, cudaFree or other allocating routine;
+ * it runs the same build pipeline as crg_scene_build, with its scratch taken
+ * from the fixed array described below.  It has no counterpart in the
+ * reference.
  *
  *   d_verts    : device float[ntri*9], de-indexed triangles
  *   ntri       : at most CRG_NOALLOC_MAX_TRIS (larger counts return
@@ -286,10 +367,15 @@ crg_status crg_scene_bvh_download(const crg_scene *scene, float *bvh2, uint32_t 
  * library holds until the process exits.  All calls share it and it keeps the
  * last call's contents: the call clears what must start at zero, but two calls
  * whose work overlaps on the GPU (different streams or threads at once) race
- * on it and must be serialised by the caller.  The first call on each device
- * looks the array's device address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  The call
- * synchronises `stream` once per BVH level, as crg_scene_build does. */
+ * on it and must be serialised by the caller.  The array's device address is
+ * looked up (cudaGetSymbolAddress) once per device with that device current:
+ * by crg_context_create on its device, else by the first call on a device no
+ * context was created on — that first call may load the library's device code
+ * and reserve the array (a driver-side allocation and a synchronisation), so
+ * make it before any stream capture, or create a context on the device first.
+ * The call synchronises `stream` once per BVH level, as crg_scene_build does;
+ * when it fails after queueing work it waits for that work to finish before
+ * returning.  Errors are described by crg_noalloc_last_error. */
 crg_status crg_build_bvh_noalloc(const float *d_verts, uint32_t ntri, const crg_build_opts *opts,
                                  void *d_wide, size_t wide_bytes, float *d_tris, uint32_t *d_order,
                                  crg_bvh_info *info, crg_stream stream);

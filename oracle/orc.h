@@ -70,8 +70,17 @@ typedef struct orc_scene_desc {
     uint32_t ntex;               /* textures (crg_scene_set_textures) */
     const float *const *tex_rgba;
     const uint32_t *tex_w, *tex_h;
-    const float *xforms;         /* ninst*16 column-major affine transforms (crg_scene_set_instances), or NULL */
+    const float *xforms;         /* ninst*16 column-major affine transforms (crg_scene_set_instances), or NULL;
+                                    with models: every model's list, concatenated in model order */
     uint32_t ninst;
+    /* models (crg_scene_add_model): nmodels consecutive primitive ranges of
+     * model_ntri[m] triangles, model m with model_ninst[m] transforms (0 = one
+     * identity instance; model_ninst = NULL: every model takes the xforms
+     * list, as crg_scene_set_instances gives it); nmodels = 0 or model_ntri =
+     * NULL: one model */
+    uint32_t nmodels;
+    const uint32_t *model_ntri;
+    const uint32_t *model_ninst;
 } orc_scene_desc;
 
 typedef struct orc_film {
@@ -135,6 +144,14 @@ float orc_ggx_d(float nh, float alpha);
 float orc_ggx_lambda(const float *w3, float alpha);
 void orc_sample_vndf(const float *wo3, float alpha, float u1, float u2, float *h3);
 float orc_fresnel_dielectric(float ci, float eta);
+/* The faithful estimator's sun sample (sampling.h:72-80 with the registry's
+ * sun frame): direction, pdf and clamped cosine with normal3, from uniforms
+ * (u1, u2); its sun disc test; the extended Lambert's local cosine-weighted
+ * direction (sampling.h:174-183).  For the cross-check with the reference's
+ * own compiled code (oracle/ref_bridge.cpp). */
+void orc_sun_sample(const crg_sun *sun, const float *normal3, float u1, float u2, float *dir3, float *pdf, float *cosine);
+int orc_sun_visible(const crg_sun *sun, const float *dir3);
+void orc_cos_hemp(float x, float y, float *out3);
 
 #ifdef __cplusplus
 }

@@ -112,7 +112,18 @@ def scene_desc(scene: dict, sun_enabled=False, sun=None, skybox=None, sky_rot=(0
         th = np.array([t.shape[0] for t in texs], np.uint32)
         keep += [texs, arr, tw, th]
         d.ntex, d.tex_rgba, d.tex_w, d.tex_h = len(texs), C.cast(arr, C.POINTER(C.c_void_p)), ptr(tw), ptr(th)
-    if scene.get("instances") is not None and len(scene["instances"]):
+    if scene.get("models") is not None:
+        # several models (crg_scene_add_model): consecutive primitive ranges, per-model instance lists
+        ms = scene["models"]
+        mn = np.array([len(np.asarray(m["verts"]).reshape(-1, 9)) for m in ms], np.uint32)
+        mk = np.array([0 if m.get("instances") is None else len(m["instances"]) for m in ms], np.uint32)
+        xs = [np.transpose(np.asarray(m["instances"], np.float32), (0, 2, 1)) for m in ms
+              if m.get("instances") is not None and len(m["instances"])]
+        xf = np.ascontiguousarray(np.concatenate(xs) if xs else np.zeros((0, 4, 4), np.float32))
+        keep += [mn, mk, xf]
+        d.nmodels, d.model_ntri, d.model_ninst = len(ms), ptr(mn), ptr(mk)
+        d.xforms, d.ninst = (ptr(xf) if len(xf) else None), len(xf)
+    elif scene.get("instances") is not None and len(scene["instances"]):
         # [n, 4, 4] row-major -> column-major (glm::mat4 layout)
         xf = np.ascontiguousarray(np.transpose(np.asarray(scene["instances"], np.float32), (0, 2, 1)))
         keep.append(xf)
@@ -211,3 +222,14 @@ def draft_render(scene: dict, camera: dict, width: int, height: int, aspect=1.0,
     rc = lib().orc_draft_render(C.byref(d), C.byref(cam), width, height, float(aspect), ptr(out))
     assert rc == 0, rc
     return out
+
+
+def camera_ray(camera: dict, settings: _abi.Settings, px: int, py: int, jx: float, jy: float):
+    """The oracle camera's ray through pixel (px, py) with jitter (jx, jy): (origin, direction)."""
+    from crender_gb300.api import make_camera
+
+    cam = make_camera(camera)
+    o = np.zeros(3, np.float32)
+    d = np.zeros(3, np.float32)
+    lib().orc_camera_ray(C.byref(cam), C.byref(settings), px, py, float(jx), float(jy), ptr(o), ptr(d))
+    return o, d

@@ -102,7 +102,18 @@ void camera_ray(const CamParams &c, float x, float y, float aspect, v3 &o, v3 &d
 }
 
 struct Scene {
-    const orc_bvh *bvh = nullptr;
+    Scene() = default;
+    Scene(const Scene &) = delete;
+    Scene &operator=(const Scene &) = delete;
+    ~Scene() {
+        for (orc_bvh *b : bvhs) orc_bvh_free(b);
+    }
+    const orc_bvh *bvh = nullptr; /* the BVH of a scene of one model */
+    /* models (cr::registry entities): each its own BVH over its own triangles,
+     * primitives [mfirst[m], mfirst[m] + its count) of the scene arrays */
+    std::vector<orc_bvh *> bvhs;
+    std::vector<uint32_t> mfirst;
+    std::vector<uint32_t> place_model; /* model of each placement (instance) */
     const float *verts = nullptr;
     const uint32_t *mat_idx = nullptr;
     const crg_material *mats = nullptr;
@@ -186,6 +197,29 @@ void hit_colour(const Scene &S, const crg_material &m, const crg_hit &h, float c
     for (int k = 0; k < 4; ++k) col[k] = c[k];
 }
 
+/* sampling::sun::sample's direction (sampling.h:35-43, 72-80): the cone of
+ * half-angle size around the sun, map_to_solid_angle with phi = 2 pi u1 and
+ * cos(theta) = 1 - u2 (1 - cos(size)), turned by the sun frame's columns
+ * (tangent, normal, bitangent; registry.cpp:44-48). */
+v3 sun_direction(const onb &F, float sun_cos, float u1, float u2) {
+    float sp, cp;
+    sincos2pi(u1, &sp, &cp);
+    const float ct = 1.0f - u2 * (1.0f - sun_cos);
+    const float st = std::sqrt(1.0f - ct * ct);
+    const v3 lv = mk(cp * st, ct, sp * st);
+    return mk((F.t.x * lv.x + F.n.x * lv.y) + F.b.x * lv.z, (F.t.y * lv.x + F.n.y * lv.y) + F.b.y * lv.z,
+              (F.t.z * lv.x + F.n.z * lv.y) + F.b.z * lv.z);
+}
+
+/* sampling::cos_hemp (sampling.h:174-183): cosine-weighted local direction,
+ * radius sqrt(x) at angle 2 pi y. */
+v3 cos_hemp(float x, float y) {
+    float sp, cp;
+    sincos2pi(y, &sp, &cp);
+    const float r = std::sqrt(x);
+    return mk(r * cp, r * sp, std::sqrt(maxf(0.0f, 1.0f - x)));
+}
+
 struct Ctx {
     const Scene *S;
     const crg_settings *set;
@@ -228,6 +262,9 @@ bool cast_query(const Scene &S, v3 o, v3 d, float tmin, float tmax, crg_hit &h, 
         crg_ray r{{o.x, o.y, o.z}, tmin, {d.x, d.y, d.z}, tmax};
         return orc_internal::closest(S.bvh, r, h);
     }
+    /* the placements are scene.cpp:79-98's entities in order, each expanded
+     * into model.cpp:99-126's instances in order; both loops keep a strictly
+     * smaller distance, so one pass over the placements in order is their result */
     float best = tmax;
     bool found = false;
     for (uint32_t j = 0; j < S.ninst; ++j) {
@@ -236,7 +273,9 @@ bool cast_query(const Scene &S, v3 o, v3 d, float tmin, float tmax, crg_hit &h, 
         inst_ray(S, j, o, d, oo, od, len);
         crg_ray r{{oo.x, oo.y, oo.z}, tmin, {od.x, od.y, od.z}, kInf};
         crg_hit hj;
-        if (!orc_internal::closest(S.bvh, r, hj)) continue;
+        const uint32_t m = S.place_model[j];
+        if (!orc_internal::closest(S.bvhs[m], r, hj)) continue;
+        hj.prim += S.mfirst[m];
         const float dist = vdist(inst_point(S, j, oo, od, hj.t), o);
         if (dist < best) {
             best = dist;
@@ -265,7 +304,7 @@ bool occluded_query(const Scene &S, v3 o, v3 d, float tmin, float tmax) {
         float len;
         inst_ray(S, j, o, d, oo, od, len);
         crg_ray r{{oo.x, oo.y, oo.z}, tmin, {od.x, od.y, od.z}, (tmax * len) / dl};
-        if (orc_internal::any(S.bvh, r)) return true;
+        if (orc_internal::any(S.bvhs[S.place_model[j]], r)) return true;
     }
     return false;
 }
@@ -388,14 +427,7 @@ v3 trace_faithful(Ctx &C, v3 o, v3 d, Aov &aov) {
             /* renderer.cpp:315-354 */
             v3 so = add(p, mul(Ng, 0.001f));
             const f4 g2 = rand4(C.pix, C.sample, 2 + 2 * i, set.seed);
-            float sp, cp;
-            sincos2pi(g2.x, &sp, &cp);
-            const float ct = 1.0f - g2.y * (1.0f - S.sun_cos);
-            const float st = std::sqrt(1.0f - ct * ct);
-            const v3 lv = mk(cp * st, ct, sp * st);
-            const onb &F = S.sun_frame;
-            const v3 sd = mk((F.t.x * lv.x + F.n.x * lv.y) + F.b.x * lv.z, (F.t.y * lv.x + F.n.y * lv.y) + F.b.y * lv.z,
-                             (F.t.z * lv.x + F.n.z * lv.y) + F.b.z * lv.z);
+            const v3 sd = sun_direction(S.sun_frame, S.sun_cos, g2.x, g2.y);
             const float cosine = clampf(dot(Ng, sd), 0.0f, 1.0f);
             crg_hit sh;
             uint32_t sinst;
@@ -677,10 +709,7 @@ v3 trace_extended(Ctx &C, v3 o, v3 d, Aov &aov, Tape *tape = nullptr) {
              * (renderer.cpp:93-97): the same integral, estimated better. */
             const onb F = build_local(Ng);
             if (have_lights) L = add(L, nee(C, i, p, Ng, T, 0, rgb, F, mk(0, 0, 0), 0.0f, tape, mi));
-            float sp, cp;
-            sincos2pi(g.y, &sp, &cp);
-            const float r = std::sqrt(g.x);
-            const v3 l = mk(r * cp, r * sp, std::sqrt(maxf(0.0f, 1.0f - g.x)));
+            const v3 l = cos_hemp(g.x, g.y);
             d = from_local(F, l);
             o = add(p, mul(Ng, 1e-4f));
             prev_pdf = l.z * kInvPi;
@@ -801,11 +830,19 @@ void inverse_rows(const float *x, float rows[24]) {
     }
 }
 
-void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
-    orc_bvh *bvh = nullptr;
-    orc_bvh_build(D.verts, D.ntri, D.build, &bvh);
-    *bvh_out = bvh;
-    S.bvh = bvh;
+void prepare(const orc_scene_desc &D, Scene &S) {
+    /* models: one BVH each, over the model's own triangles (model-local ids) */
+    const uint32_t nm = (D.nmodels && D.model_ntri) ? D.nmodels : 1;
+    uint32_t first = 0;
+    for (uint32_t m = 0; m < nm; ++m) {
+        const uint32_t n = nm == 1 ? D.ntri : D.model_ntri[m];
+        orc_bvh *b = nullptr;
+        orc_bvh_build(D.verts + (size_t)first * 9, n, D.build, &b);
+        S.bvhs.push_back(b);
+        S.mfirst.push_back(first);
+        first += n;
+    }
+    S.bvh = S.bvhs[0];
     S.verts = D.verts;
     S.mat_idx = D.mat_idx;
     S.mats = D.mats;
@@ -838,14 +875,43 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
     /* instances: inverse rows formed in double and rounded once; the emitter
      * table holds one entry per (instance, emissive triangle), instance-major,
      * weighed by the world area */
-    S.ninst = (D.xforms && D.ninst) ? D.ninst : 0;
+    /* placements: a scene of one model without instances is traced as is;
+     * otherwise every model contributes its instances in order (one identity
+     * instance when it has none, the registry's default, registry.cpp:73-74) */
+    static const float kId[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    std::vector<const float *> pxf;
+    if (nm == 1 && D.nmodels <= 1 && !(D.model_ninst && D.model_ninst[0])) {
+        for (uint32_t j = 0; D.xforms && j < D.ninst; ++j) {
+            pxf.push_back(D.xforms + 16 * (size_t)j);
+            S.place_model.push_back(0);
+        }
+    } else {
+        const float *x = D.xforms;
+        for (uint32_t m = 0; m < nm; ++m) {
+            /* without per-model counts every model takes the one list (crg_scene_set_instances) */
+            if (!D.model_ninst) x = D.xforms;
+            const uint32_t k = D.model_ninst ? D.model_ninst[m] : (D.xforms ? D.ninst : 0);
+            if (k == 0) {
+                pxf.push_back(kId);
+                S.place_model.push_back(m);
+            }
+            for (uint32_t j = 0; j < k; ++j, x += 16) {
+                pxf.push_back(x);
+                S.place_model.push_back(m);
+            }
+        }
+    }
+    S.ninst = (uint32_t)pxf.size();
     S.inst_rows.assign(24 * (size_t)S.ninst, 0.0f);
-    for (uint32_t j = 0; j < S.ninst; ++j) inverse_rows(D.xforms + 16 * (size_t)j, &S.inst_rows[24 * (size_t)j]);
+    for (uint32_t j = 0; j < S.ninst; ++j) inverse_rows(pxf[j], &S.inst_rows[24 * (size_t)j]);
     std::vector<double> w;
     double total = 0.0;
     const uint32_t ncopy = S.ninst ? S.ninst : 1;
-    for (uint32_t j = 0; j < ncopy; ++j)
-        for (uint32_t p = 0; p < D.ntri; ++p) {
+    for (uint32_t j = 0; j < ncopy; ++j) {
+        const uint32_t mj = S.ninst ? S.place_model[j] : 0;
+        const uint32_t p0 = S.ninst ? S.mfirst[mj] : 0;
+        const uint32_t p1 = S.ninst ? (mj + 1 < nm ? S.mfirst[mj + 1] : D.ntri) : D.ntri;
+        for (uint32_t p = p0; p < p1; ++p) {
             const uint32_t m = D.mat_idx[p];
             if (!(lum[m] > 0.0)) continue;
             double wv[3][3];
@@ -853,7 +919,7 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
                 const float *v = D.verts + (size_t)p * 9 + 3 * k;
                 for (int r = 0; r < 3; ++r) {
                     if (S.ninst) {
-                        const float *x = D.xforms + 16 * (size_t)j;
+                        const float *x = pxf[j];
                         wv[k][r] = (((double)x[r] * v[0] + (double)x[4 + r] * v[1]) + (double)x[8 + r] * v[2]) +
                                    (double)x[12 + r];
                     } else {
@@ -875,6 +941,7 @@ void prepare(const orc_scene_desc &D, Scene &S, orc_bvh **bvh_out) {
             w.push_back(wt);
             total += wt;
         }
+    }
     S.mat_light_pdf.assign(D.nmat, 0.0f);
     if (!(total > 0.0)) {
         S.light_prim.clear();
@@ -916,8 +983,7 @@ int orc_render_rows(const orc_scene_desc *desc, const crg_camera *cam, const crg
     if (set->width != film->width || set->height != film->height) return CRG_ERR_INVALID_ARG;
     if (y1 > set->height) y1 = set->height;
     Scene S;
-    orc_bvh *bvh = nullptr;
-    prepare(*desc, S, &bvh);
+    prepare(*desc, S);
     const CamParams cp = camera_params(*cam);
     const uint32_t W = set->width, H = set->height;
     const uint64_t npix = (uint64_t)W * (y1 > y0 ? (y1 - y0) : 0);
@@ -996,7 +1062,6 @@ int orc_render_rows(const orc_scene_desc *desc, const crg_camera *cam, const crg
     film->render_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     film->segments += seg.load();
     film->shadow_rays += shad.load();
-    orc_bvh_free(bvh);
     return CRG_OK;
 }
 
@@ -1005,8 +1070,7 @@ int orc_adjoint(const orc_scene_desc *desc, const crg_camera *cam, const crg_set
     if (!desc || !cam || !set || !adj || !grad_colour || !grad_emission) return CRG_ERR_INVALID_ARG;
     if (set->mode != CRG_MODE_EXTENDED) return CRG_ERR_UNSUPPORTED;
     Scene S;
-    orc_bvh *bvh = nullptr;
-    prepare(*desc, S, &bvh);
+    prepare(*desc, S);
     const CamParams cp = camera_params(*cam);
     const uint32_t W = set->width, H = set->height, nmat = desc->nmat;
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -1051,7 +1115,6 @@ int orc_adjoint(const orc_scene_desc *desc, const crg_camera *cam, const crg_set
         for (size_t k = 0; k < 3 * (size_t)nmat; ++k) grad_colour[k] += gc[t][k];
         for (size_t k = 0; k < nmat; ++k) grad_emission[k] += ge[t][k];
     }
-    orc_bvh_free(bvh);
     return CRG_OK;
 }
 
@@ -1069,8 +1132,7 @@ int orc_draft_render(const orc_scene_desc *desc, const crg_camera *cam, uint32_t
                      float *rgba) {
     if (!desc || !cam || !rgba || w == 0 || h == 0) return CRG_ERR_INVALID_ARG;
     Scene S;
-    orc_bvh *bvh = nullptr;
-    prepare(*desc, S, &bvh);
+    prepare(*desc, S);
     const CamParams cp = camera_params(*cam);
     const v3 fwd = mk(cp.R[0][2], cp.R[1][2], cp.R[2][2]);
     const float zn = cam->mode == CRG_CAMERA_ORTHOGRAPHIC ? 0.01f : 0.1f;
@@ -1097,7 +1159,6 @@ int orc_draft_render(const orc_scene_desc *desc, const crg_camera *cam, uint32_t
             float *out = rgba + ((size_t)(w - 1 - px) + (size_t)(h - 1 - py) * w) * 4;
             for (int k = 0; k < 4; ++k) out[k] = c[k];
         }
-    orc_bvh_free(bvh);
     return CRG_OK;
 }
 
@@ -1118,8 +1179,7 @@ int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit
                         uint64_t n) {
     if (!desc || !rays || (!hits && !occluded)) return CRG_ERR_INVALID_ARG;
     Scene S;
-    orc_bvh *bvh = nullptr;
-    prepare(*desc, S, &bvh);
+    prepare(*desc, S);
     for (uint64_t i = 0; i < n; ++i) {
         const crg_ray &r = rays[i];
         const v3 o = mk(r.org[0], r.org[1], r.org[2]), d = mk(r.dir[0], r.dir[1], r.dir[2]);
@@ -1141,8 +1201,27 @@ int orc_scene_intersect(const orc_scene_desc *desc, const crg_ray *rays, crg_hit
             hits[i] = crg_hit{kInf, 0xFFFFFFFFu, 0.0f, 0.0f};
         }
     }
-    orc_bvh_free(bvh);
     return CRG_OK;
+}
+
+/* The faithful estimator's sun sample: direction, pdf and cosine with the
+ * normal, from a sun (crg_sun's direction and size) and the two uniforms. */
+void orc_sun_sample(const crg_sun *sun, const float *normal3, float u1, float u2, float *dir3, float *pdf, float *cosine) {
+    const onb F = build_local(mk(-sun->direction[0], -sun->direction[1], -sun->direction[2]));
+    const float sun_cos = (float)std::cos((double)sun->size);
+    const v3 d = sun_direction(F, sun_cos, u1, u2);
+    dir3[0] = d.x; dir3[1] = d.y; dir3[2] = d.z;
+    *pdf = 1.0f / (kTau * (1.0f - sun_cos));
+    *cosine = clampf(dot(mk(normal3[0], normal3[1], normal3[2]), d), 0.0f, 1.0f);
+}
+/* The faithful estimator's sun disc test (dot(d, -sun.direction) > cos(size)). */
+int orc_sun_visible(const crg_sun *sun, const float *dir3) {
+    const v3 ms = mk(-sun->direction[0], -sun->direction[1], -sun->direction[2]);
+    return dot(mk(dir3[0], dir3[1], dir3[2]), ms) > (float)std::cos((double)sun->size) ? 1 : 0;
+}
+void orc_cos_hemp(float x, float y, float *out3) {
+    const v3 v = cos_hemp(x, y);
+    out3[0] = v.x; out3[1] = v.y; out3[2] = v.z;
 }
 
 /* Sampling helpers exported for known-answer and distribution tests. */

@@ -1,7 +1,8 @@
 """The C++ host adapter (crg::host::scene / camera / renderer, the interface
 of cr::scene / cr::camera / cr::renderer) driven by its self-test program: a
-renderer run to a target spp in one-sample passes, an update() that changes the
-depth and restarts, and cast_rays, each compared with direct ABI calls."""
+scene of two models (each add_model call one library model with its own BVH),
+a renderer run to a target spp in one-sample passes, an update() that changes
+the depth and restarts, and cast_rays, each compared with direct ABI calls."""
 import os
 import subprocess
 
@@ -60,7 +61,11 @@ def test_adapter_matches_abi(ctx, tmp_path, mode):
     assert spp1 == spp and spp2 == spp
     assert total_rays > 0
 
-    scene = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    # the adapter registered two models (triangles [0, 20) and [20, 36), each with
+    # the whole material table): the same two models through the ABI
+    scene = api.Scene(ctx, sc["verts"][:20], sc["mat_idx"][:20], sc["mats"])
+    scene.add_model(sc["verts"][20:], sc["mat_idx"][20:], sc["mats"])
+    scene.build(8, 1)
     film = api.Film(ctx, W, H)
     try:
         for b, got in ((bounces, s1), (bounces // 2, s2)):
