@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
     PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
+    uint32_t lanes = __ballot_sync(0xFFFFFFFFu, pix < Wd * Hd);
     if (pix < Wd * Hd) {
         const uint32_t px = pix % Wd, py = pix / Wd;
         const size_t fidx = (size_t)(Wd - 1 - px) + (size_t)(Hd - 1 - py) * Wd;
@@ -157,7 +158,10 @@ __global__ void __launch_bounds__(128) k_adjoint(SceneDev S, CamDev cam, crg_set
         PathState ps;
         Aov aov;
         uint32_t s = 0, i = 0;
-        while (live && s < set.spp) {
+        for (;;) {
+            // the lanes still replaying meet before every segment (as in the forward megakernel)
+            lanes = __ballot_sync(lanes, live && s < set.spp);
+            if (!(live && s < set.spp)) break;
             if (i == 0) {
                 C.sample = s;
                 const f4 g0 = rand4(pix, s, 0, set.seed);

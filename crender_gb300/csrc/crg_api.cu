@@ -336,17 +336,18 @@ void instance_areas(crg_scene *s, const float *verts) {
 
 // Object-space bounds of ntri de-indexed triangles (host float[ntri*9]).
 void mesh_box(const float *v, uint32_t ntri, float box[6]) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t k = 0; k < 3 * (size_t)ntri; ++k) {
+        const float *p = v + 3 * k;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = p[a] < lo[a] ? p[a] : lo[a];
+            hi[a] = p[a] > hi[a] ? p[a] : hi[a];
+        }
+    }
     for (int a = 0; a < 3; ++a) {
-        box[a] = INFINITY;
-        box[3 + a] = -INFINITY;
+        box[a] = ntri ? lo[a] : 0.0f;
+        box[3 + a] = ntri ? hi[a] : 0.0f;
     }
-    for (size_t i = 0; i < 9 * (size_t)ntri; ++i) {
-        const int a = (int)(i % 3);
-        box[a] = std::min(box[a], v[i]);
-        box[3 + a] = std::max(box[3 + a], v[i]);
-    }
-    if (ntri == 0)
-        for (int a = 0; a < 6; ++a) box[a] = 0.0f;
 }
 
 const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -462,6 +463,15 @@ crg_status update_placements(crg_scene *s) {
     dev_free(s->tlas);
     dev_free(s->light_inst);
     if (flat) return CRG_OK;
+    // the vertices come back to the host once: model boxes (for the top-level
+    // tree) and the world areas of emitter copies
+    std::vector<float> hv((size_t)s->ntri * 9);
+    if (s->ntri) CRG_CUDA(ctx, cudaMemcpy(hv.data(), s->verts.ptr, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost));
+    for (crg_model_rec &md : s->models)
+        if (!md.box_valid) {
+            mesh_box(hv.data() + (size_t)md.first * 9, md.ntri, md.box);
+            md.box_valid = true;
+        }
     std::vector<uint32_t> roots;
     std::vector<std::array<double, 6>> boxes;
     for (uint32_t m = 0; m < (uint32_t)s->models.size(); ++m) {
@@ -497,9 +507,6 @@ crg_status update_placements(crg_scene *s) {
     s->tlas_root = root;
     s->tlas_nodes = (uint32_t)(tb.nodes.size() / 16);
     s->ninst = np;
-    // emitter copies are weighed by their world areas: the vertices come back to the host once
-    std::vector<float> hv((size_t)s->ntri * 9);
-    if (s->ntri) CRG_CUDA(ctx, cudaMemcpy(hv.data(), s->verts.ptr, sizeof(float) * hv.size(), cudaMemcpyDeviceToHost));
     instance_areas(s, hv.data());
     return CRG_OK;
 }
@@ -784,7 +791,6 @@ crg_status crg_scene_create(crg_context *ctx, const float *verts, uint32_t ntri,
     }
     if (rc == CRG_OK) {
         compute_areas(s, verts);
-        mesh_box(verts, ntri, s->models[0].box);
         rc = prepare_lights(s);
     }
     if (rc != CRG_OK) {
@@ -840,18 +846,9 @@ crg_status crg_scene_create_indexed(crg_context *ctx, const float *positions, ui
         // emitter areas from the same float positions the device copied
         float tv[9];
         s->tri_area.assign(ntri, 0.0);
-        float *box = s->models[0].box;
-        for (int a = 0; a < 3; ++a) {
-            box[a] = ntri ? INFINITY : 0.0f;
-            box[3 + a] = ntri ? -INFINITY : 0.0f;
-        }
         for (uint32_t p = 0; p < ntri; ++p) {
             for (int k = 0; k < 3; ++k)
-                for (int a = 0; a < 3; ++a) {
-                    tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
-                    box[a] = std::min(box[a], tv[3 * k + a]);
-                    box[3 + a] = std::max(box[3 + a], tv[3 * k + a]);
-                }
+                for (int a = 0; a < 3; ++a) tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
             s->tri_area[p] = tri_area_of(tv);
         }
         rc = prepare_lights(s);
@@ -885,7 +882,6 @@ crg_status crg_scene_create_device(crg_context *ctx, const float *d_verts, uint3
     }
     if (rc == CRG_OK) {
         compute_areas(s, hv.data());
-        mesh_box(hv.data(), ntri, s->models[0].box);
         rc = prepare_lights(s);
     }
     if (rc != CRG_OK) {
@@ -1016,7 +1012,7 @@ crg_status crg_scene_add_model(crg_scene *scene, const float *verts, uint32_t nt
         if (e != cudaSuccess) return cuda_error(scene->ctx, e, "cudaMemcpy(model)");
         areas.resize(ntri);
         for (uint32_t p = 0; p < ntri; ++p) areas[p] = tri_area_of(verts + (size_t)p * 9);
-        mesh_box(verts, ntri, box);
+        (void)box; // computed from the device copy when the placements are rebuilt
         return CRG_OK;
     }, uvs != nullptr);
 }
@@ -1062,17 +1058,10 @@ crg_status crg_scene_add_model_indexed(crg_scene *scene, const float *positions,
         if (rc != CRG_OK) return rc;
         if (e != cudaSuccess) return cuda_error(ctx, e, "k_expand(model)");
         float tv[9];
-        for (int a = 0; a < 3; ++a) {
-            box[a] = INFINITY;
-            box[3 + a] = -INFINITY;
-        }
+        (void)box; // computed from the device copy when the placements are rebuilt
         for (uint32_t p = 0; p < ntri; ++p) {
             for (int k = 0; k < 3; ++k)
-                for (int a = 0; a < 3; ++a) {
-                    tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
-                    box[a] = std::min(box[a], tv[3 * k + a]);
-                    box[3 + a] = std::max(box[3 + a], tv[3 * k + a]);
-                }
+                for (int a = 0; a < 3; ++a) tv[3 * k + a] = positions[3 * (size_t)vertex_indices[3 * (size_t)p + k] + a];
             areas.push_back(tri_area_of(tv));
         }
         return CRG_OK;

@@ -43,6 +43,7 @@ struct crg_model_rec {
     uint32_t n_wide = 0, depth = 0;
     float sah = 0.0f;
     float box[6] = {0, 0, 0, 0, 0, 0}; // object-space bounds of its vertices (lo.xyz, hi.xyz)
+    bool box_valid = false;       // box computed (done when the scene first needs placements)
     std::vector<float> xf;        // 16 floats per instance as given; empty = one identity instance
                                   // (the mesh as is when the scene has this one model only)
 };

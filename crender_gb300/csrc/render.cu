@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, cr
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t Wd = set.width, Hd = set.height;
     PathCtx C{pix, 0, set.seed, 0, 0, 0, 0ull, 0ull};
+    uint32_t lanes = __ballot_sync(0xFFFFFFFFu, pix < Wd * Hd);
     if (pix < Wd * Hd) {
         const uint32_t px = pix % Wd, py = pix / Wd;
         const size_t fidx = (size_t)(Wd - 1 - px) + (size_t)(Hd - 1 - py) * Wd;
@@ -79,7 +80,13 @@ __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, cr
         // instead of the longest path of every sample.  A pixel's samples still run
         // and accumulate in order, so the film is unchanged.
         uint32_t s = 0, i = 0;
-        while (s < set.spp) {
+        for (;;) {
+            // the lanes still rendering meet here before every segment, so the warp
+            // enters the traversal together whatever reconvergence points the
+            // compiler chooses (without it a build of this kernel ran 4.1 instead of
+            // 7.2 lanes per warp instruction on the displaced scene, 1.65x slower)
+            lanes = __ballot_sync(lanes, s < set.spp);
+            if (s >= set.spp) break;
             if (i == 0) {
                 C.sample = (uint32_t)(spp0 + s);
                 const f4 g0 = rand4(pix, C.sample, 0, set.seed);
