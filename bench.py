@@ -142,6 +142,19 @@ TRAFFIC_PER_SAMPLE = {"box": 1720.0, "displaced": 1097.0}
 TRAFFIC_SOUP_LAUNCH = 923.3e6
 
 
+# DRAM bytes per traversed ray (read + write) of the extend kernel, from the displaced-scene
+# iteration capture (profiles/wavefront_displaced_iteration_full.md, build B: 795 MB over one
+# full-queue iteration of a 4,194,304-path pool, one ray per path)
+DRAM_PER_RAY = {"extend": 795e6 / 4194304}
+
+
+def traffic_dominant(out, stage):
+    """DRAM traffic of one frame's launches of a traversal stage: ncu bytes per ray x the frame's rays."""
+    w = out.get("work", {})
+    rays = w.get("segments" if stage == "extend" else "shadow_rays")
+    return DRAM_PER_RAY[stage] * rays if rays and stage in DRAM_PER_RAY else None
+
+
 def traffic_estimate(workload, out, units):
     """DRAM traffic per step from the ncu captures above, or None; the batch is
     scaled per scene by its samples (the per-sample traffic of a frame grows in
@@ -154,6 +167,42 @@ def traffic_estimate(workload, out, units):
     if workload in ("box", "displaced") and out.get("form") == "wavefront":
         return TRAFFIC_PER_SAMPLE[workload] * units, "per-sample traffic of one wavefront frame (ncu), times the samples"
     return None, None
+
+
+# L2 hit rates (lts__t_sector_hit_rate) of the traversal kernels from ncu captures on a GB300
+# (profiles/wavefront_displaced_iteration_full.md, build B; profiles/k_intersect_soup_full.md)
+L2_HIT = {"extend": 0.581, "shadow": 0.595, "soup_closest": 0.880, "soup_any": 0.860}
+
+
+def stage_roofline(tuned, work, sh_work, stages, node_bytes, peak):
+    """Roofline of the traversal stages of a wavefront frame and the time share of every stage.
+    Algorithmic bytes of a traversal stage: 48 B per ray (32 B ray in, 16 B hit or flag out) plus
+    node_bytes per wide node visited and 48 B per triangle tested, from the instrumented frame; its
+    time is the sum of its launches' CUDA-event durations over a frame of the host-driven loop."""
+    fuse = tuned.get("fuse", 1) or 1
+    ext_bytes = (work["segments"] * 48 + (work["nodes_visited"] - sh_work["shadow_nodes"]) * node_bytes
+                 + (work["tris_tested"] - sh_work["shadow_tris"]) * 48)
+    sh_bytes = work["shadow_rays"] * 48 + sh_work["shadow_nodes"] * node_bytes + sh_work["shadow_tris"] * 48
+    # which launches carry which traversal: fuse 1 split stages, 2 shadow test inside shade, 3 all inside shade
+    carried = {1: {"extend": ext_bytes, "shadow": sh_bytes}, 2: {"extend": ext_bytes, "shade": sh_bytes},
+               3: {"shade": ext_bytes + sh_bytes}}[fuse]
+    ms = {"extend": stages["extend_ms"], "shade": stages["shade_ms"], "shadow": stages["shadow_ms"],
+          "control_resolve_generate": stages["other_ms"]}
+    total = sum(ms.values())
+    refill = tuned.get("refill", 16)
+    kernels = {"extend": "k_wf_extend_dyn" if refill else "k_wf_extend", "shade": "k_wf_shade",
+               "shadow": "k_wf_shadow_dyn" if refill else "k_wf_shadow"}
+    rows = {}
+    for k, b in carried.items():
+        if ms[k] > 0:
+            gbs = b / (ms[k] / 1e3) / 1e9
+            rows[k] = {"kernel": kernels[k], "algorithmic_bytes": int(b), "ms": ms[k], "achieved_gbs": gbs,
+                       "frac": gbs / peak}
+    dom = max(rows, key=lambda k: ms[k]) if rows else None
+    return {"ms": ms, "share": {k: v / total for k, v in ms.items()} if total else {}, "frame_ms_host_loop": total,
+            "iterations": stages["iterations"], "traversal": rows, "dominant": dom,
+            "how": "one frame through the host-driven loop (host_loop 2) with CUDA events around every stage; "
+                   "traversal work from an instrumented frame"}
 
 
 def workload_config(w):
@@ -579,26 +628,67 @@ def main():
                 f.reset(S)
                 api.render((sb, sd)[si], cam, st, f, S)
 
-        # instrumented wavefront pass (untimed): traversal work for the byte count
+        # instrumented wavefront pass (untimed, host-driven loop): traversal work of each traversal stage
         for f in films:
             f.reset(S)
-        ctx.check(api.render_batch([sb, sd], views, films, dict(tuned, count_work=1), S))
+        ctx.check(api.render_batch([sb, sd], views, films, dict(tuned, count_work=1, host_loop=2), S))
         torch.cuda.synchronize()
         work = api.batch_stats(ctx)
+        sh_work = api.stage_times(ctx)
         rays = work["segments"] + work["shadow_rays"]
-        algo = rays * 48 + work["nodes_visited"] * sd.info()["node_bytes"] + work["tris_tested"] * 48 + units * 12
+        nb = sd.info()["node_bytes"]
+        algo = rays * 48 + work["nodes_visited"] * nb + work["tris_tested"] * 48 + units * 12
         with ClockSampler(local) as clk:
             ms = timer.steps(wave, args.steps, args.warmup)
+        # one more frame through the host-driven loop with CUDA events around every stage (untimed above):
+        # the device time of each kernel stage, for the dominant kernel's roofline and the frame's time shares
+        for f in films:
+            f.reset(S)
+        ctx.check(api.render_batch([sb, sd], views, films, dict(tuned, host_loop=2), S))
+        torch.cuda.synchronize()
+        out["stages"] = stage_roofline(tuned, work, sh_work, api.stage_times(ctx), nb, peak)
+        # per view size: the wavefront form against the megakernel on the views of each resolution
+        sizes = sorted({(st.width, st.height) for _, _, st in views}, key=lambda wh: wh[0] * wh[1])
+        groups = {wh: [i for i, (_, _, st) in enumerate(views) if (st.width, st.height) == wh] for wh in sizes}
+        by_size = {}
+        for wh, idx in groups.items():
+            sv, sf = [views[i] for i in idx], [films[i] for i in idx]
+
+            def wave_part(sv=sv, sf=sf):
+                for f in sf:
+                    f.reset(S)
+                ctx.check(api.render_batch([sb, sd], sv, sf, tuned, S))
+
+            t = timer.steps(wave_part, 1, 1)[0]
+            n = sum(st.width * st.height * st.spp for _, _, st in sv)
+            by_size[f"{wh[0]}x{wh[1]}"] = {"views": len(idx), "samples": n, "wavefront_msamples_per_s": n / t / 1e3}
         wave_leaf = (sb.info()["leaf_max"], sd.info()["leaf_max"])
         sb.build(*MEGA_BVH["box"], stream=S)  # the megakernel runs on its own best BVHs
         sd.build(*MEGA_BVH["displaced"], stream=S)
-        mega_ms = timer.steps(mega, 2, 1)
+        for wh, idx in groups.items():
+            sv, sf = [views[i] for i in idx], [films[i] for i in idx]
+
+            def mega_part(sv=sv, sf=sf):
+                for (si, cam, st), f in zip(sv, sf):
+                    f.reset(S)
+                    api.render((sb, sd)[si], cam, st, f, S)
+
+            t = timer.steps(mega_part, 1, 1)[0]
+            e = by_size[f"{wh[0]}x{wh[1]}"]
+            e["megakernel_msamples_per_s"] = e["samples"] / t / 1e3
+            e["wavefront_over_megakernel"] = e["wavefront_msamples_per_s"] / e["megakernel_msamples_per_s"]
+        out["by_view_size"] = by_size
+        mega_steps, mega_warm = max(3, args.steps // 4), args.warmup
+        mega_ms = timer.steps(mega, mega_steps, mega_warm)
         out["megakernel"] = {"value": units / (sum(mega_ms) / len(mega_ms) / 1e3) / 1e6, "unit": unit,
-                             "ms_per_step": sum(mega_ms) / len(mega_ms),
+                             "ms_per_step": sum(mega_ms) / len(mega_ms), "ms_min": min(mega_ms), "ms_max": max(mega_ms),
+                             "steps": mega_steps, "warmup": mega_warm,
                              "bvh": {k: dict(zip(("width", "treelet", "leaf_max"), v)) for k, v in MEGA_BVH.items()},
                              "how": "same 64 views, one crg_render call per view (the drop-in), on the BVH options "
-                                    "fastest for the megakernel in a sweep of width x leaf size; 1 warm-up + 2 steps"}
-        out["work"] = {**work, "mrays_per_step": rays / 1e6}
+                                    "fastest for the megakernel in a sweep of width x leaf size; the wavefront arm's "
+                                    "warm-up, a quarter of its timed steps (at least 3), L2 flushed between steps"}
+        out["work"] = {**work, "mrays_per_step": rays / 1e6, "shadow_nodes_visited": sh_work["shadow_nodes"],
+                       "shadow_tris_tested": sh_work["shadow_tris"]}
         kernel = "wavefront frame: one graph launch (k_wf_extend / k_wf_shade / k_wf_shadow / control / resolve)"
         launches = None  # counted below from the iteration count
 
@@ -818,6 +908,28 @@ def main():
         fuse = out.get("autotune", {}).get("opts", {}).get("fuse", 1) or 1
         launches = args.steps * (3 + (4 + (3, 2, 1)[fuse - 1]) * int(out["work"]["iterations"]))
     traffic, traffic_src = traffic_estimate(args.workload, out, units)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "traffic_source": traffic_src, "kernel": kernel, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": int(algo)}
+    if args.workload == "batch" and out.get("stages", {}).get("dominant"):
+        # the dominant kernel: the largest traversal stage of the frame, timed by its own CUDA events
+        st = out["stages"]
+        d = st["traversal"][st["dominant"]]
+        frame = dict(roofline, kernel="whole frame (all stages): " + kernel)
+        roofline = {"bound": "hbm", "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                    "frac": d["frac"], "traffic": traffic_dominant(out, st["dominant"]),
+                    "traffic_source": "DRAM bytes per ray of the same kernel in an ncu capture of a displaced-scene "
+                                      "iteration, times the frame's rays of that stage (an upper estimate: the box "
+                                      "scene's rays find its BVH in L1/L2)",
+                    "kernel": d["kernel"] + f" ({st['dominant']} stage, {st['share'][st['dominant']]:.2f} of the frame)",
+                    "peak_kind": peak_kind, "algorithmic_bytes_per_frame": d["algorithmic_bytes"],
+                    "stage_ms_per_frame": d["ms"], "l2_hit_rate": L2_HIT.get(st["dominant"]),
+                    "l2_hit_rate_source": "ncu lts__t_sector_hit_rate of the same kernel on the displaced scene "
+                                          "(profiles/wavefront_displaced_iteration_full.md)",
+                    "stage_share": st["share"], "frame": frame}
+    elif args.workload == "soup":
+        roofline["l2_hit_rate"] = L2_HIT["soup_closest"]
+        roofline["l2_hit_rate_source"] = "ncu capture of the same launch (profiles/k_intersect_soup_full.md)"
     config = workload_config(args.workload)
     if args.workload == "batch":
         config["samples_per_step"] = units
@@ -835,9 +947,7 @@ def main():
             "metric": unit, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "traffic_source": traffic_src, "kernel": kernel, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": int(algo)},
+            "roofline": roofline,
             "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches, **out,
         }
         print(json.dumps(line))

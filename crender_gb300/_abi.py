@@ -80,6 +80,11 @@ class BvhInfo(C.Structure):
     ]
 
 
+class StageTimes(C.Structure):
+    _fields_ = [("extend_ms", C.c_double), ("shade_ms", C.c_double), ("shadow_ms", C.c_double), ("other_ms", C.c_double),
+                ("iterations", C.c_uint64), ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64)]
+
+
 class ModelInfo(C.Structure):
     _fields_ = [
         ("first_prim", C.c_uint32),
@@ -219,7 +224,10 @@ CRG_SIGNATURES = [
     ("crg_backward", C.c_int, [vp, P(Camera), P(Settings), vp, vp, vp, c_stream]),
     ("crg_film_loss_l2", C.c_int, [vp, vp, vp, vp, c_stream]),
     ("crg_render_batch", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
+    ("crg_render_batch_async", C.c_int, [P(vp), C.c_uint32, P(View), P(vp), C.c_uint32, P(WavefrontOpts), c_stream]),
+    ("crg_batch_wait", C.c_int, [vp]),
     ("crg_batch_stats_get", C.c_int, [vp, P(RenderStats)]),
+    ("crg_batch_stage_times_get", C.c_int, [vp, P(StageTimes)]),
     ("crg_autotune_batch", C.c_int, [P(vp), C.c_uint32, P(View), C.c_uint32, P(AutotuneOpts), P(WavefrontOpts),
                                      P(C.c_uint32), P(AutotuneTrial), C.c_uint32, P(C.c_uint32), c_stream]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),

@@ -353,8 +353,9 @@ def render(scene: Scene, camera: dict, settings: _abi.Settings, film: Film, stre
     scene.ctx.check(scene.ctx.lib.crg_render(scene.h, C.byref(cam), C.byref(settings), film.h, stream))
 
 
-def render_batch(scenes, views, films, opts=None, stream=None):
-    """crg_render_batch: views = [(scene_index, camera dict, Settings)], one film each."""
+def render_batch(scenes, views, films, opts=None, stream=None, wait=True):
+    """crg_render_batch (wait) or crg_render_batch_async: views = [(scene_index, camera dict,
+    Settings)], one film each.  Returns the status."""
     ctx = scenes[0].ctx
     sc = (C.c_void_p * len(scenes))(*[s.h.value for s in scenes])
     fl = (C.c_void_p * len(films))(*[f.h.value for f in films])
@@ -364,7 +365,13 @@ def render_batch(scenes, views, films, opts=None, stream=None):
         vs[i].camera = make_camera(cam)
         vs[i].settings = st
     o = _abi.WavefrontOpts(**(opts or {}))
-    return ctx.lib.crg_render_batch(sc, len(scenes), vs, fl, len(views), C.byref(o), stream)
+    call = ctx.lib.crg_render_batch if wait else ctx.lib.crg_render_batch_async
+    return call(sc, len(scenes), vs, fl, len(views), C.byref(o), stream)
+
+
+def batch_wait(ctx) -> int:
+    """crg_batch_wait: the first error of the batches enqueued on ctx (status)."""
+    return ctx.lib.crg_batch_wait(ctx.h)
 
 
 OPT_FIELDS = ("path_pool", "chunk_samples", "block_size", "fetch", "max_iterations", "count_work", "host_loop", "fuse",
@@ -398,6 +405,14 @@ def batch_stats(ctx) -> dict:
     ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))
     return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays, nodes_visited=s.nodes_visited,
                 tris_tested=s.tris_tested, iterations=s.iterations)
+
+
+def stage_times(ctx) -> dict:
+    """crg_batch_stage_times_get: per-stage device time (ms) of the last batch run with
+    host_loop 2, and the shadow stage's share of the counted traversal work."""
+    t = _abi.StageTimes()
+    ctx.check(ctx.lib.crg_batch_stage_times_get(ctx.h, C.byref(t)))
+    return {k: getattr(t, k) for k, _ in t._fields_}
 
 
 # ---------------------------------------------------------------- differentiation

@@ -709,6 +709,7 @@ crg_status crg_context_create(int device, crg_context **out) {
 
 crg_status crg_context_destroy(crg_context *ctx) {
     if (!ctx) return CRG_ERR_INVALID_ARG;
+    batch_state_free(ctx);
     dev_free(ctx->wf_ws);
     dev_free(ctx->post_ws);
     delete ctx;
@@ -1301,8 +1302,9 @@ crg_status crg_render(crg_scene *scene, const crg_camera *camera, const crg_sett
     return CRG_OK;
 }
 
-crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, crg_film *const *films,
-                            uint32_t nviews, const crg_wavefront_opts *opts, crg_stream stream) {
+namespace {
+crg_status batch_call(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, crg_film *const *films,
+                      uint32_t nviews, const crg_wavefront_opts *opts, crg_stream stream, bool wait) {
     if (!scenes || nscenes == 0 || !scenes[0]) return CRG_ERR_INVALID_ARG;
     crg_context *ctx = scenes[0]->ctx;
     if (!views || !films || nviews == 0) return set_error(ctx, CRG_ERR_INVALID_ARG, "empty batch");
@@ -1342,16 +1344,39 @@ crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const cr
         if (opts->refill) o.refill = opts->refill == 0xFFFFFFFFu ? 0u : opts->refill;
     }
     if ((o.block_size != 64 && o.block_size != 128 && o.block_size != 256) || o.fetch % 32 || o.fetch > 4096 ||
-        o.path_pool > (1u << 28) || o.fuse > 3 || o.refill > 32)
+        o.path_pool > (1u << 28) || o.fuse > 3 || o.refill > 32 || o.host_loop > 2)
         return set_error(ctx, CRG_ERR_INVALID_ARG,
                          "wavefront options: block_size 64/128/256, fetch a multiple of 32, path_pool <= 2^28, fuse <= 3, "
-                         "refill <= 32");
-    return render_batch(ctx, scenes, nscenes, views, films, nviews, o, (cudaStream_t)stream, &ctx->batch_stats);
+                         "refill <= 32, host_loop <= 2");
+    return render_batch(ctx, scenes, nscenes, views, films, nviews, o, (cudaStream_t)stream, wait);
+}
+} // namespace
+
+crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views, crg_film *const *films,
+                            uint32_t nviews, const crg_wavefront_opts *opts, crg_stream stream) {
+    return batch_call(scenes, nscenes, views, films, nviews, opts, stream, true);
+}
+
+crg_status crg_render_batch_async(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
+                                  crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
+                                  crg_stream stream) {
+    return batch_call(scenes, nscenes, views, films, nviews, opts, stream, false);
+}
+
+crg_status crg_batch_wait(crg_context *ctx) {
+    if (!ctx) return CRG_ERR_INVALID_ARG;
+    return batch_wait(ctx);
 }
 
 crg_status crg_batch_stats_get(const crg_context *ctx, crg_render_stats *stats) {
     if (!ctx || !stats) return CRG_ERR_INVALID_ARG;
     *stats = ctx->batch_stats;
+    return CRG_OK;
+}
+
+crg_status crg_batch_stage_times_get(const crg_context *ctx, crg_stage_times *times) {
+    if (!ctx || !times) return CRG_ERR_INVALID_ARG;
+    *times = ctx->stage_times;
     return CRG_OK;
 }
 

@@ -10,6 +10,10 @@
 
 #include "../../include/crg.h"
 
+namespace crg {
+struct BatchState; // wavefront.cu
+}
+
 // Device buffer owned by a scene, film or context.
 struct DevBuf {
     void *ptr = nullptr;
@@ -24,6 +28,8 @@ struct crg_context {
     DevBuf wf_ws; // wavefront workspace (path pool, queues, sample slots), grow-only
     DevBuf post_ws; // post-process ping-pong images, grow-only
     crg_render_stats batch_stats{};
+    crg_stage_times stage_times{}; // of the last crg_render_batch run with host_loop 2
+    crg::BatchState *batch = nullptr; // wavefront graphs, pinned staging, batches in flight (wavefront.cu)
     struct Tuned {
         crg_wavefront_opts opts;
         uint32_t width;
@@ -172,9 +178,13 @@ crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &
 crg_status launch_loss_l2(crg_film *f, const float *target, float *adj, double *loss, cudaStream_t stream);
 
 // wavefront.cu
+// Enqueues a batch on `stream` (wait = false) or runs it to completion (wait = true).
 crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
                         crg_film *const *films, uint32_t nviews, const crg_wavefront_opts &o, cudaStream_t stream,
-                        crg_render_stats *stats);
+                        bool wait);
+// Waits for the batches enqueued on ctx; the first error among them, and their statistics.
+crg_status batch_wait(crg_context *ctx);
+void batch_state_free(crg_context *ctx);
 
 } // namespace crg
 

@@ -24,6 +24,9 @@
 // runs before the shade kernel of bounce i + 1.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
 #include <vector>
 
 #include "render_common.cuh"
@@ -67,7 +70,8 @@ struct Ctrl {
     unsigned int iterations, max_iterations;
     unsigned long long issued;   // next gid to issue in `chunk`
     unsigned long long segments, shadow;
-    unsigned long long nodes, tris; // traversal work (instrumented variant only)
+    unsigned long long nodes, tris; // traversal work (instrumented variant only): closest hits
+    unsigned long long nodes_sh, tris_sh; // the same for the shadow tests (split and shade+shadow stages)
 };
 
 constexpr uint32_t kFinish = 1u << 31;    // meta.x flag: finish after the shadow test
@@ -309,9 +313,9 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
             finish_and_refill(w, c, valid && finishing, slot, Lv, off);
         }
     }
-    if (CNT && FUSE >= 1) {
-        atomicAdd(&c->nodes, nodes);
-        atomicAdd(&c->tris, tris);
+    if (CNT && FUSE >= 1) { // FUSE 1: the shadow test's work; FUSE 2: closest hit and shadow test together
+        atomicAdd(FUSE == 1 ? &c->nodes_sh : &c->nodes, nodes);
+        atomicAdd(FUSE == 1 ? &c->tris_sh : &c->tris, tris);
     }
 }
 
@@ -362,8 +366,8 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
         }
     }
     if (CNT) {
-        atomicAdd(&c->nodes, nodes);
-        atomicAdd(&c->tris, tris);
+        atomicAdd(&c->nodes_sh, nodes);
+        atomicAdd(&c->tris_sh, tris);
     }
 }
 
@@ -435,8 +439,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_shadow_dyn(Wf w) {
         st, err);
     if (err) atomicOr(&c->error, 1u);
     if (CNT) {
-        atomicAdd(&c->nodes, (unsigned long long)st.nodes);
-        atomicAdd(&c->tris, (unsigned long long)st.tris);
+        atomicAdd(&c->nodes_sh, (unsigned long long)st.nodes);
+        atomicAdd(&c->tris_sh, (unsigned long long)st.tris);
     }
 }
 
@@ -616,55 +620,160 @@ void launch_bounce(const Wf &wf, const Grids &g, uint32_t block, cudaStream_t st
 
 // Host-driven loop: the same kernels launched from the host, which polls the
 // done flag every 8 iterations (for profilers that cannot see into graphs
-// with conditional nodes, and for runtimes without them).
+// with conditional nodes, and for runtimes without them).  With `times`, CUDA
+// events on the stream bracket every stage of every iteration and the device
+// time of each stage is summed into it: extend, shade, shadow, and the
+// control / resolve / generate kernels.
 template <int W, int FUSE, bool CNT, bool INST>
 crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &bg, uint32_t block, uint32_t max_iters,
-                    cudaStream_t st) {
+                    cudaStream_t st, crg_stage_times *times) {
     unsigned int *done_h = nullptr;
     if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "host-driven loop: pinned flag allocation failed (injected fault)");
     CRG_CUDA(ctx, cudaHostAlloc(&done_h, sizeof(unsigned int), cudaHostAllocDefault));
+    constexpr int kWin = 8, kMarks = 5; // iterations between polls; events per iteration
+    cudaEvent_t ev[kWin * kMarks] = {};
     crg_status rc = CRG_OK;
-    for (uint32_t it = 0; it < max_iters + 8; ++it) {
-        launch_bounce<W, FUSE, CNT, INST>(wf, bg, block, st);
+    if (times) {
+        *times = crg_stage_times{};
+        for (int k = 0; k < kWin * kMarks && rc == CRG_OK; ++k) {
+            const cudaError_t e = cudaEventCreate(&ev[k]);
+            if (e != cudaSuccess) rc = cuda_error(ctx, e, "cudaEventCreate");
+        }
+    }
+    auto mark = [&](uint32_t it, int m) {
+        if (times) cudaEventRecord(ev[(it % kWin) * kMarks + m], st);
+    };
+    for (uint32_t it = 0; rc == CRG_OK && it < max_iters + 8; ++it) {
+        mark(it, 0);
+        if (FUSE <= 1) {
+            if (!INST && wf.refill) k_wf_extend_dyn<W, CNT><<<bg.ext, block, 0, st>>>(wf);
+            else k_wf_extend<W, CNT, INST><<<bg.ext, block, 0, st>>>(wf);
+        }
+        mark(it, 1);
+        k_wf_shade<W, FUSE, CNT, INST><<<bg.shade, block, 0, st>>>(wf);
+        mark(it, 2);
+        if (FUSE == 0) {
+            if (!INST && wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<bg.shadow, block, 0, st>>>(wf);
+            else k_wf_shadow<W, CNT, INST><<<bg.shadow, block, 0, st>>>(wf);
+        }
+        mark(it, 3);
         k_wf_control<<<1, 32, 0, st>>>(wf, 0, 0);
         k_wf_resolve<<<grid, 256, 0, st>>>(wf);
         k_wf_generate<<<grid, 256, 0, st>>>(wf, 0);
         k_wf_generated<<<1, 32, 0, st>>>(wf, 0);
-        if ((it & 7) == 7) {
+        mark(it, 4);
+        if ((it % kWin) == kWin - 1) {
             cudaError_t e = cudaMemcpyAsync(done_h, &wf.ctrl->done, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) {
                 rc = cuda_error(ctx, e, "wavefront host loop");
                 break;
             }
+            if (times)
+                for (int k = 0; k < kWin; ++k) {
+                    float ms[4] = {0, 0, 0, 0};
+                    for (int m = 0; m < 4; ++m) cudaEventElapsedTime(&ms[m], ev[k * kMarks + m], ev[k * kMarks + m + 1]);
+                    times->extend_ms += ms[0];
+                    times->shade_ms += ms[1];
+                    times->shadow_ms += ms[2];
+                    times->other_ms += ms[3];
+                    times->iterations++;
+                }
             if (*done_h) break;
         }
     }
+    for (int k = 0; k < kWin * kMarks; ++k)
+        if (ev[k]) cudaEventDestroy(ev[k]);
     cudaFreeHost(done_h);
     return rc;
 }
 
-template <int W, int FUSE, bool CNT, bool INST>
-crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st,
-               bool host_loop) {
-    // prologue on the caller's stream
-    k_wf_start<<<1, 32, 0, st>>>(wf.ctrl, max_iters);
-    k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
-    k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
-    CRG_CUDA(ctx, cudaGetLastError());
-    const Grids bg = bounce_grids<W, FUSE, CNT, INST>(wf, block, ctx->sm_count);
-    if (host_loop) return run_host<W, FUSE, CNT, INST>(ctx, wf, grid, bg, block, max_iters, st);
-    // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
+// Wavefront graphs are kept per context: a graph's kernel nodes hold the Wf
+// argument by value, so a batch whose Wf (workspace pointers, pool size,
+// chunk count, options) and launch shape equal an earlier batch's relaunches
+// that batch's instantiated graph; only the plan arrays it reads change.
+struct GraphEntry {
+    std::string key;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr; // recorded after the entry's last launch
+    uint64_t used = 0;
+};
+constexpr size_t kMaxGraphs = 8;
+
+} // namespace
+
+// Per-context state of the batched form: cached graphs, the pinned staging
+// buffers of the host-side plan (two, alternating, each guarded by the event
+// of its last copy), and the control blocks of batches in flight (two pinned
+// slots, each with the event of its readback).
+struct BatchState {
+    std::vector<GraphEntry> graphs;
+    uint64_t tick = 0;
+    void *stage[2] = {nullptr, nullptr};
+    size_t stage_cap[2] = {0, 0};
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    int stage_next = 0;
+    void *ctrl[2] = {nullptr, nullptr}; // a Ctrl each
+    cudaEvent_t ctrl_ev[2] = {nullptr, nullptr};
+    bool busy[2] = {false, false};
+    uint64_t seq[2] = {0, 0}, next_seq = 1;
+    crg_render_stats stats[2] = {};
+    uint32_t loop_mode[2] = {0, 0}; // crg_wavefront_opts::host_loop of the slot's batch
+    int ctrl_next = 0;
+    crg_status sticky = CRG_OK; // first error of the batches collected since the last wait
+    std::string sticky_msg;
+};
+
+namespace {
+
+crg_status state_of(crg_context *ctx, BatchState *&b) {
+    if (!ctx->batch) {
+        if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "batch state allocation failed (injected fault)");
+        ctx->batch = new (std::nothrow) BatchState();
+        if (!ctx->batch) return set_error(ctx, CRG_ERR_OOM, "batch state allocation failed");
+    }
+    b = ctx->batch;
+    return CRG_OK;
+}
+
+// The instantiated graph of one loop body, from the cache or built now.
+template <int W, int FUSE, bool CNT, bool INST>
+crg_status cached_graph(crg_context *ctx, const Wf &wf, const Grids &bg, uint32_t grid, uint32_t block, GraphEntry *&out) {
+    BatchState *B = nullptr;
+    crg_status rc = state_of(ctx, B);
+    if (rc != CRG_OK) return rc;
+    const uint32_t shape[9] = {(uint32_t)W, (uint32_t)FUSE, CNT ? 1u : 0u, INST ? 1u : 0u, grid, block,
+                               bg.ext,      bg.shade,       bg.shadow};
+    std::string key((const char *)&wf, sizeof(Wf));
+    key.append((const char *)shape, sizeof(shape));
+    for (GraphEntry &g : B->graphs)
+        if (g.key == key) {
+            g.used = ++B->tick;
+            out = &g;
+            return CRG_OK;
+        }
+    if (B->graphs.size() >= kMaxGraphs) { // evict the least recently used, once its last launch is done
+        size_t lru = 0;
+        for (size_t k = 1; k < B->graphs.size(); ++k)
+            if (B->graphs[k].used < B->graphs[lru].used) lru = k;
+        GraphEntry &g = B->graphs[lru];
+        cudaEventSynchronize(g.done);
+        cudaEventDestroy(g.done);
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+        B->graphs.erase(B->graphs.begin() + (long)lru);
+    }
+    // one graph: WHILE (not done) { extend, shade, shadow, control, resolve, generate }
+    GraphEntry e;
+    e.key = key;
     cudaStream_t cap = nullptr;
-    crg_status rc = CRG_OK;
     do {
-        cudaError_t e;
-        if ((e = cudaGraphCreate(&graph, 0)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphCreate"); break; }
+        cudaError_t er;
+        if ((er = cudaGraphCreate(&e.graph, 0)) != cudaSuccess) { rc = cuda_error(ctx, er, "cudaGraphCreate"); break; }
         cudaGraphConditionalHandle handle;
-        if ((e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) {
-            rc = cuda_error(ctx, e, "cudaGraphConditionalHandleCreate");
+        if ((er = cudaGraphConditionalHandleCreate(&handle, e.graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaGraphConditionalHandleCreate");
             break;
         }
         cudaGraphNodeParams cp = {};
@@ -673,17 +782,17 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
         cp.conditional.type = cudaGraphCondTypeWhile;
         cp.conditional.size = 1;
         cudaGraphNode_t node;
-        if ((e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp)) != cudaSuccess) {
-            rc = cuda_error(ctx, e, "cudaGraphAddNode(while)");
+        if ((er = cudaGraphAddNode(&node, e.graph, nullptr, nullptr, 0, &cp)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaGraphAddNode(while)");
             break;
         }
         cudaGraph_t body = cp.conditional.phGraph_out[0];
-        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) {
-            rc = cuda_error(ctx, e, "cudaStreamCreate");
+        if ((er = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaStreamCreate");
             break;
         }
-        if ((e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess) {
-            rc = cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph");
+        if ((er = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaStreamBeginCaptureToGraph");
             break;
         }
         launch_bounce<W, FUSE, CNT, INST>(wf, bg, block, cap);
@@ -691,17 +800,47 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
         k_wf_resolve<<<grid, 256, 0, cap>>>(wf);
         k_wf_generate<<<grid, 256, 0, cap>>>(wf, 0);
         k_wf_generated<<<1, 32, 0, cap>>>(wf, 0);
-        e = cudaStreamEndCapture(cap, &body);
-        if (e != cudaSuccess) { rc = cuda_error(ctx, e, "cudaStreamEndCapture"); break; }
-        if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphInstantiate"); break; }
-        if ((e = cudaGraphLaunch(exec, st)) != cudaSuccess) { rc = cuda_error(ctx, e, "cudaGraphLaunch"); break; }
-        // the executable graph is destroyed below: wait for it first
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) { rc = cuda_error(ctx, e, "wavefront frame"); break; }
+        er = cudaStreamEndCapture(cap, &body);
+        if (er != cudaSuccess) { rc = cuda_error(ctx, er, "cudaStreamEndCapture"); break; }
+        if ((er = cudaGraphInstantiate(&e.exec, e.graph, 0)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaGraphInstantiate");
+            break;
+        }
+        if ((er = cudaEventCreateWithFlags(&e.done, cudaEventDisableTiming)) != cudaSuccess) {
+            rc = cuda_error(ctx, er, "cudaEventCreate");
+            break;
+        }
     } while (0);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     if (cap) cudaStreamDestroy(cap);
-    return rc;
+    if (rc != CRG_OK) {
+        if (e.exec) cudaGraphExecDestroy(e.exec);
+        if (e.graph) cudaGraphDestroy(e.graph);
+        return rc;
+    }
+    e.used = ++B->tick;
+    B->graphs.push_back(e);
+    out = &B->graphs.back();
+    return CRG_OK;
+}
+
+template <int W, int FUSE, bool CNT, bool INST>
+crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, uint32_t max_iters, cudaStream_t st,
+               uint32_t host_loop) {
+    // prologue on the caller's stream
+    k_wf_start<<<1, 32, 0, st>>>(wf.ctrl, max_iters);
+    k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
+    k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
+    CRG_CUDA(ctx, cudaGetLastError());
+    const Grids bg = bounce_grids<W, FUSE, CNT, INST>(wf, block, ctx->sm_count);
+    if (host_loop)
+        return run_host<W, FUSE, CNT, INST>(ctx, wf, grid, bg, block, max_iters, st,
+                                            host_loop == 2 ? &ctx->stage_times : nullptr);
+    GraphEntry *g = nullptr;
+    const crg_status rc = cached_graph<W, FUSE, CNT, INST>(ctx, wf, bg, grid, block, g);
+    if (rc != CRG_OK) return rc;
+    CRG_CUDA(ctx, cudaGraphLaunch(g->exec, st));
+    CRG_CUDA(ctx, cudaEventRecord(g->done, st));
+    return CRG_OK;
 }
 
 template <int W, int FUSE>
@@ -737,7 +876,7 @@ int occupancy(uint32_t width, uint32_t fuse, int block) {
 
 template <int W>
 crg_status dispatch_w(crg_context *ctx, const Wf &wf, uint32_t fuse, bool cnt, bool inst, uint32_t grid, uint32_t block,
-                      uint32_t max_iters, cudaStream_t st, bool hl) {
+                      uint32_t max_iters, cudaStream_t st, uint32_t hl) {
     if (inst) // batches with placements run the split stages
         return cnt ? run<W, 0, true, true>(ctx, wf, grid, block, max_iters, st, hl)
                    : run<W, 0, false, true>(ctx, wf, grid, block, max_iters, st, hl);
@@ -752,7 +891,7 @@ crg_status dispatch_w(crg_context *ctx, const Wf &wf, uint32_t fuse, bool cnt, b
 }
 
 crg_status dispatch(crg_context *ctx, const Wf &wf, uint32_t width, uint32_t fuse, bool cnt, bool inst, uint32_t grid,
-                    uint32_t block, uint32_t max_iters, cudaStream_t st, bool hl) {
+                    uint32_t block, uint32_t max_iters, cudaStream_t st, uint32_t hl) {
     switch (width) {
     case 2: return dispatch_w<2>(ctx, wf, fuse, cnt, inst, grid, block, max_iters, st, hl);
     case 4: return dispatch_w<4>(ctx, wf, fuse, cnt, inst, grid, block, max_iters, st, hl);
@@ -760,11 +899,77 @@ crg_status dispatch(crg_context *ctx, const Wf &wf, uint32_t width, uint32_t fus
     }
 }
 
+std::string ctx_message(const crg_context *ctx) {
+    std::lock_guard<std::mutex> lock(ctx->error_mutex);
+    return ctx->last_error;
+}
+
+// Reads back the control block of the batch in `slot` (waiting for it), turns
+// its error word into a status, and keeps its statistics.
+crg_status collect(crg_context *ctx, BatchState *B, int slot) {
+    if (!B->busy[slot]) return CRG_OK;
+    B->busy[slot] = false;
+    CRG_CUDA(ctx, cudaEventSynchronize(B->ctrl_ev[slot]));
+    const Ctrl &c = *(const Ctrl *)B->ctrl[slot];
+    crg_render_stats &s = B->stats[slot];
+    s.segments = c.segments;
+    s.shadow_rays = c.shadow;
+    s.nodes_visited = c.nodes + c.nodes_sh;
+    s.tris_tested = c.tris + c.tris_sh;
+    s.iterations = c.iterations;
+    ctx->batch_stats = s;
+    if (B->loop_mode[slot] == 2) {
+        ctx->stage_times.shadow_nodes = c.nodes_sh;
+        ctx->stage_times.shadow_tris = c.tris_sh;
+    }
+    if (c.error & 2u) return set_error(ctx, CRG_ERR_TIMEOUT, "wavefront: iteration cap reached before the batch drained");
+    if (c.error & 1u) return set_error(ctx, CRG_ERR_DEVICE, "wavefront: traversal stack overflow");
+    return CRG_OK;
+}
+
 } // namespace
+
+crg_status batch_wait(crg_context *ctx) {
+    BatchState *B = ctx->batch;
+    if (!B) return CRG_OK;
+    // oldest first, so the statistics left are the last batch's
+    const int first = (B->busy[0] && B->busy[1]) ? (B->seq[0] < B->seq[1] ? 0 : 1) : (B->busy[0] ? 0 : 1);
+    for (int k = 0; k < 2; ++k) {
+        const crg_status rc = collect(ctx, B, first ^ k);
+        if (rc != CRG_OK && !B->sticky) {
+            B->sticky = rc;
+            B->sticky_msg = ctx_message(ctx);
+        }
+    }
+    const crg_status rc = B->sticky;
+    if (rc != CRG_OK) set_error(ctx, rc, B->sticky_msg);
+    B->sticky = CRG_OK;
+    B->sticky_msg.clear();
+    return rc;
+}
+
+void batch_state_free(crg_context *ctx) {
+    BatchState *B = ctx->batch;
+    if (!B) return;
+    cudaDeviceSynchronize();
+    for (GraphEntry &g : B->graphs) {
+        if (g.done) cudaEventDestroy(g.done);
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (B->stage[k]) cudaFreeHost(B->stage[k]);
+        if (B->stage_ev[k]) cudaEventDestroy(B->stage_ev[k]);
+        if (B->ctrl[k]) cudaFreeHost(B->ctrl[k]);
+        if (B->ctrl_ev[k]) cudaEventDestroy(B->ctrl_ev[k]);
+    }
+    delete B;
+    ctx->batch = nullptr;
+}
 
 crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
                         crg_film *const *films, uint32_t nviews, const crg_wavefront_opts &o, cudaStream_t st,
-                        crg_render_stats *stats) {
+                        bool wait) {
     // ---- host-side plan: views, segments, chunks
     const uint32_t width = scenes[0]->width;
     std::vector<SceneDev> sdev(nscenes);
@@ -784,7 +989,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
         total += (unsigned long long)V.npix * V.set.spp;
     }
     if (total == 0) { // nothing to trace: films and their sample counts stay as they are
-        if (stats) *stats = crg_render_stats{};
+        ctx->batch_stats = crg_render_stats{};
         return CRG_OK;
     }
     const unsigned long long C = o.chunk_samples;
@@ -873,10 +1078,33 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.qb = (uint32_t *)take(n_q);
     wf.qsh = (uint32_t *)take(n_q);
     wf.slots = (float4 *)take(n_slots);
-    CRG_CUDA(ctx, cudaMemcpyAsync(d_sc, sdev.data(), sizeof(SceneDev) * nscenes, cudaMemcpyHostToDevice, st));
-    CRG_CUDA(ctx, cudaMemcpyAsync(d_vd, vdev.data(), sizeof(ViewDev) * nviews, cudaMemcpyHostToDevice, st));
-    CRG_CUDA(ctx, cudaMemcpyAsync(d_sg, segs.data(), sizeof(Segment) * segs.size(), cudaMemcpyHostToDevice, st));
-    CRG_CUDA(ctx, cudaMemcpyAsync(d_ch, chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, st));
+    // the plan goes to the device through a pinned staging buffer (a copy from pageable memory
+    // would wait for the stream), alternating between two so that the host can prepare the next
+    // batch while this one's copy is pending
+    BatchState *B = nullptr;
+    if ((rc = state_of(ctx, B)) != CRG_OK) return rc;
+    {
+        const int k = B->stage_next;
+        B->stage_next ^= 1;
+        const size_t plan = n_sc + n_vd + n_sg + n_ch;
+        if (B->stage_ev[k]) CRG_CUDA(ctx, cudaEventSynchronize(B->stage_ev[k]));
+        else CRG_CUDA(ctx, cudaEventCreateWithFlags(&B->stage_ev[k], cudaEventDisableTiming));
+        if (B->stage_cap[k] < plan) {
+            if (B->stage[k]) cudaFreeHost(B->stage[k]);
+            B->stage[k] = nullptr;
+            B->stage_cap[k] = 0;
+            if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "pinned plan staging failed (injected fault)");
+            CRG_CUDA(ctx, cudaHostAlloc(&B->stage[k], plan, cudaHostAllocDefault));
+            B->stage_cap[k] = plan;
+        }
+        char *h = (char *)B->stage[k];
+        std::memcpy(h, sdev.data(), sizeof(SceneDev) * nscenes);
+        std::memcpy(h + n_sc, vdev.data(), sizeof(ViewDev) * nviews);
+        std::memcpy(h + n_sc + n_vd, segs.data(), sizeof(Segment) * segs.size());
+        std::memcpy(h + n_sc + n_vd + n_sg, chunks.data(), sizeof(Chunk) * chunks.size());
+        CRG_CUDA(ctx, cudaMemcpyAsync(d_sc, h, plan, cudaMemcpyHostToDevice, st)); // d_sc .. d_ch are contiguous
+        CRG_CUDA(ctx, cudaEventRecord(B->stage_ev[k], st));
+    }
     // persistent grid: resident blocks of the launched kernels on every SM
     const uint32_t fuse = instanced ? 0u : (o.fuse ? o.fuse - 1 : 0); // fusion level 0..2 (split with placements)
     int per_sm = occupancy(width, fuse, (int)o.block_size);
@@ -888,24 +1116,35 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     for (const Chunk &ch : chunks) iters += ((ch.gid_end - ch.gid_begin) / std::max<uint32_t>(P, 1) + 2) * (maxb + 2) * 4;
     uint32_t max_iters = (uint32_t)std::min<unsigned long long>(iters, 0x7FFFFFFFull);
     if (o.max_iterations) max_iters = o.max_iterations;
-    const bool cnt = o.count_work != 0, hl = o.host_loop != 0;
+    const bool cnt = o.count_work != 0;
+    const uint32_t hl = o.host_loop;
+    // the control block comes back through a pinned slot, read when the batch is waited for
+    const int slot = B->ctrl_next;
+    if (B->busy[slot]) { // the slot's earlier batch: collect it first
+        if ((rc = collect(ctx, B, slot)) != CRG_OK && !B->sticky) {
+            B->sticky = rc;
+            B->sticky_msg = ctx_message(ctx);
+        }
+    }
+    if (!B->ctrl[slot]) {
+        if (fault_injected()) return set_error(ctx, CRG_ERR_OOM, "pinned control block failed (injected fault)");
+        CRG_CUDA(ctx, cudaHostAlloc(&B->ctrl[slot], sizeof(Ctrl), cudaHostAllocDefault));
+        CRG_CUDA(ctx, cudaEventCreateWithFlags(&B->ctrl_ev[slot], cudaEventDisableTiming));
+    }
     rc = dispatch(ctx, wf, width, fuse, cnt, instanced, grid, o.block_size, max_iters, st, hl);
     if (rc != CRG_OK) return rc;
-    Ctrl host{};
-    CRG_CUDA(ctx, cudaMemcpyAsync(&host, wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
-    CRG_CUDA(ctx, cudaStreamSynchronize(st));
-    if (host.error & 2u) return set_error(ctx, CRG_ERR_TIMEOUT, "wavefront: iteration cap reached before the batch drained");
-    if (host.error & 1u) return set_error(ctx, CRG_ERR_DEVICE, "wavefront: traversal stack overflow");
+    CRG_CUDA(ctx, cudaMemcpyAsync(B->ctrl[slot], wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
+    CRG_CUDA(ctx, cudaEventRecord(B->ctrl_ev[slot], st));
+    B->busy[slot] = true;
+    B->seq[slot] = B->next_seq++;
+    B->stats[slot] = crg_render_stats{};
+    B->stats[slot].samples = total;
+    B->loop_mode[slot] = hl;
+    B->ctrl_next ^= 1;
+    if (hl != 2) ctx->stage_times = crg_stage_times{};
+    // sample indices of the films' next calls continue after this batch's
     for (uint32_t v = 0; v < nviews; ++v) films[v]->spp += vdev[v].set.spp;
-    if (stats) {
-        stats->samples = total;
-        stats->segments = host.segments;
-        stats->shadow_rays = host.shadow;
-        stats->nodes_visited = host.nodes;
-        stats->tris_tested = host.tris;
-        stats->iterations = host.iterations;
-    }
-    return CRG_OK;
+    return wait ? batch_wait(ctx) : CRG_OK;
 }
 
 } // namespace crg

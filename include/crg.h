@@ -531,7 +531,9 @@ typedef struct crg_wavefront_opts {
     uint32_t count_work;    /* 1 = instrumented kernels: crg_batch_stats_get also reports
                                nodes visited and triangles tested */
     uint32_t host_loop;     /* 1 = drive the loop from the host instead of one graph with a
-                               device-side condition (same kernels; for profilers) */
+                               device-side condition (same kernels; for profilers); 2 = the
+                               same, timing every stage with CUDA events on the stream
+                               (crg_batch_stage_times_get) */
     uint32_t fuse;          /* stage fusion (films are identical for every value; default 1):
                                1 = separate extend / shade / shadow kernels and queues;
                                2 = the shadow test runs inside shade (no shadow queue);
@@ -551,10 +553,29 @@ typedef struct crg_wavefront_opts {
  * megakernel's.  AOV planes are not written.  All scenes must be built with the
  * same width and context; films must be distinct.  Replaces the per-pass loop
  * of the renderer (src/render/renderer.cpp:116-144) for many cameras at once.
- * Calls on one context must not overlap (they share its workspace). */
+ * Calls on one context must not overlap (they share its workspace).  This call
+ * waits for the batch (crg_render_batch_async does not). */
 crg_status crg_render_batch(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
                             crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
                             crg_stream stream);
+
+/* Stream-ordered form of crg_render_batch: enqueues the batch on `stream` and
+ * returns without waiting for it, so the host prepares the next batch (or
+ * other work) while this one renders.  The instantiated graph of the loop is
+ * kept by the context and relaunched for every later batch of the same shape
+ * (views, segments, chunks, path pool, options): only the plan it reads is
+ * copied, through pinned staging buffers.  Film sample counts advance at
+ * once; the films' contents follow the stream.  Errors found on the device
+ * (iteration cap, stack overflow) are reported by crg_batch_wait, which also
+ * makes crg_batch_stats_get describe the last batch.  Batches of one context
+ * must be enqueued on one stream (they share its workspace); the host waits
+ * only when it is two batches ahead of the device.  No reference counterpart
+ * (the reference's loop, renderer.cpp:116-144, runs one pass at a time). */
+crg_status crg_render_batch_async(crg_scene *const *scenes, uint32_t nscenes, const crg_view *views,
+                                  crg_film *const *films, uint32_t nviews, const crg_wavefront_opts *opts,
+                                  crg_stream stream);
+/* Waits for every batch enqueued on ctx; returns the first error among them. */
+crg_status crg_batch_wait(crg_context *ctx);
 
 /* Autotuner of the wavefront form.  Renders a reduced copy of the batch (each
  * view's spp scaled down so the trial holds about sample_budget samples, into
@@ -641,6 +662,21 @@ typedef struct crg_render_stats {
 crg_status crg_render_stats_get(const crg_scene *scene, crg_render_stats *stats);
 /* Statistics of the last crg_render_batch on this context. */
 crg_status crg_batch_stats_get(const crg_context *ctx, crg_render_stats *stats);
+
+/* Device time of each stage of the last crg_render_batch run with
+ * host_loop = 2 (all zero otherwise), summed over its loop iterations from
+ * CUDA events on the launching stream: extend (closest hits), shade, shadow
+ * (NEE any hits; zero when fused into shade), and the control / resolve /
+ * generate kernels.  With count_work, the shadow stage's share of
+ * crg_render_stats::nodes_visited / tris_tested (the rest is extend's).
+ * No reference counterpart (the reference's timer, src/render/timer.h, times
+ * whole passes). */
+typedef struct crg_stage_times {
+    double extend_ms, shade_ms, shadow_ms, other_ms;
+    uint64_t iterations;
+    uint64_t shadow_nodes, shadow_tris;
+} crg_stage_times;
+crg_status crg_batch_stage_times_get(const crg_context *ctx, crg_stage_times *times);
 /* Turn on per-launch counting of segments, shadow rays, nodes visited and
  * triangles tested for crg_render (runs an instrumented kernel variant). */
 crg_status crg_scene_set_counting(crg_scene *scene, int enabled);

@@ -47,6 +47,7 @@ def test_struct_layouts_match_c(tmp_path):
     structs = {"crg_ray": _abi.Ray, "crg_hit": _abi.Hit, "crg_material": _abi.Material, "crg_sun": _abi.Sun,
                "crg_camera": _abi.Camera, "crg_settings": _abi.Settings, "crg_build_opts": _abi.BuildOpts,
                "crg_bvh_info": _abi.BvhInfo, "crg_render_stats": _abi.RenderStats, "crg_model_info": _abi.ModelInfo,
+               "crg_stage_times": _abi.StageTimes,
                "crg_post_settings": _abi.PostSettings}
     lines = []
     for cname, py in structs.items():

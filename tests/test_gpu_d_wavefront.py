@@ -225,3 +225,108 @@ def test_autotune_leaf_sizes(ctx):
     finally:
         sa.close()
         sb.close()
+
+
+@pytest.mark.parametrize("fuse", [1, 2])
+def test_stage_timing_and_shadow_work_split(ctx, fuse):
+    """host_loop 2 times every stage with CUDA events (crg_batch_stage_times_get)
+    and renders the megakernel's film; with count_work the shadow stage's share
+    of the traversal work is reported apart from the closest hits'."""
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    st = api.make_settings(64, 48, 8, 8, 3, 1, 11, 64 / 48)
+    f = api.Film(ctx, st.width, st.height, f64=True)
+    ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], dict(host_loop=2, count_work=1, fuse=fuse,
+                                                                       path_pool=4096)))
+    work, t = api.batch_stats(ctx), api.stage_times(ctx)
+    _same(f.download(f64=True), _mega(ctx, s, sc["camera"], st))
+    assert 0 < t["shadow_nodes"] < work["nodes_visited"] and 0 < t["shadow_tris"] < work["tris_tested"]
+    assert t["iterations"] >= work["iterations"] - 8
+    assert t["extend_ms"] > 0 and t["shade_ms"] > 0 and t["other_ms"] > 0
+    assert (t["shadow_ms"] > 0) == (fuse == 1)  # fuse 2 tests the shadow rays inside shade
+    ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], dict(path_pool=4096)))
+    assert api.stage_times(ctx)["extend_ms"] == 0  # only host_loop 2 times stages
+    f.close()
+    s.close()
+
+
+def test_async_batches_overlap_the_host_and_match_the_synchronous_form(ctx):
+    """crg_render_batch_async returns once the batch is enqueued: two batches in
+    a row on one stream leave the stream busy when the second call returns,
+    crg_batch_wait then reports success, and the films equal those of the
+    synchronous form (the cached graph relaunched with a new plan)."""
+    import ctypes as C
+    import time
+
+    from test_zz_no_alloc import _cudart
+
+    rt = _cudart()
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1, 3)
+    sts = [api.make_settings(512, 512, 32, 8, 3, 1, 21 + k) for k in range(2)]
+    ref = []
+    for st in sts:
+        f = api.Film(ctx, 512, 512)
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f]))
+        ref.append(f.download()["sum"])
+        f.close()
+    films = [api.Film(ctx, 512, 512) for _ in sts]
+    assert rt.cudaDeviceSynchronize() == 0
+    t0 = time.perf_counter()
+    for st, f in zip(sts, films):
+        ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f], wait=False))
+    enqueue_s = time.perf_counter() - t0
+    busy = rt.cudaStreamQuery(None)
+    assert api.batch_wait(ctx) == 0
+    assert busy == 600, busy  # cudaErrorNotReady: the host returned while the GPU was rendering
+    for f, r in zip(films, ref):
+        assert np.array_equal(f.download()["sum"].view(np.uint32), r.view(np.uint32))
+        f.close()
+    assert enqueue_s < 1.0
+    s.close()
+
+
+def test_async_errors_arrive_with_the_wait(ctx):
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    st = api.make_settings(64, 64, 16, 8, 3, 1, 5)
+    f = api.Film(ctx, 64, 64)
+    assert api.render_batch([s], [(0, sc["camera"], st)], [f], dict(max_iterations=2, path_pool=256), wait=False) == 0
+    assert api.batch_wait(ctx) == 4  # CRG_ERR_TIMEOUT, found on the device
+    assert b"iteration cap" in ctx.lib.crg_last_error_string(ctx.h)
+    assert api.batch_wait(ctx) == 0  # reported once
+    f.reset()
+    ctx.check(api.render_batch([s], [(0, sc["camera"], st)], [f]))
+    assert np.array_equal(f.download()["sum"].view(np.uint32), _mega(ctx, s, sc["camera"], st)["sum"].view(np.uint32))
+    f.close()
+    s.close()
+
+
+def test_small_batch_call_overhead(ctx, capsys):
+    """Per-call cost of a small batch (one 64x64 view, 1 spp): the synchronous
+    call against enqueueing alone; the loop's graph is instantiated once and
+    relaunched by every later call of the same shape."""
+    import time
+
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    st = api.make_settings(64, 64, 1, 8, 3, 1, 5)
+    f = api.Film(ctx, 64, 64)
+    view = [(0, sc["camera"], st)]
+    for _ in range(3):
+        ctx.check(api.render_batch([s], view, [f]))
+    n = 50
+    t0 = time.perf_counter()
+    for _ in range(n):
+        ctx.check(api.render_batch([s], view, [f]))
+    sync_us = (time.perf_counter() - t0) / n * 1e6
+    t0 = time.perf_counter()
+    for _ in range(n):
+        ctx.check(api.render_batch([s], view, [f], wait=False))
+    enq_us = (time.perf_counter() - t0) / n * 1e6
+    assert api.batch_wait(ctx) == 0
+    with capsys.disabled():
+        print(f"\nsmall batch: {sync_us:.0f} us per synchronous call, {enq_us:.0f} us per enqueue")
+    assert enq_us < sync_us
+    f.close()
+    s.close()
