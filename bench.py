@@ -610,7 +610,7 @@ def main():
                                       max_iterations=0, count_work=0, host_loop=0, fuse=1, refill=16), 8
             out["autotune"] = {"skipped": True, "width": tuned_width, "opts": tuned}
         else:
-            tuned, tuned_width, trials = api.autotune_batch([sb, sd], views, sample_budget=1 << 28, widths=4 | 8,
+            tuned, tuned_width, trials = api.autotune_batch([sb, sd], views, sample_budget=1 << 28, widths=2 | 4 | 8,
                                                             stream=S, leaves=LEAVES)
             out["autotune"] = {"seconds": time.perf_counter() - t0, "width": tuned_width, "opts": tuned,
                                "leaf_max": {"box": sb.info()["leaf_max"], "displaced": sd.info()["leaf_max"]},

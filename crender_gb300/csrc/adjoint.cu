@@ -250,15 +250,15 @@ crg_status launch_backward(crg_scene *s, const CamDev &cam, const crg_settings &
     const size_t dyn = per_copy * copies;
     switch (s->width) {
     case 2:
-        if (S.ninst) k_adjoint<2, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        if (S.ninst > kLoopPlacements) k_adjoint<2, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         else k_adjoint<2, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         break;
     case 4:
-        if (S.ninst) k_adjoint<4, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        if (S.ninst > kLoopPlacements) k_adjoint<4, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         else k_adjoint<4, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         break;
     default:
-        if (S.ninst) k_adjoint<8, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
+        if (S.ninst > kLoopPlacements) k_adjoint<8, true><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         else k_adjoint<8, false><<<blocks, T, dyn, st>>>(S, cam, set, adj, g_col, g_em, s->nmat, copies);
         break;
     }

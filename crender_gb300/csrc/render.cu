@@ -82,9 +82,7 @@ __global__ void __launch_bounds__(128, MINB) k_render(SceneDev S, CamDev cam, cr
         uint32_t s = 0, i = 0;
         for (;;) {
             // the lanes still rendering meet here before every segment, so the warp
-            // enters the traversal together whatever reconvergence points the
-            // compiler chooses (without it a build of this kernel ran 4.1 instead of
-            // 7.2 lanes per warp instruction on the displaced scene, 1.65x slower)
+            // enters each segment's traversal together
             lanes = __ballot_sync(lanes, s < set.spp);
             if (s >= set.spp) break;
             if (i == 0) {
@@ -175,7 +173,7 @@ void launch_w(const SceneDev &S, const CamDev &cam, const crg_settings &set, con
               int sm_count, cudaStream_t st) {
     const uint64_t npix = (uint64_t)set.width * set.height;
     const uint32_t blocks = (uint32_t)((npix + 127) / 128);
-    if (S.ninst) launch_m<W, 4, true>(S, cam, set, F, spp0, blocks, st); // placements: one variant
+    if (S.ninst > kLoopPlacements) launch_m<W, 4, true>(S, cam, set, F, spp0, blocks, st); // the top-level tree
     else if ((uint64_t)blocks >= 5ull * (uint64_t)(sm_count > 0 ? sm_count : 1)) launch_m<W, 5, false>(S, cam, set, F, spp0, blocks, st);
     else launch_m<W, 4, false>(S, cam, set, F, spp0, blocks, st);
 }

@@ -359,19 +359,73 @@ __device__ __forceinline__ bool occluded_placements(const SceneDev &S, v3 o, v3 
     return occ;
 }
 
+// Scenes with at most this many placements are traced by a plain loop over
+// them in order (the reference's loops as written, each traversal pruned by
+// the best world distance); larger ones through the top-level tree.
+constexpr uint32_t kLoopPlacements = 4;
+
+// Closest hit over a few placements, one after the other.
+template <int W, bool CNT>
+__device__ __forceinline__ void closest_placement_loop(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, Hit &h,
+                                                       TravStats &st, uint32_t &err) {
+    bool occ;
+    const float dl = sqrtf(dot(d, d));
+    float best = tmax;
+    h.prim = 0xFFFFFFFFu;
+    h.inst = kNoInst;
+    for (uint32_t j = 0; j < S.ninst; ++j) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, j, o, d, oo, od, len);
+        const float bound = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
+        const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+        Hit hj;
+        traverse<W, false, CNT>(S.nodes, S.tris, r, bound, hj.t, hj.prim, hj.slot, hj.u, hj.v, occ, st, err,
+                                __ldg(&S.inst_root[j]));
+        if (hj.prim == 0xFFFFFFFFu) continue;
+        const float dist = vdist(inst_point(S, j, oo, od, hj.t), o);
+        if (dist < best) {
+            best = dist;
+            h = hj;
+            h.inst = j;
+        }
+    }
+}
+
+// Any hit over a few placements, one after the other.
+template <int W, bool CNT>
+__device__ __forceinline__ bool occluded_placement_loop(const SceneDev &S, v3 o, v3 d, float tmin, float tmax,
+                                                        TravStats &st, uint32_t &err) {
+    float t, u, v;
+    uint32_t p, sl;
+    bool occ = false;
+    const float dl = sqrtf(dot(d, d));
+    for (uint32_t j = 0; j < S.ninst && !occ; ++j) {
+        v3 oo, od;
+        float len;
+        inst_ray(S, j, o, d, oo, od, len);
+        const RayPre r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, tmin);
+        traverse<W, true, CNT>(S.nodes, S.tris, r, (tmax * len) / dl, t, p, sl, u, v, occ, st, err,
+                               __ldg(&S.inst_root[j]));
+    }
+    return occ;
+}
+
 // Closest hit with tmin < t (object space for instances, as the reference's
 // tnear) and world distance below tmax.  INST = false compiles the one-mesh
-// path only (kernels launched for scenes without placements).
+// path and the loop over a few placements; INST = true the top-level tree.
 template <int W, bool CNT, bool INST>
 __device__ __forceinline__ bool closest_t(const SceneDev &S, v3 o, v3 d, float tmin, float tmax, Hit &h, PathCtx &C) {
     bool occ;
     TravStats st{0, 0};
-    if (!INST || S.ninst == 0) {
+    if (S.ninst == 0) {
         const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
         traverse<W, false, CNT>(S.nodes, S.tris, r, tmax, h.t, h.prim, h.slot, h.u, h.v, occ, st, C.err);
         h.inst = kNoInst;
-    } else {
+    } else if (INST) {
         closest_placements<W, CNT>(S, o, d, tmin, tmax, h, st, C.err);
+    } else {
+        closest_placement_loop<W, CNT>(S, o, d, tmin, tmax, h, st, C.err);
     }
     if (CNT) {
         C.nodes += st.nodes;
@@ -393,11 +447,13 @@ __device__ __forceinline__ bool occluded_t(const SceneDev &S, v3 o, v3 d, float 
     uint32_t p, sl;
     bool occ = false;
     TravStats st{0, 0};
-    if (!INST || S.ninst == 0) {
+    if (S.ninst == 0) {
         const RayPre r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, tmin);
         traverse<W, true, CNT>(S.nodes, S.tris, r, tmax, t, p, sl, u, v, occ, st, C.err);
-    } else {
+    } else if (INST) {
         occ = occluded_placements<W, CNT>(S, o, d, tmin, tmax, st, C.err);
+    } else {
+        occ = occluded_placement_loop<W, CNT>(S, o, d, tmin, tmax, st, C.err);
     }
     if (CNT) {
         C.nodes += st.nodes;

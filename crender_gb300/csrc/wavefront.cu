@@ -1057,9 +1057,11 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.fetch = o.fetch;
     // per-lane refill resumes a traversal of one mesh; a ray through instances
     // loops over them, so batches with an instanced scene use the static kernels
-    bool instanced = false;
-    for (uint32_t i = 0; i < nscenes; ++i)
+    bool instanced = false, tree = false; // placements; more of them than the plain loop takes
+    for (uint32_t i = 0; i < nscenes; ++i) {
         if (scenes[i]->ninst) instanced = true;
+        if (scenes[i]->ninst > kLoopPlacements) tree = true;
+    }
     wf.refill = instanced ? 0u : o.refill;
     bool sun_requests = false; // the faithful estimator's sun test steps through alpha surfaces
     for (uint32_t v = 0; v < nviews; ++v)
@@ -1131,7 +1133,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
         CRG_CUDA(ctx, cudaHostAlloc(&B->ctrl[slot], sizeof(Ctrl), cudaHostAllocDefault));
         CRG_CUDA(ctx, cudaEventCreateWithFlags(&B->ctrl_ev[slot], cudaEventDisableTiming));
     }
-    rc = dispatch(ctx, wf, width, fuse, cnt, instanced, grid, o.block_size, max_iters, st, hl);
+    rc = dispatch(ctx, wf, width, fuse, cnt, tree, grid, o.block_size, max_iters, st, hl);
     if (rc != CRG_OK) return rc;
     CRG_CUDA(ctx, cudaMemcpyAsync(B->ctrl[slot], wf.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
     CRG_CUDA(ctx, cudaEventRecord(B->ctrl_ev[slot], st));

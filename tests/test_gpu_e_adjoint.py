@@ -120,6 +120,79 @@ def test_matches_finite_differences_and_cost(ctx):
         P.close()
 
 
+def test_finite_differences_on_every_parameter(ctx, capsys):
+    """Central FD with common random numbers on all 105 parameters of the
+    inverse problem (34 x RGB albedos, the light's RGB colour) and on the
+    light's emission (crg_backward's d_grad_emission), at 256 x 256, 32 spp,
+    roulette off.  Each FD is taken at h and h/2: their difference is the FD's
+    own noise floor (float32 per-sample rounding), and a parameter passes when
+    it agrees with the adjoint to 1e-3 relative or within three noise floors."""
+    sc = _init_scene()
+    P = Problem(ctx, sc)
+    try:
+        target = scenes.inverse_box()
+        T = Problem(ctx, target, spp=256, seed_fwd=99)
+        tgt = T.render(T.fwd, f64=True)
+        T.close()
+        img = P.render(P.fwd, f64=True)
+        adj = (2.0 * (img - tgt) / img.size).astype(np.float32)
+        a64 = adj.astype(np.float64)
+        gc, ge = P.backward(adj)
+
+        def fd(field, m, c, h):
+            mp, mm = sc["mats"].copy(), sc["mats"].copy()
+            if field == "colour":
+                mp[m]["colour"][c] += h
+                mm[m]["colour"][c] -= h
+            else:
+                mp[m]["emission"] += h
+                mm[m]["emission"] -= h
+            P.set_mats(mp)
+            fp = float(np.dot(a64, P.render(P.bwd, f64=True)))
+            P.set_mats(mm)
+            fm = float(np.dot(a64, P.render(P.bwd, f64=True)))
+            return (fp - fm) / (2 * h)
+
+        rows = []
+        for m in range(35):
+            for c in range(3):
+                rows.append(("colour", m, c, gc[m, c], 1e-3))
+        rows.append(("emission", 34, 0, ge[34], 17e-3))
+        within_rel, within_floor, report = 0, 0, []
+        for field, m, c, g, h in rows:
+            f1, f2 = fd(field, m, c, h), fd(field, m, c, h / 2)
+            floor = abs(f1 - f2)
+            err = abs(g - f1)
+            ok_rel = err <= 1e-3 * abs(g)
+            ok_floor = err <= 3.0 * floor
+            within_rel += ok_rel
+            within_floor += (not ok_rel) and ok_floor
+            report.append((field, m, c, g, f1, floor))
+            assert ok_rel or ok_floor, (field, m, c, g, f1, floor)
+        P.set_mats(sc["mats"])
+        with capsys.disabled():
+            print(f"\nFD on {len(rows)} parameters: {within_rel} within 1e-3 relative, "
+                  f"{within_floor} within 3x their FD noise floor")
+        assert within_rel >= 0.9 * len(rows)
+    finally:
+        P.close()
+
+
+def test_matches_oracle_fp64_at_full_resolution(ctx, orc):
+    """The FP64 oracle gradient at the inverse problem's 256 x 256 (2 spp)."""
+    sc = _init_scene()
+    P = Problem(ctx, sc, W=256, spp=2, rr=3)
+    try:
+        adj = np.random.default_rng(2).uniform(-1, 1, 256 * 256 * 3).astype(np.float32)
+        gc, ge = P.backward(adj)
+        oc, oe = orc.adjoint(sc, sc["camera"], P.bwd, adj)
+        assert np.abs(oc).max() > 0
+        assert np.allclose(gc, oc, rtol=1e-9, atol=1e-12 * np.abs(oc).max())
+        assert np.allclose(ge, oe, rtol=1e-9, atol=1e-12 * np.abs(oe).max())
+    finally:
+        P.close()
+
+
 def test_adam_recovers_parameters(ctx):
     true_sc = scenes.inverse_box()
     T = Problem(ctx, true_sc, spp=1024, seed_fwd=77)
