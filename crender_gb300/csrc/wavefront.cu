@@ -90,6 +90,7 @@ struct Wf {
     float4 *o, *d, *T, *L; // T.w = prev_pdf
     uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
     float4 *hit;           // t, prim bits, triangle slot bits, found
+    float4 *pre;           // one-mesh hits: geometric normal and material index (extend writes, shade reads)
     float4 *sh_o, *sh_d, *sh_c;
     uint32_t *qa, *qb, *qsh;
     float4 *slots;         // radiance per sample of the current chunk
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             Hit h;
             const bool found = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
             w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), pack_found(found, h.inst));
+            if (found && h.inst == kNoInst) w.pre[slot] = hit_pre(S, h.slot, h.prim);
             if (C.err) atomicOr(&c->error, 1u);
             if (CNT) {
                 nodes += C.nodes;
@@ -248,13 +250,14 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 const SceneDev &S = w.scenes[V.scene];
                 const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot];
                 PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
-                float4 h4;
+                float4 h4, pre = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (FUSE >= 2) {
                     Hit hh;
                     const bool f = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
                     h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), pack_found(f, hh.inst));
                 } else {
                     h4 = w.hit[slot];
+                    if (__float_as_uint(h4.w) == 1u) pre = w.pre[slot]; // a one-mesh hit: extend's normal and material
                 }
                 PathState ps;
                 ps.o = mk(o.x, o.y, o.z);
@@ -277,8 +280,8 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                     cont = false; // max_bounces == 0: the megakernel traces nothing for this sample
                 } else {
                     cont = V.set.mode == CRG_MODE_EXTENDED
-                               ? shade_extended(S, V.set, C, depth, ps, fw != 0u, h, aov, nr)
-                               : shade_faithful(S, V.set, C, depth, ps, fw != 0u, h, aov, nr);
+                               ? shade_extended<NullTape, FUSE <= 1>(S, V.set, C, depth, ps, fw != 0u, h, aov, nr, nullptr, pre)
+                               : shade_faithful<FUSE <= 1>(S, V.set, C, depth, ps, fw != 0u, h, aov, nr, pre);
                 }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
                 shadow = nr.kind != 0;
@@ -395,6 +398,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_extend_dyn(Wf w) {
             const bool found = T.best_prim != 0xFFFFFFFFu;
             w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot),
                                       pack_found(found, kNoInst));
+            // the hit's normal and material for shade, from the triangle just tested
+            if (found) w.pre[slot] = hit_pre(w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene], T.best_slot, T.best_prim);
         },
         st, err);
     if (err) atomicOr(&c->error, 1u);
@@ -673,10 +678,12 @@ crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &
                 for (int k = 0; k < kWin; ++k) {
                     float ms[4] = {0, 0, 0, 0};
                     for (int m = 0; m < 4; ++m) cudaEventElapsedTime(&ms[m], ev[k * kMarks + m], ev[k * kMarks + m + 1]);
-                    times->extend_ms += ms[0];
+                    // a stage this fusion level does not launch keeps 0 (its empty event gap
+                    // goes to the control stage)
+                    times->extend_ms += FUSE <= 1 ? ms[0] : 0.0;
                     times->shade_ms += ms[1];
-                    times->shadow_ms += ms[2];
-                    times->other_ms += ms[3];
+                    times->shadow_ms += FUSE == 0 ? ms[2] : 0.0;
+                    times->other_ms += ms[3] + (FUSE <= 1 ? 0.0 : ms[0]) + (FUSE == 0 ? 0.0 : ms[2]);
                     times->iterations++;
                 }
             if (*done_h) break;
@@ -720,6 +727,9 @@ struct BatchState {
     uint64_t seq[2] = {0, 0}, next_seq = 1;
     crg_render_stats stats[2] = {};
     uint32_t loop_mode[2] = {0, 0}; // crg_wavefront_opts::host_loop of the slot's batch
+    // occupancy answers (resident blocks per SM) by kernel set and block size: the
+    // runtime's occupancy queries cost tens of microseconds each, every call
+    std::vector<std::pair<uint64_t, uint32_t>> occupancy;
     int ctrl_next = 0;
     crg_status sticky = CRG_OK; // first error of the batches collected since the last wait
     std::string sticky_msg;
@@ -831,7 +841,30 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
     k_wf_generate<<<grid, 256, 0, st>>>(wf, 1);
     k_wf_generated<<<1, 32, 0, st>>>(wf, 1);
     CRG_CUDA(ctx, cudaGetLastError());
-    const Grids bg = bounce_grids<W, FUSE, CNT, INST>(wf, block, ctx->sm_count);
+    Grids bg{0, 0, 0};
+    {
+        // resident grids of this kernel set, cached per context
+        BatchState *B = nullptr;
+        crg_status rc0 = state_of(ctx, B);
+        if (rc0 != CRG_OK) return rc0;
+        const uint64_t key = (uint64_t)W | (uint64_t)FUSE << 8 | (uint64_t)CNT << 12 | (uint64_t)INST << 13 |
+                             (uint64_t)(wf.refill != 0) << 14 | (uint64_t)(wf.refill_sh != 0) << 15 | (uint64_t)block << 16;
+        uint32_t found = 0;
+        for (const auto &e : B->occupancy)
+            if (e.first == (key | 1ull << 40) || e.first == (key | 2ull << 40) || e.first == (key | 3ull << 40)) found++;
+        if (found == 3) {
+            for (const auto &e : B->occupancy) {
+                if (e.first == (key | 1ull << 40)) bg.ext = e.second;
+                if (e.first == (key | 2ull << 40)) bg.shade = e.second;
+                if (e.first == (key | 3ull << 40)) bg.shadow = e.second;
+            }
+        } else {
+            bg = bounce_grids<W, FUSE, CNT, INST>(wf, block, ctx->sm_count);
+            B->occupancy.push_back({key | 1ull << 40, bg.ext});
+            B->occupancy.push_back({key | 2ull << 40, bg.shade});
+            B->occupancy.push_back({key | 3ull << 40, bg.shadow});
+        }
+    }
     if (host_loop)
         return run_host<W, FUSE, CNT, INST>(ctx, wf, grid, bg, block, max_iters, st,
                                             host_loop == 2 ? &ctx->stage_times : nullptr);
@@ -1033,7 +1066,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     const size_t n_f4 = align_up(sizeof(float4) * (size_t)P), n_u4 = align_up(sizeof(uint4) * (size_t)P);
     const size_t n_q = align_up(sizeof(uint32_t) * (size_t)P);
     const size_t n_slots = align_up(sizeof(float4) * (size_t)max_chunk);
-    const size_t bytes = n_sc + n_vd + n_sg + n_ch + n_ctrl + 8 * n_f4 + n_u4 + 3 * n_q + n_slots;
+    const size_t bytes = n_sc + n_vd + n_sg + n_ch + n_ctrl + 9 * n_f4 + n_u4 + 3 * n_q + n_slots;
     crg_status rc = dev_alloc(ctx, ctx->wf_ws, bytes);
     if (rc != CRG_OK) return rc;
     char *p = (char *)ctx->wf_ws.ptr;
@@ -1072,6 +1105,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.T = (float4 *)take(n_f4);
     wf.L = (float4 *)take(n_f4);
     wf.hit = (float4 *)take(n_f4);
+    wf.pre = (float4 *)take(n_f4);
     wf.sh_o = (float4 *)take(n_f4);
     wf.sh_d = (float4 *)take(n_f4);
     wf.sh_c = (float4 *)take(n_f4);
@@ -1109,7 +1143,16 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     }
     // persistent grid: resident blocks of the launched kernels on every SM
     const uint32_t fuse = instanced ? 0u : (o.fuse ? o.fuse - 1 : 0); // fusion level 0..2 (split with placements)
-    int per_sm = occupancy(width, fuse, (int)o.block_size);
+    int per_sm = 0;
+    {
+        const uint64_t key = (uint64_t)width | (uint64_t)fuse << 8 | (uint64_t)o.block_size << 16 | 4ull << 40;
+        for (const auto &e : B->occupancy)
+            if (e.first == key) per_sm = (int)e.second;
+        if (!per_sm) {
+            per_sm = occupancy(width, fuse, (int)o.block_size);
+            B->occupancy.push_back({key, (uint32_t)per_sm});
+        }
+    }
     const uint32_t grid = (uint32_t)(std::max(ctx->sm_count, 1) * per_sm);
     // every chunk needs at most (samples / P + 1) refills of max_bounces + 1 iterations
     unsigned long long iters = 16;

@@ -124,9 +124,13 @@ def test_finite_differences_on_every_parameter(ctx, capsys):
     """Central FD with common random numbers on all 105 parameters of the
     inverse problem (34 x RGB albedos, the light's RGB colour) and on the
     light's emission (crg_backward's d_grad_emission), at 256 x 256, 32 spp,
-    roulette off.  Each FD is taken at h and h/2: their difference is the FD's
-    own noise floor (float32 per-sample rounding), and a parameter passes when
-    it agrees with the adjoint to 1e-3 relative or within three noise floors."""
+    roulette off.  The forward pass sums float32 per-sample radiance, so an FD
+    carries rounding noise of its own: each FD is taken at h and h/2, and a
+    parameter passes when it agrees with the adjoint to 1e-3 relative, or
+    within its noise floor: three times the h / h-half spread, and at least
+    1e-5 of the largest gradient (parameters whose gradient is that small
+    lose their digits to the rounding of the other contributions to the same
+    pixels)."""
     sc = _init_scene()
     P = Problem(ctx, sc)
     try:
@@ -159,12 +163,13 @@ def test_finite_differences_on_every_parameter(ctx, capsys):
                 rows.append(("colour", m, c, gc[m, c], 1e-3))
         rows.append(("emission", 34, 0, ge[34], 17e-3))
         within_rel, within_floor, report = 0, 0, []
+        gmax = max(np.abs(gc).max(), np.abs(ge[34]))
         for field, m, c, g, h in rows:
             f1, f2 = fd(field, m, c, h), fd(field, m, c, h / 2)
-            floor = abs(f1 - f2)
+            floor = max(3.0 * abs(f1 - f2), 1e-5 * gmax)
             err = abs(g - f1)
             ok_rel = err <= 1e-3 * abs(g)
-            ok_floor = err <= 3.0 * floor
+            ok_floor = err <= floor
             within_rel += ok_rel
             within_floor += (not ok_rel) and ok_floor
             report.append((field, m, c, g, f1, floor))
@@ -172,7 +177,10 @@ def test_finite_differences_on_every_parameter(ctx, capsys):
         P.set_mats(sc["mats"])
         with capsys.disabled():
             print(f"\nFD on {len(rows)} parameters: {within_rel} within 1e-3 relative, "
-                  f"{within_floor} within 3x their FD noise floor")
+                  f"{within_floor} within their FD noise floor; largest |gradient| {gmax:.3e}")
+            for field, m, c, g, f1, floor in report:
+                if abs(g - f1) > 1e-3 * abs(g):
+                    print(f"  {field}[{m}, {c}]: adjoint {g:.6e}, FD {f1:.6e}, noise floor {floor:.2e}")
         assert within_rel >= 0.9 * len(rows)
     finally:
         P.close()
