@@ -476,28 +476,9 @@ struct HitGeom {
     float dist;
     v3 ro, rd;
 };
-// The geometric normal and material index of a one-mesh hit, as the
-// wavefront's extend stage stores them for shade: {Ng.xyz, material bits}.
-__device__ __forceinline__ float4 hit_pre(const SceneDev &S, uint32_t slot, uint32_t prim) {
-    v3 a, b, c;
-    slot_verts(S, slot, a, b, c);
-    const v3 Ng = normalize(cross(sub(b, a), sub(c, a)));
-    return make_float4(Ng.x, Ng.y, Ng.z, __uint_as_float(__ldg(&S.mat_idx[prim])));
-}
-
-// PRE: a one-mesh hit's normal comes from `pre` (hit_pre, the same
-// expression evaluated by the extend stage) instead of the triangle's vertices.
-template <bool WORLD_N, bool PRE = false>
-__device__ __forceinline__ HitGeom hit_geom(const SceneDev &S, const Hit &h, v3 o, v3 d, float4 pre = float4{}) {
+template <bool WORLD_N>
+__device__ __forceinline__ HitGeom hit_geom(const SceneDev &S, const Hit &h, v3 o, v3 d) {
     HitGeom g;
-    if (PRE && h.inst == kNoInst) {
-        g.p = add(o, mul(d, h.t));
-        g.dist = h.t;
-        g.ro = o;
-        g.rd = d;
-        g.Ng = mk(pre.x, pre.y, pre.z);
-        return g;
-    }
     v3 a, b, c;
     slot_verts(S, h.slot, a, b, c);
     if (h.inst == kNoInst) {
@@ -584,9 +565,8 @@ __device__ __forceinline__ void path_start(PathState &ps, v3 o, v3 d) {
 
 // ------------------------------------------------------------------ faithful
 // process_hit + the bounce body of _sample_pixel (renderer.cpp:21-102, 272-355).
-template <bool PRE = false>
 __device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set, const PathCtx &C, uint32_t i, PathState &ps,
-                               bool found, const Hit &h, Aov &aov, NeeReq &nr, float4 pre = float4{}) {
+                               bool found, const Hit &h, Aov &aov, NeeReq &nr) {
     nr.kind = 0;
     if (!found) {
         const v3 env = sample_sky(S, ps.d);
@@ -594,10 +574,9 @@ __device__ inline bool shade_faithful(const SceneDev &S, const crg_settings &set
         ps.L = add(ps.L, mulv(ps.T, env));
         return false;
     }
-    const HitGeom hg = hit_geom<false, PRE>(S, h, ps.o, ps.d, pre);
+    const HitGeom hg = hit_geom<false>(S, h, ps.o, ps.d);
     const v3 p = hg.p, Ng = hg.Ng;
-    const crg_material &m =
-        S.mats[(PRE && h.inst == kNoInst) ? __float_as_uint(pre.w) : __ldg(&S.mat_idx[h.prim])];
+    const crg_material &m = S.mats[__ldg(&S.mat_idx[h.prim])];
     const float4 col = hit_colour(S, m, h.prim, h.slot, hg.ro, hg.rd);
     const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;
     if (c3 == 0.0f) {
@@ -804,10 +783,9 @@ __device__ inline void nee_prepare(const SceneDev &S, const PathCtx &C, uint32_t
 
 // Extended estimator bounce: MIS-weighted emission, emissive-triangle NEE,
 // Lambert (geometric-normal hemisphere) / GGX VNDF / Fresnel dielectric, RR.
-template <class Tape = NullTape, bool PRE = false>
+template <class Tape = NullTape>
 __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set, const PathCtx &C, uint32_t i, PathState &ps,
-                                      bool found, const Hit &h, Aov &aov, NeeReq &nr, Tape *tape = nullptr,
-                                      float4 pre = float4{}) {
+                                      bool found, const Hit &h, Aov &aov, NeeReq &nr, Tape *tape = nullptr) {
     nr.kind = 0;
     if (!found) {
         const v3 env = sample_sky(S, ps.d);
@@ -817,9 +795,9 @@ __device__ inline bool shade_extended(const SceneDev &S, const crg_settings &set
         if (tape) tape->env(contrib);
         return false;
     }
-    const HitGeom hg = hit_geom<true, PRE>(S, h, ps.o, ps.d, pre);
+    const HitGeom hg = hit_geom<true>(S, h, ps.o, ps.d);
     const v3 p = hg.p, Ng = hg.Ng;
-    const uint32_t mi = (PRE && h.inst == kNoInst) ? __float_as_uint(pre.w) : __ldg(&S.mat_idx[h.prim]);
+    const uint32_t mi = __ldg(&S.mat_idx[h.prim]);
     const crg_material &m = S.mats[mi];
     const float4 col = hit_colour(S, m, h.prim, h.slot, hg.ro, hg.rd);
     const float c0 = col.x, c1 = col.y, c2 = col.z, c3 = col.w;

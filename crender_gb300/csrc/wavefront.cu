@@ -90,7 +90,6 @@ struct Wf {
     float4 *o, *d, *T, *L; // T.w = prev_pdf
     uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
     float4 *hit;           // t, prim bits, triangle slot bits, found
-    float4 *pre;           // one-mesh hits: geometric normal and material index (extend writes, shade reads)
     float4 *sh_o, *sh_d, *sh_c;
     uint32_t *qa, *qb, *qsh;
     float4 *slots;         // radiance per sample of the current chunk
@@ -198,7 +197,6 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             Hit h;
             const bool found = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
             w.hit[slot] = make_float4(h.t, __uint_as_float(h.prim), __uint_as_float(h.slot), pack_found(found, h.inst));
-            if (found && h.inst == kNoInst) w.pre[slot] = hit_pre(S, h.slot, h.prim);
             if (C.err) atomicOr(&c->error, 1u);
             if (CNT) {
                 nodes += C.nodes;
@@ -250,14 +248,13 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 const SceneDev &S = w.scenes[V.scene];
                 const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot];
                 PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
-                float4 h4, pre = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float4 h4;
                 if (FUSE >= 2) {
                     Hit hh;
                     const bool f = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, hh, C);
                     h4 = make_float4(hh.t, __uint_as_float(hh.prim), __uint_as_float(hh.slot), pack_found(f, hh.inst));
                 } else {
                     h4 = w.hit[slot];
-                    if (__float_as_uint(h4.w) == 1u) pre = w.pre[slot]; // a one-mesh hit: extend's normal and material
                 }
                 PathState ps;
                 ps.o = mk(o.x, o.y, o.z);
@@ -280,8 +277,8 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                     cont = false; // max_bounces == 0: the megakernel traces nothing for this sample
                 } else {
                     cont = V.set.mode == CRG_MODE_EXTENDED
-                               ? shade_extended<NullTape, FUSE <= 1>(S, V.set, C, depth, ps, fw != 0u, h, aov, nr, nullptr, pre)
-                               : shade_faithful<FUSE <= 1>(S, V.set, C, depth, ps, fw != 0u, h, aov, nr, pre);
+                               ? shade_extended(S, V.set, C, depth, ps, fw != 0u, h, aov, nr)
+                               : shade_faithful(S, V.set, C, depth, ps, fw != 0u, h, aov, nr);
                 }
                 if (cont && depth + 1 >= V.set.max_bounces) cont = false;
                 shadow = nr.kind != 0;
@@ -398,8 +395,6 @@ __global__ void __launch_bounds__(256, 4) k_wf_extend_dyn(Wf w) {
             const bool found = T.best_prim != 0xFFFFFFFFu;
             w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot),
                                       pack_found(found, kNoInst));
-            // the hit's normal and material for shade, from the triangle just tested
-            if (found) w.pre[slot] = hit_pre(w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene], T.best_slot, T.best_prim);
         },
         st, err);
     if (err) atomicOr(&c->error, 1u);
@@ -1066,7 +1061,7 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     const size_t n_f4 = align_up(sizeof(float4) * (size_t)P), n_u4 = align_up(sizeof(uint4) * (size_t)P);
     const size_t n_q = align_up(sizeof(uint32_t) * (size_t)P);
     const size_t n_slots = align_up(sizeof(float4) * (size_t)max_chunk);
-    const size_t bytes = n_sc + n_vd + n_sg + n_ch + n_ctrl + 9 * n_f4 + n_u4 + 3 * n_q + n_slots;
+    const size_t bytes = n_sc + n_vd + n_sg + n_ch + n_ctrl + 8 * n_f4 + n_u4 + 3 * n_q + n_slots;
     crg_status rc = dev_alloc(ctx, ctx->wf_ws, bytes);
     if (rc != CRG_OK) return rc;
     char *p = (char *)ctx->wf_ws.ptr;
@@ -1105,7 +1100,6 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.T = (float4 *)take(n_f4);
     wf.L = (float4 *)take(n_f4);
     wf.hit = (float4 *)take(n_f4);
-    wf.pre = (float4 *)take(n_f4);
     wf.sh_o = (float4 *)take(n_f4);
     wf.sh_d = (float4 *)take(n_f4);
     wf.sh_c = (float4 *)take(n_f4);
