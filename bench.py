@@ -878,6 +878,17 @@ def main():
         out["any_hit"] = {"value": n / (sum(ms_any) / len(ms_any) / 1e3) / 1e6, "unit": "Mrays/s",
                           "ms_per_step": sum(ms_any) / len(ms_any), "rays": n, "occluded_fraction": occluded / n,
                           "kernel": "k_intersect_dyn<8> (any hit, per-lane refill)"}
+        # the warp-cooperative scheme on the same rays (8 lanes per ray, nodes staged in shared memory)
+        ms_wc = timer.steps(lambda: ctx.check(lib.crg_intersect_closest_with(scene.h, rb.ptr, hb.ptr, n,
+                                                                             api.TRAVERSAL_WARP, S)),
+                            args.steps, args.warmup)
+        ms_wa = timer.steps(lambda: ctx.check(lib.crg_intersect_any_with(scene.h, sb.ptr, ob.ptr, n,
+                                                                         api.TRAVERSAL_WARP, S)),
+                            args.steps, args.warmup)
+        out["warp_traversal"] = {
+            "closest_mrays_per_s": n / (sum(ms_wc) / len(ms_wc) / 1e3) / 1e6,
+            "any_mrays_per_s": n / (sum(ms_wa) / len(ms_wa) / 1e3) / 1e6, "rays": n,
+            "kernel": "k_intersect_warp<8> (crg_intersect_*_with, CRG_TRAVERSAL_WARP)"}
         sb.free()
         ob.free()
         pr = api.PinnedArray(ctx, rays_h.shape, rays_h.dtype)

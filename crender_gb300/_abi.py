@@ -153,6 +153,7 @@ FILM_F64, FILM_AOV = 1, 2
 TONEMAP_LINEAR, TONEMAP_REINHARD, TONEMAP_JIM_RICHARD, TONEMAP_UNCHARTED = 0, 1, 2, 3
 POST_FAITHFUL, POST_FULL = 0, 1
 INVALID_PRIM = 0xFFFFFFFF
+TRAVERSAL_THREAD, TRAVERSAL_WARP = 0, 1  # crg_traversal
 NOALLOC_MAX_TRIS = 16384
 
 STATUS = {
@@ -208,6 +209,8 @@ CRG_SIGNATURES = [
     ("crg_intersect_closest", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_any", C.c_int, [vp, vp, vp, C.c_uint64, c_stream]),
     ("crg_intersect_closest_counted", C.c_int, [vp, vp, vp, vp, vp, C.c_uint64, c_stream]),
+    ("crg_intersect_closest_with", C.c_int, [vp, vp, vp, C.c_uint64, C.c_int, c_stream]),
+    ("crg_intersect_any_with", C.c_int, [vp, vp, vp, C.c_uint64, C.c_int, c_stream]),
     ("crg_scene_poll_error", C.c_int, [vp]),
     ("crg_film_create", C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, P(vp)]),
     ("crg_film_destroy", C.c_int, [vp]),

@@ -22,6 +22,7 @@ def _default_sun_direction():
 
 
 # cr::entity::sun (src/render/entities/components.h:23-29), bit-identical to crg_scene_set_sun(.., NULL)
+TRAVERSAL_THREAD, TRAVERSAL_WARP = _abi.TRAVERSAL_THREAD, _abi.TRAVERSAL_WARP
 DEFAULT_SUN = dict(
     size=np.float32(3.14159265359) / np.float32(48.0),
     intensity=100.0,
@@ -265,14 +266,22 @@ class Scene:
         h, w = rgba.shape[:2]
         self.ctx.check(self.ctx.lib.crg_scene_set_skybox(self.h, ptr(rgba), w, h, float(rot[0]), float(rot[1])))
 
-    def intersect(self, rays: np.ndarray, any_hit=False, counted=False):
-        """Host rays in, host results out (uploads, launches, downloads)."""
+    def intersect(self, rays: np.ndarray, any_hit=False, counted=False, traversal=None):
+        """Host rays in, host results out (uploads, launches, downloads).  `traversal`:
+        None (the default scheme), TRAVERSAL_THREAD or TRAVERSAL_WARP."""
         n = len(rays)
         rb = DeviceBuffer.from_array(self.ctx, rays)
         ob = DeviceBuffer(self.ctx, max(n * (4 if any_hit else 16), 16))
         extra = []
         try:
-            if any_hit:
+            if traversal is not None and not counted:
+                if any_hit:
+                    self.ctx.check(self.ctx.lib.crg_intersect_any_with(self.h, rb.ptr, ob.ptr, n, traversal, None))
+                    out = ob.download(np.zeros(n, np.uint32))
+                else:
+                    self.ctx.check(self.ctx.lib.crg_intersect_closest_with(self.h, rb.ptr, ob.ptr, n, traversal, None))
+                    out = ob.download(np.zeros(n, _abi.HIT_DTYPE))
+            elif any_hit:
                 self.ctx.check(self.ctx.lib.crg_intersect_any(self.h, rb.ptr, ob.ptr, n, None))
                 out = ob.download(np.zeros(n, np.uint32))
             elif counted:

@@ -1136,6 +1136,26 @@ crg_status crg_intersect_any(const crg_scene *scene, const crg_ray *d_rays, uint
     return launch_intersect(scene, d_rays, nullptr, d_occluded, nullptr, nullptr, n, true, (cudaStream_t)stream);
 }
 
+crg_status crg_intersect_closest_with(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits, uint64_t n,
+                                      crg_traversal traversal, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return set_error(scene->ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (n && (!d_rays || !d_hits)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null ray or hit array");
+    if (traversal != CRG_TRAVERSAL_THREAD && traversal != CRG_TRAVERSAL_WARP)
+        return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "unknown traversal scheme");
+    return launch_intersect(scene, d_rays, d_hits, nullptr, nullptr, nullptr, n, false, (cudaStream_t)stream, traversal);
+}
+
+crg_status crg_intersect_any_with(const crg_scene *scene, const crg_ray *d_rays, uint32_t *d_occluded, uint64_t n,
+                                  crg_traversal traversal, crg_stream stream) {
+    if (!scene) return CRG_ERR_INVALID_ARG;
+    if (!scene->built) return set_error(scene->ctx, CRG_ERR_NOT_BUILT, "scene not built");
+    if (n && (!d_rays || !d_occluded)) return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "null ray or output array");
+    if (traversal != CRG_TRAVERSAL_THREAD && traversal != CRG_TRAVERSAL_WARP)
+        return set_error(scene->ctx, CRG_ERR_INVALID_ARG, "unknown traversal scheme");
+    return launch_intersect(scene, d_rays, nullptr, d_occluded, nullptr, nullptr, n, true, (cudaStream_t)stream, traversal);
+}
+
 crg_status crg_intersect_closest_counted(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits, uint32_t *d_nodes,
                                          uint32_t *d_tris, uint64_t n, crg_stream stream) {
     if (!scene) return CRG_ERR_INVALID_ARG;

@@ -153,7 +153,8 @@ constexpr uint32_t kTlasLeaf = 0x80000000u;
 
 // traverse.cu
 crg_status launch_intersect(const crg_scene *s, const crg_ray *rays, crg_hit *hits, uint32_t *occluded,
-                            uint32_t *nodes, uint32_t *tris, uint64_t n, bool any, cudaStream_t stream);
+                            uint32_t *nodes, uint32_t *tris, uint64_t n, bool any, cudaStream_t stream,
+                            int traversal = CRG_TRAVERSAL_THREAD);
 
 // render.cu
 struct CamDev {

@@ -860,6 +860,14 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
             B->occupancy.push_back({key | 3ull << 40, bg.shadow});
         }
     }
+    {
+        // a pool smaller than a resident grid's threads needs fewer blocks: in a small batch the
+        // others would only start, find the queue empty and exit, every stage of every bounce
+        const uint32_t need = std::max<uint32_t>(1u, (uint32_t)(((uint64_t)wf.P + block - 1) / block));
+        bg.ext = std::min(bg.ext, need);
+        bg.shade = std::min(bg.shade, need);
+        bg.shadow = std::min(bg.shadow, need);
+    }
     if (host_loop)
         return run_host<W, FUSE, CNT, INST>(ctx, wf, grid, bg, block, max_iters, st,
                                             host_loop == 2 ? &ctx->stage_times : nullptr);

@@ -399,6 +399,22 @@ crg_status crg_intersect_closest_counted(const crg_scene *scene, const crg_ray *
                                          uint32_t *d_nodes, uint32_t *d_tris, uint64_t n,
                                          crg_stream stream);
 
+/* Traversal schemes of the batched queries (the results are the same):
+ *   THREAD: one ray per thread, its group stack in local memory (the default
+ *           of crg_intersect_closest / crg_intersect_any);
+ *   WARP:   W lanes per ray (W = the BVH width), 32 / W rays per warp: the
+ *           ray's node is read with 16-byte vector loads by its lanes into
+ *           shared memory, each lane tests one child box, pending triangles
+ *           are tested W at a time, and each ray's group stack lives in its
+ *           warp's shared memory.  Scenes traced through placements use
+ *           THREAD. */
+typedef enum crg_traversal { CRG_TRAVERSAL_THREAD = 0, CRG_TRAVERSAL_WARP = 1 } crg_traversal;
+/* crg_intersect_closest / crg_intersect_any with an explicit traversal scheme. */
+crg_status crg_intersect_closest_with(const crg_scene *scene, const crg_ray *d_rays, crg_hit *d_hits, uint64_t n,
+                                      crg_traversal traversal, crg_stream stream);
+crg_status crg_intersect_any_with(const crg_scene *scene, const crg_ray *d_rays, uint32_t *d_occluded, uint64_t n,
+                                  crg_traversal traversal, crg_stream stream);
+
 /* Reads and clears the scene's device error word, which a kernel sets instead
  * of trapping when a traversal stack would overflow.  Returns CRG_ERR_DEVICE
  * when it was set.  Synchronises with the device. */
