@@ -69,7 +69,7 @@ def build(verbose: bool = False, ptxas_v: bool = False) -> str:
     objs = [os.path.join(OUT, s.replace(".cu", ".o")) for s in SOURCES]
     lib = os.path.join(OUT, "libcrg.so")
     tmp = lib + ".tmp"
-    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xcompiler", "-pthread"])
     os.replace(tmp, lib)
     logs.append(build_host(lib))
     log = "".join(logs)

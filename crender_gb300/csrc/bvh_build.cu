@@ -309,14 +309,22 @@ __global__ void k_bottom_up(Tree T, uint32_t n, uint32_t *__restrict__ visits, i
 }
 
 // ----------------------------------------------------------------- treelets
-// One thread restructures the 7-leaf treelet rooted at x (Karras & Aila 2013),
-// exactly as the CPU form: growth by largest area, DP over subsets in
-// increasing size with partitions containing the lowest set bit, first minimum
-// kept, internal nodes reused in formation order, pre-order rebuild.
-__device__ void optimize_treelet(const Tree &T, uint32_t r) {
+// The 7-leaf treelet rooted at r is restructured (Karras & Aila 2013) by the
+// 32 lanes of a warp, with the same result as the CPU form: growth by largest
+// area, DP over subsets in increasing size with partitions containing the
+// lowest set bit, first minimum kept (in the CPU's enumeration, q = rest,
+// (q - 1) & rest, ...: the larger partition wins a tie), internal nodes
+// reused in formation order, pre-order rebuild.  Every lane forms the
+// treelet (the same coherent loads); the subset areas and the DP are split
+// over the lanes, in shared memory; the owning lane `leader` (the one whose
+// arrival at r made it ready) writes the rebuilt nodes.
+__device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *aS, float *cS, uint8_t *pS) {
+    const uint32_t lane = threadIdx.x & 31u;
+    float cost_r;
     {
         const Box b = box_of_cg(T, r);
-        T.cost[r] = kCi * area(b) + (cost_of_cg(T, left_of(T, r)) + cost_of_cg(T, right_of(T, r)));
+        cost_r = kCi * area(b) + (cost_of_cg(T, left_of(T, r)) + cost_of_cg(T, right_of(T, r)));
+        if (leader) T.cost[r] = cost_r;
     }
     uint32_t leaves[7];
     uint32_t internals[6];
@@ -339,102 +347,166 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r) {
     }
     if (nl < 3) return;
     const int nsub = 1 << nl;
-    float aS[128], cS[128];
-    uint8_t pS[128];
     Box lb[7];
     for (int j = 0; j < nl; ++j) lb[j] = box_of_cg(T, leaves[j]);
-    for (int s = 1; s < nsub; ++s) {
+    for (int s = (int)lane + 1; s < nsub; s += 32) {
         Box b = lb[__ffs(s) - 1];
         for (int j = __ffs(s); j < nl; ++j)
             if (s & (1 << j)) b = merge(b, lb[j]);
         aS[s] = area(b);
     }
-    for (int j = 0; j < nl; ++j) {
-        cS[1 << j] = cost_of_cg(T, leaves[j]);
-        pS[1 << j] = 0;
+    if ((int)lane < nl) {
+        cS[1 << lane] = cost_of_cg(T, leaves[lane]);
+        pS[1 << lane] = 0;
     }
+    __syncwarp();
     for (int k = 2; k <= nl; ++k) {
-        for (int s = 1; s < nsub; ++s) {
-            if (__popc(s) != k) continue;
-            float best = FLT_MAX;
-            int bp = 0;
-            const int low = s & -s;
-            const int rest = s ^ low;
-            for (int q = rest;; q = (q - 1) & rest) {
-                const int P = q | low;
-                if (P != s) {
-                    const float c = cS[P] + cS[s ^ P];
-                    if (c < best) { best = c; bp = P; }
+        if (k <= 5) {
+            // a subset per lane (at most 15 partitions each), in the CPU's partition order
+            for (int s = (int)lane + 1; s < nsub; s += 32) {
+                if (__popc(s) != k) continue;
+                float best = FLT_MAX;
+                int bp = 0;
+                const int low = s & -s;
+                const int rest = s ^ low;
+                for (int q = rest;; q = (q - 1) & rest) {
+                    const int P = q | low;
+                    if (P != s) {
+                        const float c = cS[P] + cS[s ^ P];
+                        if (c < best) { best = c; bp = P; }
+                    }
+                    if (q == 0) break;
                 }
-                if (q == 0) break;
+                cS[s] = kCi * aS[s] + best;
+                pS[s] = (uint8_t)bp;
             }
-            cS[s] = kCi * aS[s] + best;
-            pS[s] = (uint8_t)bp;
+        } else {
+            // subsets of 6 or 7 leaves one at a time, their 31 / 63 partitions over the lanes
+            for (int s = 1; s < nsub; ++s) {
+                if (__popc(s) != k) continue;
+                const int low = s & -s;
+                const int rest = s ^ low;
+                const int m = k - 1, npart = (1 << m) - 1; // q = rest (P == s) excluded
+                float best = INFINITY;
+                int bp = -1;
+                for (int t = (int)lane; t < npart; t += 32) {
+                    int q = 0, bit = 0; // deposit t's bits into rest's set bits
+                    for (int rr = rest; rr; rr &= rr - 1, ++bit)
+                        if (t & (1 << bit)) q |= rr & -rr;
+                    const int P = q | low;
+                    const float c = cS[P] + cS[s ^ P];
+                    if (c < best || (c == best && P > bp)) { best = c; bp = P; }
+                }
+#pragma unroll
+                for (int off = 16; off >= 1; off >>= 1) {
+                    const float oc = __shfl_xor_sync(0xFFFFFFFFu, best, off);
+                    const int op = __shfl_xor_sync(0xFFFFFFFFu, bp, off);
+                    if (oc < best || (oc == best && op > bp)) { best = oc; bp = op; }
+                }
+                if (lane == 0u) {
+                    cS[s] = kCi * aS[s] + best;
+                    pS[s] = (uint8_t)bp;
+                }
+            }
         }
+        __syncwarp();
     }
     const int full = nsub - 1;
-    if (!(cS[full] < __ldcg(&T.cost[r]))) return;
-    // pre-order rebuild with an explicit stack; record (subset, node) pairs
-    int st_s[8];
-    uint32_t st_n[8];
-    int sp = 0, next = 0;
-    int post_s[6 + 1];
-    uint32_t post_n[6 + 1];
-    int np = 0;
-    st_s[sp] = full;
-    st_n[sp] = r;
-    sp++;
-    while (sp > 0) {
-        --sp;
-        const int S = st_s[sp];
-        const uint32_t node = st_n[sp];
-        const int P = pS[S];
-        const int parts[2] = {P, S ^ P};
-        uint32_t kids[2];
-        for (int c = 0; c < 2; ++c) {
-            if (__popc(parts[c]) == 1) kids[c] = leaves[__ffs(parts[c]) - 1];
-            else kids[c] = internals[next++];
-        }
-        // children pointers (.w of the node's float4 pair); box written below
-        T.nbox[2 * (size_t)node].w = __uint_as_float(kids[0]);
-        T.nbox[2 * (size_t)node + 1].w = __uint_as_float(kids[1]);
-        for (int c = 0; c < 2; ++c) {
-            if (kids[c] & LEAF) T.leaf_parent[kids[c] & ~LEAF] = node;
-            else T.parent[kids[c]] = node;
-        }
-        post_s[np] = S;
-        post_n[np] = node;
-        np++;
-        for (int c = 1; c >= 0; --c)
-            if (!(kids[c] & LEAF) && __popc(parts[c]) > 1) {
-                st_s[sp] = parts[c];
-                st_n[sp] = kids[c];
-                sp++;
+    if (!(cS[full] < cost_r)) {
+        __syncwarp();
+        return;
+    }
+    if (leader) {
+        // pre-order rebuild with an explicit stack; record (subset, node) pairs
+        int st_s[8];
+        uint32_t st_n[8];
+        int sp = 0, next = 0;
+        int post_s[6 + 1];
+        uint32_t post_n[6 + 1];
+        int np = 0;
+        st_s[sp] = full;
+        st_n[sp] = r;
+        sp++;
+        while (sp > 0) {
+            --sp;
+            const int S = st_s[sp];
+            const uint32_t node = st_n[sp];
+            const int P = pS[S];
+            const int parts[2] = {P, S ^ P};
+            uint32_t kids[2];
+            for (int c = 0; c < 2; ++c) {
+                if (__popc(parts[c]) == 1) kids[c] = leaves[__ffs(parts[c]) - 1];
+                else kids[c] = internals[next++];
             }
+            // children pointers (.w of the node's float4 pair); box written below
+            T.nbox[2 * (size_t)node].w = __uint_as_float(kids[0]);
+            T.nbox[2 * (size_t)node + 1].w = __uint_as_float(kids[1]);
+            for (int c = 0; c < 2; ++c) {
+                if (kids[c] & LEAF) T.leaf_parent[kids[c] & ~LEAF] = node;
+                else T.parent[kids[c]] = node;
+            }
+            post_s[np] = S;
+            post_n[np] = node;
+            np++;
+            for (int c = 1; c >= 0; --c)
+                if (!(kids[c] & LEAF) && __popc(parts[c]) > 1) {
+                    st_s[sp] = parts[c];
+                    st_n[sp] = kids[c];
+                    sp++;
+                }
+        }
+        for (int q = np - 1; q >= 0; --q) {
+            const int S = post_s[q];
+            const uint32_t x = post_n[q];
+            Box b = lb[__ffs(S) - 1];
+            for (int j = __ffs(S); j < nl; ++j)
+                if (S & (1 << j)) b = merge(b, lb[j]);
+            const uint32_t lc = __float_as_uint(T.nbox[2 * (size_t)x].w), rc = __float_as_uint(T.nbox[2 * (size_t)x + 1].w);
+            T.nbox[2 * (size_t)x] = make_float4(b.lo[0], b.lo[1], b.lo[2], __uint_as_float(lc));
+            T.nbox[2 * (size_t)x + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], __uint_as_float(rc));
+            T.count[x] = count_of_cg(T, lc) + count_of_cg(T, rc);
+            T.cost[x] = cS[S];
+        }
     }
-    for (int q = np - 1; q >= 0; --q) {
-        const int S = post_s[q];
-        const uint32_t x = post_n[q];
-        Box b = lb[__ffs(S) - 1];
-        for (int j = __ffs(S); j < nl; ++j)
-            if (S & (1 << j)) b = merge(b, lb[j]);
-        const uint32_t lc = __float_as_uint(T.nbox[2 * (size_t)x].w), rc = __float_as_uint(T.nbox[2 * (size_t)x + 1].w);
-        T.nbox[2 * (size_t)x] = make_float4(b.lo[0], b.lo[1], b.lo[2], __uint_as_float(lc));
-        T.nbox[2 * (size_t)x + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], __uint_as_float(rc));
-        T.count[x] = count_of_cg(T, lc) + count_of_cg(T, rc);
-        T.cost[x] = cS[S];
-    }
+    __syncwarp(); // the shared arrays are reused by the warp's next treelet
 }
 
-__global__ void k_treelet(Tree T, uint32_t n, uint32_t *__restrict__ visits, uint32_t gamma) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        uint32_t x = __ldcg(&T.leaf_parent[j]);
-        while (x != NONE) {
-            __threadfence();
-            if (atomicAdd(&visits[x], 1u) == 0u) break;
-            __threadfence();
-            if (__ldcg(&T.count[x]) >= gamma) optimize_treelet(T, x);
-            x = __ldcg(&T.parent[x]);
+// Bottom-up pass over the tree by warps of 32 leaves: a lane goes on to a
+// node's parent only on the node's second arrival (both subtrees final); the
+// nodes of at least `gamma` leaves that the lanes reach in a step are
+// restructured one after another by the whole warp.  Launched with 128
+// threads per block.
+__global__ void __launch_bounds__(128) k_treelet(Tree T, uint32_t n, uint32_t *__restrict__ visits, uint32_t gamma) {
+    __shared__ float s_a[4][128], s_c[4][128];
+    __shared__ uint8_t s_p[4][128];
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u; base < n; base += nwarps * 32u) {
+        const uint32_t j = base + lane;
+        uint32_t x = j < n ? __ldcg(&T.leaf_parent[j]) : NONE;
+        bool active = x != NONE;
+        while (__any_sync(0xFFFFFFFFu, active)) {
+            bool need = false;
+            if (active) {
+                __threadfence();
+                if (atomicAdd(&visits[x], 1u) == 0u) {
+                    active = false;
+                } else {
+                    __threadfence();
+                    need = __ldcg(&T.count[x]) >= gamma;
+                }
+            }
+            uint32_t m;
+            while ((m = __ballot_sync(0xFFFFFFFFu, need)) != 0u) {
+                const int leader = __ffs(m) - 1;
+                const uint32_t r = __shfl_sync(0xFFFFFFFFu, x, leader);
+                optimize_treelet(T, r, (int)lane == leader, s_a[wib], s_c[wib], s_p[wib]);
+                if ((int)lane == leader) need = false;
+            }
+            if (active) {
+                x = __ldcg(&T.parent[x]);
+                if (x == NONE) active = false;
+            }
         }
     }
 }

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "crg_internal.h"
@@ -173,9 +174,38 @@ double tri_area_of(const float *v) {
     return 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
 }
 
+// Runs fn(begin, end) over [0, n) in contiguous ranges on up to 16 host
+// threads (one range when n is small); each index is computed once, by the
+// same code, so the results do not depend on the split.
+template <class Fn>
+void parallel_ranges(size_t n, Fn fn) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = n < (1u << 16) ? 1 : std::min<size_t>(std::min(16u, hw), n);
+    if (nt <= 1) {
+        fn((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t step = (n + nt - 1) / nt;
+    try {
+        for (size_t t = 1; t < nt; ++t) {
+            const size_t b = t * step, e = std::min(n, b + step);
+            if (b < e) pool.emplace_back(fn, b, e);
+        }
+    } catch (...) { // no thread could be started: the rest on this one
+        const size_t done = (pool.size() + 1) * step;
+        if (done < n) fn(done, n);
+    }
+    fn((size_t)0, std::min(n, step));
+    for (auto &th : pool) th.join();
+}
+
 void compute_areas(crg_scene *s, const float *verts) {
     s->tri_area.assign(s->ntri, 0.0);
-    for (uint32_t p = 0; p < s->ntri; ++p) s->tri_area[p] = tri_area_of(verts + (size_t)p * 9);
+    double *a = s->tri_area.data();
+    parallel_ranges(s->ntri, [a, verts](size_t b, size_t e) {
+        for (size_t p = b; p < e; ++p) a[p] = tri_area_of(verts + p * 9);
+    });
 }
 
 // Alias table (Walker 1977, built with Vose's 1991 two-worklist method in
