@@ -309,16 +309,24 @@ __global__ void k_bottom_up(Tree T, uint32_t n, uint32_t *__restrict__ visits, i
 }
 
 // ----------------------------------------------------------------- treelets
+// A warp's working set for one treelet, in shared memory.
+struct TreeletWork {
+    float aS[128], cS[128]; // subset areas and costs
+    uint8_t pS[128];        // best partition of each subset
+    uint32_t leaves[7], internals[6];
+    float lb[7][6];         // the treelet leaves' boxes (lo.xyz, hi.xyz)
+};
+
 // The 7-leaf treelet rooted at r is restructured (Karras & Aila 2013) by the
 // 32 lanes of a warp, with the same result as the CPU form: growth by largest
-// area, DP over subsets in increasing size with partitions containing the
-// lowest set bit, first minimum kept (in the CPU's enumeration, q = rest,
-// (q - 1) & rest, ...: the larger partition wins a tie), internal nodes
-// reused in formation order, pre-order rebuild.  Every lane forms the
-// treelet (the same coherent loads); the subset areas and the DP are split
-// over the lanes, in shared memory; the owning lane `leader` (the one whose
-// arrival at r made it ready) writes the rebuilt nodes.
-__device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *aS, float *cS, uint8_t *pS) {
+// area (first maximum), DP over subsets in increasing size with partitions
+// containing the lowest set bit, first minimum kept (in the CPU's
+// enumeration, q = rest, (q - 1) & rest, ...: the larger partition wins a
+// tie), internal nodes reused in formation order, pre-order rebuild.  The
+// growth step's areas, the subset areas and the DP are split over the lanes;
+// the owning lane `leader` (the one whose arrival at r made it ready) writes
+// the rebuilt nodes.
+__device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, TreeletWork &w) {
     const uint32_t lane = threadIdx.x & 31u;
     float cost_r;
     {
@@ -326,38 +334,61 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
         cost_r = kCi * area(b) + (cost_of_cg(T, left_of(T, r)) + cost_of_cg(T, right_of(T, r)));
         if (leader) T.cost[r] = cost_r;
     }
-    uint32_t leaves[7];
-    uint32_t internals[6];
     int nl = 2, ni = 0;
-    leaves[0] = left_of(T, r);
-    leaves[1] = right_of(T, r);
+    if (lane == 0u) {
+        w.leaves[0] = left_of(T, r);
+        w.leaves[1] = right_of(T, r);
+    }
+    __syncwarp();
     while (nl < 7) {
-        int best = -1;
-        float best_a = -1.0f;
-        for (int j = 0; j < nl; ++j) {
-            if (leaves[j] & LEAF) continue;
-            const float a = area(box_of_cg(T, leaves[j]));
-            if (a > best_a) { best_a = a; best = j; }
+        // the internal leaf of largest area (lowest index on ties); none: the treelet is complete
+        const uint32_t lj = (int)lane < nl ? w.leaves[lane] : LEAF;
+        float a = -1.0f;
+        if (!(lj & LEAF)) {
+            a = area(box_of_cg(T, lj));
+            if (!(a > -1.0f)) a = -1.0f; // NaN: never chosen
         }
-        if (best < 0) break;
-        const uint32_t x = leaves[best];
-        internals[ni++] = x;
-        leaves[best] = left_of(T, x);
-        leaves[nl++] = right_of(T, x);
+        int bj = (int)lane;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const float oa = __shfl_xor_sync(0xFFFFFFFFu, a, off);
+            const int oj = __shfl_xor_sync(0xFFFFFFFFu, bj, off);
+            if (oa > a || (oa == a && oj < bj)) { a = oa; bj = oj; }
+        }
+        if (!(a > -1.0f)) break;
+        const uint32_t x = __shfl_sync(0xFFFFFFFFu, lj, bj);
+        if (lane == 0u) {
+            w.internals[ni] = x;
+            w.leaves[bj] = left_of(T, x);
+            w.leaves[nl] = right_of(T, x);
+        }
+        ++ni;
+        ++nl;
+        __syncwarp();
     }
-    if (nl < 3) return;
+    if (nl < 3) {
+        __syncwarp();
+        return;
+    }
     const int nsub = 1 << nl;
-    Box lb[7];
-    for (int j = 0; j < nl; ++j) lb[j] = box_of_cg(T, leaves[j]);
-    for (int s = (int)lane + 1; s < nsub; s += 32) {
-        Box b = lb[__ffs(s) - 1];
-        for (int j = __ffs(s); j < nl; ++j)
-            if (s & (1 << j)) b = merge(b, lb[j]);
-        aS[s] = area(b);
-    }
     if ((int)lane < nl) {
-        cS[1 << lane] = cost_of_cg(T, leaves[lane]);
-        pS[1 << lane] = 0;
+        const uint32_t lj = w.leaves[lane];
+        const Box b = box_of_cg(T, lj);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            w.lb[lane][k] = b.lo[k];
+            w.lb[lane][3 + k] = b.hi[k];
+        }
+        w.cS[1 << lane] = (lj & LEAF) ? kCt * area(b) : __ldcg(&T.cost[lj]);
+        w.pS[1 << lane] = 0;
+    }
+    __syncwarp();
+    for (int s = (int)lane + 1; s < nsub; s += 32) {
+        const int j0 = __ffs(s) - 1;
+        Box b{{w.lb[j0][0], w.lb[j0][1], w.lb[j0][2]}, {w.lb[j0][3], w.lb[j0][4], w.lb[j0][5]}};
+        for (int j = j0 + 1; j < nl; ++j)
+            if (s & (1 << j)) b = merge(b, Box{{w.lb[j][0], w.lb[j][1], w.lb[j][2]}, {w.lb[j][3], w.lb[j][4], w.lb[j][5]}});
+        w.aS[s] = area(b);
     }
     __syncwarp();
     for (int k = 2; k <= nl; ++k) {
@@ -372,13 +403,13 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
                 for (int q = rest;; q = (q - 1) & rest) {
                     const int P = q | low;
                     if (P != s) {
-                        const float c = cS[P] + cS[s ^ P];
+                        const float c = w.cS[P] + w.cS[s ^ P];
                         if (c < best) { best = c; bp = P; }
                     }
                     if (q == 0) break;
                 }
-                cS[s] = kCi * aS[s] + best;
-                pS[s] = (uint8_t)bp;
+                w.cS[s] = kCi * w.aS[s] + best;
+                w.pS[s] = (uint8_t)bp;
             }
         } else {
             // subsets of 6 or 7 leaves one at a time, their 31 / 63 partitions over the lanes
@@ -386,7 +417,7 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
                 if (__popc(s) != k) continue;
                 const int low = s & -s;
                 const int rest = s ^ low;
-                const int m = k - 1, npart = (1 << m) - 1; // q = rest (P == s) excluded
+                const int npart = (1 << (k - 1)) - 1; // q = rest (P == s) excluded
                 float best = INFINITY;
                 int bp = -1;
                 for (int t = (int)lane; t < npart; t += 32) {
@@ -394,7 +425,7 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
                     for (int rr = rest; rr; rr &= rr - 1, ++bit)
                         if (t & (1 << bit)) q |= rr & -rr;
                     const int P = q | low;
-                    const float c = cS[P] + cS[s ^ P];
+                    const float c = w.cS[P] + w.cS[s ^ P];
                     if (c < best || (c == best && P > bp)) { best = c; bp = P; }
                 }
 #pragma unroll
@@ -404,15 +435,15 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
                     if (oc < best || (oc == best && op > bp)) { best = oc; bp = op; }
                 }
                 if (lane == 0u) {
-                    cS[s] = kCi * aS[s] + best;
-                    pS[s] = (uint8_t)bp;
+                    w.cS[s] = kCi * w.aS[s] + best;
+                    w.pS[s] = (uint8_t)bp;
                 }
             }
         }
         __syncwarp();
     }
     const int full = nsub - 1;
-    if (!(cS[full] < cost_r)) {
+    if (!(w.cS[full] < cost_r)) {
         __syncwarp();
         return;
     }
@@ -431,12 +462,12 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
             --sp;
             const int S = st_s[sp];
             const uint32_t node = st_n[sp];
-            const int P = pS[S];
+            const int P = w.pS[S];
             const int parts[2] = {P, S ^ P};
             uint32_t kids[2];
             for (int c = 0; c < 2; ++c) {
-                if (__popc(parts[c]) == 1) kids[c] = leaves[__ffs(parts[c]) - 1];
-                else kids[c] = internals[next++];
+                if (__popc(parts[c]) == 1) kids[c] = w.leaves[__ffs(parts[c]) - 1];
+                else kids[c] = w.internals[next++];
             }
             // children pointers (.w of the node's float4 pair); box written below
             T.nbox[2 * (size_t)node].w = __uint_as_float(kids[0]);
@@ -458,17 +489,18 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
         for (int q = np - 1; q >= 0; --q) {
             const int S = post_s[q];
             const uint32_t x = post_n[q];
-            Box b = lb[__ffs(S) - 1];
-            for (int j = __ffs(S); j < nl; ++j)
-                if (S & (1 << j)) b = merge(b, lb[j]);
+            const int j0 = __ffs(S) - 1;
+            Box b{{w.lb[j0][0], w.lb[j0][1], w.lb[j0][2]}, {w.lb[j0][3], w.lb[j0][4], w.lb[j0][5]}};
+            for (int j = j0 + 1; j < nl; ++j)
+                if (S & (1 << j)) b = merge(b, Box{{w.lb[j][0], w.lb[j][1], w.lb[j][2]}, {w.lb[j][3], w.lb[j][4], w.lb[j][5]}});
             const uint32_t lc = __float_as_uint(T.nbox[2 * (size_t)x].w), rc = __float_as_uint(T.nbox[2 * (size_t)x + 1].w);
             T.nbox[2 * (size_t)x] = make_float4(b.lo[0], b.lo[1], b.lo[2], __uint_as_float(lc));
             T.nbox[2 * (size_t)x + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], __uint_as_float(rc));
             T.count[x] = count_of_cg(T, lc) + count_of_cg(T, rc);
-            T.cost[x] = cS[S];
+            T.cost[x] = w.cS[S];
         }
     }
-    __syncwarp(); // the shared arrays are reused by the warp's next treelet
+    __syncwarp(); // the warp's next treelet reuses the working set
 }
 
 // Bottom-up pass over the tree by warps of 32 leaves: a lane goes on to a
@@ -477,8 +509,7 @@ __device__ void optimize_treelet(const Tree &T, uint32_t r, bool leader, float *
 // restructured one after another by the whole warp.  Launched with 128
 // threads per block.
 __global__ void __launch_bounds__(128) k_treelet(Tree T, uint32_t n, uint32_t *__restrict__ visits, uint32_t gamma) {
-    __shared__ float s_a[4][128], s_c[4][128];
-    __shared__ uint8_t s_p[4][128];
+    __shared__ TreeletWork s_w[4];
     const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u; base < n; base += nwarps * 32u) {
@@ -500,7 +531,7 @@ __global__ void __launch_bounds__(128) k_treelet(Tree T, uint32_t n, uint32_t *_
             while ((m = __ballot_sync(0xFFFFFFFFu, need)) != 0u) {
                 const int leader = __ffs(m) - 1;
                 const uint32_t r = __shfl_sync(0xFFFFFFFFu, x, leader);
-                optimize_treelet(T, r, (int)lane == leader, s_a[wib], s_c[wib], s_p[wib]);
+                optimize_treelet(T, r, (int)lane == leader, s_w[wib]);
                 if ((int)lane == leader) need = false;
             }
             if (active) {
