@@ -233,6 +233,8 @@ CRG_SIGNATURES = [
     ("crg_batch_stage_times_get", C.c_int, [vp, P(StageTimes)]),
     ("crg_autotune_batch", C.c_int, [P(vp), C.c_uint32, P(View), C.c_uint32, P(AutotuneOpts), P(WavefrontOpts),
                                      P(C.c_uint32), P(AutotuneTrial), C.c_uint32, P(C.c_uint32), c_stream]),
+    ("crg_autotune_cache_save", C.c_int, [vp, C.c_char_p]),
+    ("crg_autotune_cache_load", C.c_int, [vp, C.c_char_p, P(C.c_uint32)]),
     ("crg_render_stats_get", C.c_int, [vp, P(RenderStats)]),
     ("crg_scene_set_counting", C.c_int, [vp, C.c_int]),
 ]

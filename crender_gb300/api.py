@@ -8,6 +8,7 @@ names follow the reference interface they stand for: Scene ~ cr::scene
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -414,6 +415,19 @@ def batch_stats(ctx) -> dict:
     ctx.check(ctx.lib.crg_batch_stats_get(ctx.h, C.byref(s)))
     return dict(samples=s.samples, segments=s.segments, shadow_rays=s.shadow_rays, nodes_visited=s.nodes_visited,
                 tris_tested=s.tris_tested, iterations=s.iterations)
+
+
+def autotune_cache_save(ctx, path: str):
+    """crg_autotune_cache_save: the context's autotuner answers to a text file."""
+    ctx.check(ctx.lib.crg_autotune_cache_save(ctx.h, os.fsencode(path)))
+
+
+def autotune_cache_load(ctx, path: str) -> int:
+    """crg_autotune_cache_load: adds a file's answers (measured on this kind of device) to
+    the context's cache; returns how many were read."""
+    n = C.c_uint32(0)
+    ctx.check(ctx.lib.crg_autotune_cache_load(ctx.h, os.fsencode(path), C.byref(n)))
+    return n.value
 
 
 def stage_times(ctx) -> dict:

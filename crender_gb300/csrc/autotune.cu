@@ -233,3 +233,103 @@ extern "C" crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nsce
         }
     return CRG_OK;
 }
+
+namespace {
+
+// "name|sm_count" of the context's device, spaces kept out of the line format
+std::string device_tag(crg_context *ctx) {
+    cudaDeviceProp p{};
+    if (cudaGetDeviceProperties(&p, ctx->device) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return "unknown|0";
+    }
+    std::string name(p.name);
+    for (char &c : name)
+        if (c == ' ' || c == '\t' || c == '\n' || c == '|') c = '_';
+    return name + "|" + std::to_string(p.multiProcessorCount);
+}
+
+constexpr const char *kCacheHeader = "crg-autotune-cache 1";
+
+} // namespace
+
+extern "C" crg_status crg_autotune_cache_save(crg_context *ctx, const char *path) {
+    if (!ctx || !path) return set_error(ctx, CRG_ERR_INVALID_ARG, "autotune cache: null argument");
+    std::FILE *f = std::fopen(path, "w");
+    if (!f) return set_error(ctx, CRG_ERR_INVALID_ARG, std::string("autotune cache: cannot write ") + path);
+    bool ok = std::fprintf(f, "%s\ndevice %s\n", kCacheHeader, device_tag(ctx).c_str()) > 0;
+    for (const auto &kv : ctx->tune_cache) {
+        const crg_wavefront_opts &o = kv.second.opts;
+        ok = ok && std::fprintf(f, "%s\t%u\t%u %u %u %u %u %u %u %u %u\t", kv.first.c_str(), kv.second.width, o.path_pool,
+                                o.chunk_samples, o.block_size, o.fetch, o.max_iterations, o.count_work, o.host_loop,
+                                o.fuse, o.refill) > 0;
+        for (size_t i = 0; i < kv.second.leaf.size(); ++i)
+            ok = ok && std::fprintf(f, i ? ",%u" : "%u", kv.second.leaf[i]) > 0;
+        ok = ok && std::fputc('\n', f) != EOF;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return set_error(ctx, CRG_ERR_INVALID_ARG, std::string("autotune cache: write failed: ") + path);
+    return CRG_OK;
+}
+
+extern "C" crg_status crg_autotune_cache_load(crg_context *ctx, const char *path, uint32_t *count) {
+    if (count) *count = 0;
+    if (!ctx || !path) return set_error(ctx, CRG_ERR_INVALID_ARG, "autotune cache: null argument");
+    std::FILE *f = std::fopen(path, "r");
+    if (!f) return set_error(ctx, CRG_ERR_INVALID_ARG, std::string("autotune cache: cannot open ") + path);
+    std::vector<std::string> lines;
+    {
+        std::string cur;
+        int ch;
+        while ((ch = std::fgetc(f)) != EOF) {
+            if (ch == '\n') {
+                lines.push_back(cur);
+                cur.clear();
+            } else {
+                cur.push_back((char)ch);
+            }
+        }
+        if (!cur.empty()) lines.push_back(cur);
+        std::fclose(f);
+    }
+    auto bad = [&](size_t line) {
+        return set_error(ctx, CRG_ERR_INVALID_ARG,
+                         std::string("autotune cache: malformed line ") + std::to_string(line + 1) + " of " + path);
+    };
+    if (lines.size() < 2 || lines[0] != kCacheHeader) return bad(0);
+    if (lines[1].compare(0, 7, "device ") != 0) return bad(1);
+    if (lines[1].substr(7) != device_tag(ctx)) return CRG_OK; // measured on another kind of device
+    std::vector<std::pair<std::string, crg_context::Tuned>> got;
+    for (size_t i = 2; i < lines.size(); ++i) {
+        const std::string &l = lines[i];
+        if (l.empty()) continue;
+        const size_t t1 = l.find('\t');
+        const size_t t2 = t1 == std::string::npos ? t1 : l.find('\t', t1 + 1);
+        const size_t t3 = t2 == std::string::npos ? t2 : l.find('\t', t2 + 1);
+        if (t3 == std::string::npos || t1 == 0) return bad(i);
+        crg_context::Tuned tu{};
+        crg_wavefront_opts &o = tu.opts;
+        char tail = 0;
+        if (std::sscanf(l.substr(t1 + 1, t2 - t1 - 1).c_str(), "%u%c", &tu.width, &tail) != 1) return bad(i);
+        if (!(tu.width == 2 || tu.width == 4 || tu.width == 8)) return bad(i);
+        if (std::sscanf(l.substr(t2 + 1, t3 - t2 - 1).c_str(), "%u %u %u %u %u %u %u %u %u%c", &o.path_pool,
+                        &o.chunk_samples, &o.block_size, &o.fetch, &o.max_iterations, &o.count_work, &o.host_loop,
+                        &o.fuse, &o.refill, &tail) != 9)
+            return bad(i);
+        const std::string leaves = l.substr(t3 + 1);
+        size_t p = 0;
+        while (p < leaves.size()) {
+            size_t q = leaves.find(',', p);
+            if (q == std::string::npos) q = leaves.size();
+            unsigned v = 0;
+            if (q == p || std::sscanf(leaves.substr(p, q - p).c_str(), "%u%c", &v, &tail) != 1 || v < 1 || v > 3)
+                return bad(i);
+            tu.leaf.push_back(v);
+            p = q + 1;
+        }
+        got.emplace_back(l.substr(0, t1), tu);
+    }
+    for (auto &kv : got) ctx->tune_cache[kv.first] = kv.second;
+    if (count) *count = (uint32_t)got.size();
+    return CRG_OK;
+}

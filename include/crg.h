@@ -629,6 +629,20 @@ crg_status crg_autotune_batch(crg_scene *const *scenes, uint32_t nscenes, const 
                               crg_autotune_trial *trials, uint32_t trials_cap, uint32_t *ntrials,
                               crg_stream stream);
 
+/* The context's autotuner cache outlives the process through a text file: one
+ * header line, a line naming the device the answers were measured on (name and
+ * SM count), then one line per batch shape (shape key, BVH width, the nine
+ * crg_wavefront_opts fields, the scenes' leaf sizes).  crg_autotune_cache_save
+ * writes every cached answer (an empty cache writes the two header lines).
+ * crg_autotune_cache_load adds a file's answers to the cache, replacing
+ * answers for the same shapes, and stores how many it read in *count (may be
+ * NULL).  A file written on another kind of device reads nothing (CRG_OK,
+ * *count = 0): the answers are timings of that device.  A file that cannot be
+ * opened or a malformed line fails with CRG_ERR_INVALID_ARG, and then nothing
+ * of the file is added. */
+crg_status crg_autotune_cache_save(crg_context *ctx, const char *path);
+crg_status crg_autotune_cache_load(crg_context *ctx, const char *path, uint32_t *count);
+
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replaces the material table (same count, e.g. after an optimiser step)

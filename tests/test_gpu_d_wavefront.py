@@ -10,7 +10,7 @@ leave the context usable."""
 import numpy as np
 import pytest
 
-from crender_gb300 import api, scenes
+from crender_gb300 import CrgError, api, scenes
 from test_gpu_c_render import _box_variant
 
 pytestmark = pytest.mark.gpu
@@ -225,6 +225,47 @@ def test_autotune_leaf_sizes(ctx):
     finally:
         sa.close()
         sb.close()
+
+
+def test_autotune_cache_file(ctx, tmp_path):
+    """The autotuner's answers survive the process: saved to a file, loaded by
+    a fresh context, they answer the same batch shape without trials (scenes
+    rebuilt at the saved width and leaf sizes); a file from another kind of
+    device reads nothing; a malformed file is refused and adds nothing."""
+    a = _box_variant("plain")
+    views = [(0, a["camera"], api.make_settings(48, 48, 16, 8, 3, 1, 1))]
+    leaves = (1 << 1) | (1 << 2) | (1 << 3)
+    path = str(tmp_path / "tune.txt")
+    sa = api.Scene(ctx, a["verts"], a["mat_idx"], a["mats"]).build(8, 1)
+    try:
+        opts, width, _ = api.autotune_batch([sa], views, sample_budget=1 << 15, widths=4 | 8, leaves=leaves)
+        leaf = sa.info()["leaf_max"]
+        api.autotune_cache_save(ctx, path)
+    finally:
+        sa.close()
+    text = open(path).read().splitlines()
+    assert text[0] == "crg-autotune-cache 1" and text[1].startswith("device ") and len(text) >= 3
+    ctx2 = api.Context(0)
+    try:
+        assert api.autotune_cache_load(ctx2, path) == len(text) - 2
+        s2 = api.Scene(ctx2, a["verts"], a["mat_idx"], a["mats"]).build(2 if width != 2 else 4, 1, 3)
+        try:
+            again, width2, trials = api.autotune_batch([s2], views, sample_budget=1 << 15, widths=4 | 8, leaves=leaves)
+            assert trials == [] and again == opts and width2 == width
+            assert s2.info()["width"] == width and s2.info()["leaf_max"] == leaf
+        finally:
+            s2.close()
+        other = tmp_path / "other.txt"
+        other.write_text("\n".join([text[0], "device Some_Other_GPU|8"] + text[2:]) + "\n")
+        assert api.autotune_cache_load(ctx2, str(other)) == 0
+        bad = tmp_path / "bad.txt"
+        bad.write_text("\n".join(text[:2] + ["shape-without-fields"]) + "\n")
+        with pytest.raises(CrgError):
+            api.autotune_cache_load(ctx2, str(bad))
+        with pytest.raises(CrgError):
+            api.autotune_cache_load(ctx2, str(tmp_path / "missing.txt"))
+    finally:
+        ctx2.close()
 
 
 @pytest.mark.parametrize("fuse", [1, 2])
