@@ -216,19 +216,6 @@ __device__ __forceinline__ float2 qpair(uint32_t word, int k) {
     return __fadd2_rn(biased, make_float2(-8388608.0f, -8388608.0f));
 }
 
-// Three-input minimum / maximum (one instruction on sm_100 and later); for
-// non-NaN inputs the same value as two fminf / fmaxf.
-__device__ __forceinline__ float fmax3(float a, float b, float c) {
-    float d;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-__device__ __forceinline__ float fmin3(float a, float b, float c) {
-    float d;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-
 struct TravStats {
     uint32_t nodes, tris;
 };
@@ -317,8 +304,8 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
             const uint32_t mw = w[ME + wi];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const float tn = fmax3(h ? txn.y : txn.x, h ? tyn.y : tyn.x, fmaxf(h ? tzn.y : tzn.x, r.tmin));
-                const float tf = fmin3(h ? txf.y : txf.x, h ? tyf.y : tyf.x, fminf(h ? tzf.y : tzf.x, tfar));
+                const float tn = fmaxf(fmaxf(h ? txn.y : txn.x, h ? tyn.y : tyn.x), fmaxf(h ? tzn.y : tzn.x, r.tmin));
+                const float tf = fminf(fminf(h ? txf.y : txf.x, h ? tyf.y : tyf.x), fminf(h ? tzf.y : tzf.x, tfar));
                 const uint32_t meta = (mw >> (8 * (bo + h))) & 0xFFu;
                 if (tn <= tf * 1.00000095f) bits |= (meta >> 5) << (meta & 31u);
             }
