@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
 
 // Extend with per-lane ray refill (dyn_traverse): the same hits as k_wf_extend.
 template <int W, bool CNT>
-__global__ void __launch_bounds__(256, 4) k_wf_extend_dyn(Wf w) {
+__global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
     const uint32_t *in = q_in(w, *c);
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_extend_dyn(Wf w) {
 // are all emitter tests (any hit below tmax); sun requests (faithful
 // estimator with the sun on) go through k_wf_shadow.
 template <int W, bool CNT>
-__global__ void __launch_bounds__(256, 4) k_wf_shadow_dyn(Wf w) {
+__global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->sh_count;
     TravStats st{0, 0};
