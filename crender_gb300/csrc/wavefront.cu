@@ -76,6 +76,8 @@ struct Ctrl {
 
 constexpr uint32_t kFinish = 1u << 31;    // meta.x flag: finish after the shadow test
 constexpr uint32_t kPrevDelta = 1u << 30; // meta.x flag: previous bounce was a delta lobe
+constexpr uint32_t kFresh = 1u << 29;     // meta.x flag: a new sample whose camera ray, throughput and
+                                          // radiance are not stored (derived from view, pixel and sample)
 
 struct Wf {
     Ctrl *ctrl;
@@ -124,8 +126,34 @@ __device__ __forceinline__ void warp_push(bool want, uint32_t value, uint32_t *q
     if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
 }
 
-// Starts sample `gid` of the batch in path slot `slot` (camera ray, empty
-// throughput and radiance), exactly as the megakernel starts a sample.
+// The camera ray of `sample` at pixel `pix` of view V, exactly as the
+// megakernel starts a sample.
+__device__ __forceinline__ void sample_ray(const ViewDev &V, uint32_t pix, uint32_t sample, v3 &o, v3 &d) {
+    const uint32_t Wd = V.set.width, Hd = V.set.height;
+    const uint32_t px = pix % Wd, py = pix / Wd;
+    const f4 g0 = rand4(pix, sample, 0, V.set.seed);
+    const float x = ((float)px + g0.x) / (float)Wd;
+    const float y = ((float)py + g0.y) / (float)Hd;
+    camera_ray(V.cam, x, y, V.set.aspect, o, d);
+}
+
+// The ray a path traces next: a new sample's camera ray (recomputed), else
+// the stored one.
+__device__ __forceinline__ void path_ray(const Wf &w, uint32_t slot, const uint4 &m, float4 &o, float4 &d) {
+    if (m.x & kFresh) {
+        v3 a, b;
+        sample_ray(w.views[m.x & 0xFFFFu], m.y, m.z, a, b);
+        o = make_float4(a.x, a.y, a.z, 0.0f);
+        d = make_float4(b.x, b.y, b.z, 0.0f);
+    } else {
+        o = w.o[slot];
+        d = w.d[slot];
+    }
+}
+
+// Starts sample `gid` of the batch in path slot `slot`: only its meta word is
+// written (kFresh: camera ray, unit throughput and zero radiance are implied;
+// extend and shade derive them).
 __device__ void start_sample(const Wf &w, uint32_t slot, unsigned long long gid, const Chunk &ch) {
     uint32_t lo = ch.seg_begin, hi = ch.seg_end - 1;
     while (lo < hi) {
@@ -139,18 +167,7 @@ __device__ void start_sample(const Wf &w, uint32_t slot, unsigned long long gid,
     const uint32_t s = sg.s0 + (uint32_t)(rel / V.npix);
     const uint32_t pix = (uint32_t)(rel % V.npix);
     const uint32_t sample = (uint32_t)(V.spp0 + s);
-    const uint32_t Wd = V.set.width, Hd = V.set.height;
-    const uint32_t px = pix % Wd, py = pix / Wd;
-    const f4 g0 = rand4(pix, sample, 0, V.set.seed);
-    const float x = ((float)px + g0.x) / (float)Wd;
-    const float y = ((float)py + g0.y) / (float)Hd;
-    v3 o, d;
-    camera_ray(V.cam, x, y, V.set.aspect, o, d);
-    w.o[slot] = make_float4(o.x, o.y, o.z, 0.0f);
-    w.d[slot] = make_float4(d.x, d.y, d.z, 0.0f);
-    w.T[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    w.L[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    w.meta[slot] = make_uint4(sg.view | kPrevDelta, pix, sample, (uint32_t)(gid - ch.gid_begin));
+    w.meta[slot] = make_uint4(sg.view | kPrevDelta | kFresh, pix, sample, (uint32_t)(gid - ch.gid_begin));
 }
 
 // Writes a finished sample and, if the chunk has more, starts the next one
@@ -190,9 +207,10 @@ __global__ void __launch_bounds__(256) k_wf_extend(Wf w) {
             const unsigned int qi = base + k;
             if (qi >= n) break;
             const uint32_t slot = in[qi];
-            const uint32_t view = w.meta[slot].x & 0xFFFFu;
-            const SceneDev &S = w.scenes[w.views[view].scene];
-            const float4 o = w.o[slot], d = w.d[slot];
+            const uint4 m = w.meta[slot];
+            const SceneDev &S = w.scenes[w.views[m.x & 0xFFFFu].scene];
+            float4 o, d;
+            path_ray(w, slot, m, o, d);
             PathCtx C{0, 0, 0, 0, 0, 0, 0ull, 0ull};
             Hit h;
             const bool found = closest<W, CNT, INST>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), INFINITY, h, C);
@@ -246,7 +264,15 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 const uint32_t view = m.x & 0xFFFFu, depth = (m.x >> 16) & 0x3FFu;
                 const ViewDev &V = w.views[view];
                 const SceneDev &S = w.scenes[V.scene];
-                const float4 o = w.o[slot], d = w.d[slot], T = w.T[slot], L = w.L[slot];
+                float4 o, d, T, L;
+                path_ray(w, slot, m, o, d);
+                if (m.x & kFresh) {
+                    T = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                    L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                } else {
+                    T = w.T[slot];
+                    L = w.L[slot];
+                }
                 PathCtx C{m.y, m.z, V.set.seed, 0, 0, 0, 0ull, 0ull};
                 float4 h4;
                 if (FUSE >= 2) {
@@ -383,10 +409,12 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
         &c->head_ext, n, w.refill,
         [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
             slot = in[qi];
-            const SceneDev &S = w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene];
+            const uint4 m = w.meta[slot];
+            const SceneDev &S = w.scenes[w.views[m.x & 0xFFFFu].scene];
             nodes = S.nodes;
             tris = S.tris;
-            const float4 o = w.o[slot], d = w.d[slot];
+            float4 o, d;
+            path_ray(w, slot, m, o, d);
             r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
             tmax = INFINITY;
             return true;
