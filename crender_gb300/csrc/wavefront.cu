@@ -315,8 +315,8 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                     tris += C.tris;
                 }
                 Lv = make_float4(ps.L.x, ps.L.y, ps.L.z, 0.0f);
-                w.L[slot] = Lv;
                 off = m.w;
+                finishing = !cont && (FUSE >= 1 || !shadow);
                 if (FUSE == 0 && shadow) {
                     w.sh_o[slot] = make_float4(nr.o.x, nr.o.y, nr.o.z, nr.tmax);
                     w.sh_d[slot] = make_float4(nr.d.x, nr.d.y, nr.d.z, __uint_as_float(nr.kind));
@@ -325,13 +325,15 @@ __global__ void __launch_bounds__(256, FUSE == 0 ? 3 : 2) k_wf_shade(Wf w) {
                 uint32_t mx_ = (m.x & 0xFFFFu) | ((depth + 1) << 16) | (ps.prev_delta ? kPrevDelta : 0u);
                 if (FUSE == 0 && !cont && shadow) mx_ |= kFinish;
                 m.x = mx_;
-                w.meta[slot] = m;
+                if (!finishing) { // a finishing path's radiance goes to its sample slot; its state is dead
+                    w.L[slot] = Lv;
+                    w.meta[slot] = m;
+                }
                 if (cont) {
                     w.o[slot] = make_float4(ps.o.x, ps.o.y, ps.o.z, 0.0f);
                     w.d[slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, 0.0f);
                     w.T[slot] = make_float4(ps.T.x, ps.T.y, ps.T.z, ps.prev_pdf);
                 }
-                finishing = !cont && (FUSE >= 1 || !shadow);
             }
             if (FUSE == 0) warp_push(valid && shadow, slot, w.qsh, &c->sh_count);
             else warp_count(valid && shadow, &c->sh_count);
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
     const uint32_t *in = q_in(w, *c);
     TravStats st{0, 0};
     uint32_t err = 0;
-    dyn_traverse<W, false, CNT, 4>(
+    dyn_traverse<W, false, CNT, 8>(
         &c->head_ext, n, w.refill,
         [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
             slot = in[qi];
@@ -441,7 +443,7 @@ __global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
     const unsigned int n = c->sh_count;
     TravStats st{0, 0};
     uint32_t err = 0;
-    dyn_traverse<W, true, CNT, 4>(
+    dyn_traverse<W, true, CNT, 8>(
         &c->head_sh, n, w.refill_sh,
         [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
             slot = w.qsh[qi];
