@@ -143,9 +143,9 @@ TRAFFIC_SOUP_LAUNCH = 923.3e6
 
 
 # DRAM bytes per traversed ray (read + write) of the extend kernel, from the displaced-scene
-# iteration capture (profiles/wavefront_displaced_iteration_full.md, build B: 795 MB over one
+# iteration capture (profiles/wavefront_displaced_iteration_full.md, build C: 811 MB over one
 # full-queue iteration of a 4,194,304-path pool, one ray per path)
-DRAM_PER_RAY = {"extend": 795e6 / 4194304}
+DRAM_PER_RAY = {"extend": 811.3e6 / 4194304}
 
 
 def traffic_dominant(out, stage):
@@ -170,8 +170,8 @@ def traffic_estimate(workload, out, units):
 
 
 # L2 hit rates (lts__t_sector_hit_rate) of the traversal kernels from ncu captures on a GB300
-# (profiles/wavefront_displaced_iteration_full.md, build B; profiles/k_intersect_soup_full.md)
-L2_HIT = {"extend": 0.581, "shadow": 0.595, "soup_closest": 0.880, "soup_any": 0.860}
+# (profiles/wavefront_displaced_iteration_full.md, build C; profiles/k_intersect_soup_full.md)
+L2_HIT = {"extend": 0.671, "shadow": 0.671, "soup_closest": 0.880, "soup_any": 0.860}
 
 
 def stage_roofline(tuned, work, sh_work, stages, node_bytes, peak):
@@ -205,7 +205,7 @@ def stage_roofline(tuned, work, sh_work, stages, node_bytes, peak):
                    "traversal work from an instrumented frame"}
 
 
-def workload_config(w):
+def workload_config(w, form="megakernel"):
     if w == "post":
         return {"workload": "post-processing of a 3840x2160 RGBA32F image: bloom threshold + 10 separable 15-tap "
                             "blur passes + composite with the Uncharted tone curve (every pixel covered)",
@@ -217,11 +217,11 @@ def workload_config(w):
                             "treelet-optimised BVH",
                 "views": 64, "samples_per_step": 4728979456, "l2": L2_NOTE}
     if w == "box":
-        return {"workload": "box scene (36 tris) 512x512, 64 spp, 8 segments, RR from 3, extended estimator, megakernel",
+        return {"workload": "box scene (36 tris) 512x512, 64 spp, 8 segments, RR from 3, extended estimator, " + form,
                 "resolution": [512, 512], "spp": 64, "max_bounces": 8, "rr_depth": 3, "l2": L2_NOTE}
     if w == "displaced":
         return {"workload": "displaced icosphere (4,196,562 tris) 1920x1080, 16 spp per step, depth 16, RR from 3, "
-                            "extended estimator, megakernel", "l2": L2_NOTE}
+                            "extended estimator, " + form, "l2": L2_NOTE}
     if w == "inverse":
         return {"workload": "inverse rendering, box scene with 34 per-triangle albedos + light radiance, 256x256, "
                             "32 spp forward + L2 loss vs a 4096-spp target + 32 spp path-replay backward, depth 8, "
@@ -323,7 +323,7 @@ def run_reference(args):
     print(json.dumps({
         "impl": "reference", "metric": unit, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": workload_config(args.workload),
+        "data": "synthetic", "config": workload_config(args.workload, args.form),
         "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU oracle: C++ restatement of CRender's estimator with an LBVH + watertight traversal standing in "
@@ -941,7 +941,7 @@ def main():
     elif args.workload == "soup":
         roofline["l2_hit_rate"] = L2_HIT["soup_closest"]
         roofline["l2_hit_rate_source"] = "ncu capture of the same launch (profiles/k_intersect_soup_full.md)"
-    config = workload_config(args.workload)
+    config = workload_config(args.workload, args.form)
     if args.workload == "batch":
         config["samples_per_step"] = units
         if args.spp_div > 1:
