@@ -421,12 +421,16 @@ __device__ __forceinline__ void traverse(const uint4 *__restrict__ nodes, const 
 // at once) as soon as at least `min_refill` lanes are idle, so long queries
 // no longer hold the short ones' lanes idle.  Between refill checks each busy
 // lane advances its query by up to STEPS node visits.
-//   fetch(idx, payload&, r&, tmax&, nodes&, tris&) -> bool: loads query idx;
-//        false = the query was completed inside fetch (no traversal needed)
+//   fetch(idx, payload&, r&, tmax&, root&, nodes&, tris&) -> bool: loads query
+//        idx and its first traversal (BVH root node); false = the query was
+//        completed inside fetch (no traversal needed)
+//   advance(payload, const Trav&, r&, tmax&, root&) -> bool: called when a
+//        traversal ends; true = the query goes on with another traversal
+//        (the next placement of a scene), set up in r, tmax and root
 //   done(payload, const Trav&): consumes a finished query
-template <int W, bool ANY, bool COUNT, int STEPS, class Fetch, class Done>
+template <int W, bool ANY, bool COUNT, int STEPS, class Fetch, class Advance, class Done>
 __device__ __forceinline__ void dyn_traverse(unsigned int *head, unsigned int n, uint32_t min_refill, Fetch &&fetch,
-                                             Done &&done, TravStats &st, uint32_t &err) {
+                                             Advance &&advance, Done &&done, TravStats &st, uint32_t &err) {
     const uint32_t lane = threadIdx.x & 31u;
     bool has = false, exhausted = false;
     uint32_t payload = 0;
@@ -447,8 +451,9 @@ __device__ __forceinline__ void dyn_traverse(unsigned int *head, unsigned int n,
                 const unsigned int my = base + (unsigned int)__popc(idle & ((1u << lane) - 1u));
                 if (my < n) {
                     float tmax;
-                    if (fetch(my, payload, r, tmax, nodes, tris)) {
-                        trav_init(T, r, tmax);
+                    uint32_t root = 0u;
+                    if (fetch(my, payload, r, tmax, root, nodes, tris)) {
+                        trav_init(T, r, tmax, root);
                         has = true;
                     }
                 }
@@ -459,8 +464,14 @@ __device__ __forceinline__ void dyn_traverse(unsigned int *head, unsigned int n,
             continue;
         }
         if (has && trav_step<W, ANY, COUNT>(T, stack, nodes, tris, r, STEPS, st, err)) {
-            has = false;
-            done(payload, T);
+            float tmax;
+            uint32_t root = 0u;
+            if (advance(payload, T, r, tmax, root)) {
+                trav_init(T, r, tmax, root);
+            } else {
+                has = false;
+                done(payload, T);
+            }
         }
     }
 }

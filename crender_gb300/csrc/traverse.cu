@@ -93,8 +93,10 @@ __global__ void __launch_bounds__(128) k_intersect_dyn(const uint4 *__restrict__
     uint32_t e = 0;
     dyn_traverse<W, ANY, false, 4>(
         head, n, refill,
-        [&](unsigned int i, uint32_t &payload, RayPre &r, float &tmax, const uint4 *&nd, const float4 *&tr) {
+        [&](unsigned int i, uint32_t &payload, RayPre &r, float &tmax, uint32_t &root, const uint4 *&nd,
+            const float4 *&tr) {
             payload = i;
+            root = 0u;
             const float4 r0 = __ldg(&rays[2 * (size_t)i]);
             const float4 r1 = __ldg(&rays[2 * (size_t)i + 1]);
             r = ray_prep(r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r0.w);
@@ -103,6 +105,7 @@ __global__ void __launch_bounds__(128) k_intersect_dyn(const uint4 *__restrict__
             tr = tris;
             return true;
         },
+        [](uint32_t, const Trav &, RayPre &, float &, uint32_t &) { return false; },
         [&](uint32_t i, const Trav &T) {
             if (ANY) {
                 occluded[i] = T.occluded ? 1u : 0u;

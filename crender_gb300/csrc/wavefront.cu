@@ -88,7 +88,8 @@ struct Wf {
     uint32_t nchunks, P, fetch;
     uint32_t refill;       // extend: 0 = static fetch of `fetch` entries, else the per-lane refill threshold
     uint32_t refill_sh;    // shadow: the same (0 when a batch can produce sun requests)
-    uint32_t pad_[3];
+    uint32_t placed;       // 1: a scene of the batch has placements (the refill kernels loop over them)
+    uint32_t pad_[2];
     float4 *o, *d, *T, *L; // T.w = prev_pdf
     uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
     float4 *hit;           // t, prim bits, triangle slot bits, found
@@ -400,16 +401,26 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
 }
 
 // Extend with per-lane ray refill (dyn_traverse): the same hits as k_wf_extend.
-template <int W, bool CNT>
+// PL: batches whose scenes may have placements (at most kLoopPlacements of
+// them): a lane traces its ray through the placements one after the other, as
+// closest_placement_loop does, each placement a traversal of its own that the
+// lane resumes between refill checks.
+template <int W, bool CNT, bool PL>
 __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
     const uint32_t *in = q_in(w, *c);
     TravStats st{0, 0};
     uint32_t err = 0;
+    // per-lane state of a ray through placements
+    const SceneDev *Sp = nullptr;
+    v3 wo = mk(0.0f, 0.0f, 0.0f), wd = wo, oo = wo, od = wo;
+    float dl = 0.0f, best = INFINITY, bt = 0.0f;
+    uint32_t k = 0, bprim = 0xFFFFFFFFu, bslot = 0u, binst = kNoInst;
     dyn_traverse<W, false, CNT, 8>(
         &c->head_ext, n, w.refill,
-        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
+        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, uint32_t &root, const uint4 *&nodes,
+            const float4 *&tris) {
             slot = in[qi];
             const uint4 m = w.meta[slot];
             const SceneDev &S = w.scenes[w.views[m.x & 0xFFFFu].scene];
@@ -417,11 +428,53 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
             tris = S.tris;
             float4 o, d;
             path_ray(w, slot, m, o, d);
-            r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
             tmax = INFINITY;
+            root = 0u;
+            if (!PL || S.ninst == 0) {
+                r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
+                if (PL) Sp = &S;
+                return true;
+            }
+            Sp = &S;
+            wo = mk(o.x, o.y, o.z);
+            wd = mk(d.x, d.y, d.z);
+            dl = sqrtf(dot(wd, wd));
+            best = INFINITY;
+            bprim = 0xFFFFFFFFu;
+            binst = kNoInst;
+            k = 0;
+            float len;
+            inst_ray(S, 0, wo, wd, oo, od, len);
+            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+            root = __ldg(&S.inst_root[0]);
+            return true;
+        },
+        [&](uint32_t, const Trav &T, RayPre &r, float &tmax, uint32_t &root) {
+            if (!PL || Sp->ninst == 0) return false;
+            if (T.best_prim != 0xFFFFFFFFu) {
+                const float dist = vdist(inst_point(*Sp, k, oo, od, T.best_t), wo);
+                if (dist < best) {
+                    best = dist;
+                    bt = T.best_t;
+                    bprim = T.best_prim;
+                    bslot = T.best_slot;
+                    binst = k;
+                }
+            }
+            if (++k >= Sp->ninst) return false;
+            float len;
+            inst_ray(*Sp, k, wo, wd, oo, od, len);
+            tmax = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
+            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+            root = __ldg(&Sp->inst_root[k]);
             return true;
         },
         [&](uint32_t slot, const Trav &T) {
+            if (PL && Sp->ninst != 0) {
+                w.hit[slot] = make_float4(bt, __uint_as_float(bprim), __uint_as_float(bslot),
+                                          pack_found(bprim != 0xFFFFFFFFu, binst));
+                return;
+            }
             const bool found = T.best_prim != 0xFFFFFFFFu;
             w.hit[slot] = make_float4(T.best_t, __uint_as_float(T.best_prim), __uint_as_float(T.best_slot),
                                       pack_found(found, kNoInst));
@@ -436,23 +489,58 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
 
 // Shadow tests with per-lane ray refill, for batches whose shadow requests
 // are all emitter tests (any hit below tmax); sun requests (faithful
-// estimator with the sun on) go through k_wf_shadow.
-template <int W, bool CNT>
+// estimator with the sun on) go through k_wf_shadow.  PL: as k_wf_extend_dyn,
+// the placements one after the other (occluded_placement_loop), stopping at
+// the first that occludes.
+template <int W, bool CNT, bool PL>
 __global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->sh_count;
     TravStats st{0, 0};
     uint32_t err = 0;
+    const SceneDev *Sp = nullptr;
+    v3 wo = mk(0.0f, 0.0f, 0.0f), wd = wo;
+    float dl = 0.0f, tw = 0.0f;
+    uint32_t k = 0;
     dyn_traverse<W, true, CNT, 8>(
         &c->head_sh, n, w.refill_sh,
-        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, const uint4 *&nodes, const float4 *&tris) {
+        [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, uint32_t &root, const uint4 *&nodes,
+            const float4 *&tris) {
             slot = w.qsh[qi];
             const SceneDev &S = w.scenes[w.views[w.meta[slot].x & 0xFFFFu].scene];
             const float4 so = w.sh_o[slot], sd = w.sh_d[slot];
             nodes = S.nodes;
             tris = S.tris;
-            r = ray_prep(so.x, so.y, so.z, sd.x, sd.y, sd.z, 1e-5f);
-            tmax = so.w;
+            root = 0u;
+            if (!PL || S.ninst == 0) {
+                r = ray_prep(so.x, so.y, so.z, sd.x, sd.y, sd.z, 1e-5f);
+                tmax = so.w;
+                if (PL) Sp = &S;
+                return true;
+            }
+            Sp = &S;
+            wo = mk(so.x, so.y, so.z);
+            wd = mk(sd.x, sd.y, sd.z);
+            dl = sqrtf(dot(wd, wd));
+            tw = so.w;
+            k = 0;
+            v3 oo, od;
+            float len;
+            inst_ray(S, 0, wo, wd, oo, od, len);
+            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+            tmax = (tw * len) / dl;
+            root = __ldg(&S.inst_root[0]);
+            return true;
+        },
+        [&](uint32_t, const Trav &T, RayPre &r, float &tmax, uint32_t &root) {
+            if (!PL || Sp->ninst == 0 || T.occluded) return false;
+            if (++k >= Sp->ninst) return false;
+            v3 oo, od;
+            float len;
+            inst_ray(*Sp, k, wo, wd, oo, od, len);
+            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+            tmax = (tw * len) / dl;
+            root = __ldg(&Sp->inst_root[k]);
             return true;
         },
         [&](uint32_t slot, const Trav &T) {
@@ -619,31 +707,46 @@ uint32_t resident_grid(K kernel, uint32_t block, int sms) {
     return (uint32_t)(std::max(sms, 1) * std::max(per_sm, 1));
 }
 
-// INST: kernels for batches with a scene traced through placements (the
-// split stages without per-lane refill, which resumes a traversal of one mesh).
+// INST: kernels for batches with a scene traced through the top-level tree
+// (the split stages without per-lane refill); batches whose scenes have at
+// most kLoopPlacements placements run the refill kernels' placement loop.
 template <int W, int FUSE, bool CNT, bool INST>
 Grids bounce_grids(const Wf &wf, uint32_t block, int sms) {
     Grids g{0, 0, 0};
     if (FUSE <= 1)
-        g.ext = (!INST && wf.refill) ? resident_grid(k_wf_extend_dyn<W, CNT>, block, sms)
+        g.ext = (!INST && wf.refill) ? (wf.placed ? resident_grid(k_wf_extend_dyn<W, CNT, true>, block, sms)
+                                                  : resident_grid(k_wf_extend_dyn<W, CNT, false>, block, sms))
                                      : resident_grid(k_wf_extend<W, CNT, INST>, block, sms);
     g.shade = resident_grid(k_wf_shade<W, FUSE, CNT, INST>, block, sms);
     if (FUSE == 0)
-        g.shadow = (!INST && wf.refill_sh) ? resident_grid(k_wf_shadow_dyn<W, CNT>, block, sms)
+        g.shadow = (!INST && wf.refill_sh) ? (wf.placed ? resident_grid(k_wf_shadow_dyn<W, CNT, true>, block, sms)
+                                                        : resident_grid(k_wf_shadow_dyn<W, CNT, false>, block, sms))
                                            : resident_grid(k_wf_shadow<W, CNT, INST>, block, sms);
     return g;
+}
+
+// The traversal stages with per-lane refill.
+template <int W, bool CNT>
+void launch_extend_dyn(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
+    if (wf.placed) k_wf_extend_dyn<W, CNT, true><<<grid, block, 0, st>>>(wf);
+    else k_wf_extend_dyn<W, CNT, false><<<grid, block, 0, st>>>(wf);
+}
+template <int W, bool CNT>
+void launch_shadow_dyn(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
+    if (wf.placed) k_wf_shadow_dyn<W, CNT, true><<<grid, block, 0, st>>>(wf);
+    else k_wf_shadow_dyn<W, CNT, false><<<grid, block, 0, st>>>(wf);
 }
 
 // The per-bounce kernels of one loop iteration for a fusion level.
 template <int W, int FUSE, bool CNT, bool INST>
 void launch_bounce(const Wf &wf, const Grids &g, uint32_t block, cudaStream_t st) {
     if (FUSE <= 1) {
-        if (!INST && wf.refill) k_wf_extend_dyn<W, CNT><<<g.ext, block, 0, st>>>(wf);
+        if (!INST && wf.refill) launch_extend_dyn<W, CNT>(wf, g.ext, block, st);
         else k_wf_extend<W, CNT, INST><<<g.ext, block, 0, st>>>(wf);
     }
     k_wf_shade<W, FUSE, CNT, INST><<<g.shade, block, 0, st>>>(wf);
     if (FUSE == 0) {
-        if (!INST && wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<g.shadow, block, 0, st>>>(wf);
+        if (!INST && wf.refill_sh) launch_shadow_dyn<W, CNT>(wf, g.shadow, block, st);
         else k_wf_shadow<W, CNT, INST><<<g.shadow, block, 0, st>>>(wf);
     }
 }
@@ -676,14 +779,14 @@ crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &
     for (uint32_t it = 0; rc == CRG_OK && it < max_iters + 8; ++it) {
         mark(it, 0);
         if (FUSE <= 1) {
-            if (!INST && wf.refill) k_wf_extend_dyn<W, CNT><<<bg.ext, block, 0, st>>>(wf);
+            if (!INST && wf.refill) launch_extend_dyn<W, CNT>(wf, bg.ext, block, st);
             else k_wf_extend<W, CNT, INST><<<bg.ext, block, 0, st>>>(wf);
         }
         mark(it, 1);
         k_wf_shade<W, FUSE, CNT, INST><<<bg.shade, block, 0, st>>>(wf);
         mark(it, 2);
         if (FUSE == 0) {
-            if (!INST && wf.refill_sh) k_wf_shadow_dyn<W, CNT><<<bg.shadow, block, 0, st>>>(wf);
+            if (!INST && wf.refill_sh) launch_shadow_dyn<W, CNT>(wf, bg.shadow, block, st);
             else k_wf_shadow<W, CNT, INST><<<bg.shadow, block, 0, st>>>(wf);
         }
         mark(it, 3);
@@ -873,7 +976,8 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
         crg_status rc0 = state_of(ctx, B);
         if (rc0 != CRG_OK) return rc0;
         const uint64_t key = (uint64_t)W | (uint64_t)FUSE << 8 | (uint64_t)CNT << 12 | (uint64_t)INST << 13 |
-                             (uint64_t)(wf.refill != 0) << 14 | (uint64_t)(wf.refill_sh != 0) << 15 | (uint64_t)block << 16;
+                             (uint64_t)(wf.refill != 0) << 14 | (uint64_t)(wf.refill_sh != 0) << 15 | (uint64_t)block << 16 |
+                             (uint64_t)(wf.placed != 0) << 36;
         uint32_t found = 0;
         for (const auto &e : B->occupancy)
             if (e.first == (key | 1ull << 40) || e.first == (key | 2ull << 40) || e.first == (key | 3ull << 40)) found++;
@@ -916,11 +1020,11 @@ int occupancy_of(int block) {
     a = b;
     if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
-    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false>, block, 0) == cudaSuccess)
+    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
-    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false>, block, 0) == cudaSuccess)
+    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     cudaGetLastError();
     return std::max(a, 1);
@@ -1121,18 +1225,20 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.nchunks = (uint32_t)chunks.size();
     wf.P = P;
     wf.fetch = o.fetch;
-    // per-lane refill resumes a traversal of one mesh; a ray through instances
-    // loops over them, so batches with an instanced scene use the static kernels
+    // per-lane refill resumes a traversal: of one mesh, or of a placement in the
+    // loop over a few of them; a ray through the top-level tree is not resumable,
+    // so batches with such a scene use the static kernels
     bool instanced = false, tree = false; // placements; more of them than the plain loop takes
     for (uint32_t i = 0; i < nscenes; ++i) {
         if (scenes[i]->ninst) instanced = true;
         if (scenes[i]->ninst > kLoopPlacements) tree = true;
     }
-    wf.refill = instanced ? 0u : o.refill;
+    wf.refill = tree ? 0u : o.refill;
+    wf.placed = instanced && !tree ? 1u : 0u;
     bool sun_requests = false; // the faithful estimator's sun test steps through alpha surfaces
     for (uint32_t v = 0; v < nviews; ++v)
         if (vdev[v].set.mode == CRG_MODE_FAITHFUL && scenes[vdev[v].scene]->sun_enabled) sun_requests = true;
-    wf.refill_sh = (sun_requests || instanced) ? 0u : o.refill;
+    wf.refill_sh = (sun_requests || tree) ? 0u : o.refill;
     wf.o = (float4 *)take(n_f4);
     wf.d = (float4 *)take(n_f4);
     wf.T = (float4 *)take(n_f4);

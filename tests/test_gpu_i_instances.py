@@ -85,6 +85,34 @@ def test_wavefront_equals_megakernel(ctx):
     s.close()
 
 
+def test_wavefront_refill_through_placements_in_a_mixed_batch(ctx):
+    """A scene of three placements (the loop, with per-lane refill) beside a
+    one-mesh scene in one batch: every refill threshold and fusion level gives
+    the megakernel's films."""
+    sc, box = scenes.instanced_box(), scenes.box_scene()
+    s = gpu_scene(ctx, sc)
+    b = api.Scene(ctx, box["verts"], box["mat_idx"], box["mats"]).build(8, 1)
+    views = [(0, sc["camera"], api.make_settings(64, 40, 8, 8, 3, 1, 7, 64 / 40)),
+             (1, box["camera"], api.make_settings(40, 40, 4, 8, 3, 1, 8)),
+             (0, sc["camera"], api.make_settings(24, 24, 4, 8, 3, 0, 9))]
+    mega = []
+    for si, cam, st in views:
+        f = api.Film(ctx, st.width, st.height)
+        api.render((s, b)[si], cam, st, f)
+        mega.append(f.download()["sum"])
+        f.close()
+    try:
+        for fuse, refill in ((1, 4), (1, 16), (1, 32), (2, 8)):
+            films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
+            ctx.check(api.render_batch([s, b], views, films, dict(fuse=fuse, refill=refill)))
+            for f, m in zip(films, mega):
+                assert np.array_equal(f.download()["sum"].view(np.uint32), m.view(np.uint32)), (fuse, refill)
+                f.close()
+    finally:
+        s.close()
+        b.close()
+
+
 def test_adjoint_matches_oracle(ctx, orc):
     sc = scenes.instanced_box()
     s = gpu_scene(ctx, sc)
