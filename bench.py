@@ -678,7 +678,7 @@ def main():
             e["megakernel_msamples_per_s"] = e["samples"] / t / 1e3
             e["wavefront_over_megakernel"] = e["wavefront_msamples_per_s"] / e["megakernel_msamples_per_s"]
         out["by_view_size"] = by_size
-        mega_steps, mega_warm = max(3, args.steps // 4), args.warmup
+        mega_steps, mega_warm = args.steps, args.warmup
         mega_ms = timer.steps(mega, mega_steps, mega_warm)
         out["megakernel"] = {"value": units / (sum(mega_ms) / len(mega_ms) / 1e3) / 1e6, "unit": unit,
                              "ms_per_step": sum(mega_ms) / len(mega_ms), "ms_min": min(mega_ms), "ms_max": max(mega_ms),
@@ -686,7 +686,7 @@ def main():
                              "bvh": {k: dict(zip(("width", "treelet", "leaf_max"), v)) for k, v in MEGA_BVH.items()},
                              "how": "same 64 views, one crg_render call per view (the drop-in), on the BVH options "
                                     "fastest for the megakernel in a sweep of width x leaf size; the wavefront arm's "
-                                    "warm-up, a quarter of its timed steps (at least 3), L2 flushed between steps"}
+                                    "warm-up and timed steps, L2 flushed between steps"}
         out["work"] = {**work, "mrays_per_step": rays / 1e6, "shadow_nodes_visited": sh_work["shadow_nodes"],
                        "shadow_tris_tested": sh_work["shadow_tris"]}
         kernel = "wavefront frame: one graph launch (k_wf_extend / k_wf_shade / k_wf_shadow / control / resolve)"
