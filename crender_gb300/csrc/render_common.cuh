@@ -305,6 +305,69 @@ __device__ __forceinline__ bool tlas_walk(const SceneDev &S, const TlasRay &t, f
     }
 }
 
+// The same walk, resumable: tlas_next returns the next placement whose box the
+// ray may reach under `bound` (the best world distance so far), or kNoInst
+// when the walk is over; the caller traces the placement between calls.
+// Placements come in tlas_walk's order and with its pruning.
+struct TlasWalk {
+    uint32_t stack[kTlasStack];
+    float sent[kTlasStack];
+    uint32_t ref;
+    int sp;
+    bool pop; // the last placement returned: continue with the stack
+    bool ok;  // false: the stack overflowed
+};
+__device__ __forceinline__ void tlas_begin(const SceneDev &S, TlasWalk &wk) {
+    wk.ref = S.tlas_root;
+    wk.sp = 0;
+    wk.pop = false;
+    wk.ok = true;
+}
+__device__ __forceinline__ uint32_t tlas_next(const SceneDev &S, const TlasRay &t, float bound, TlasWalk &wk) {
+    for (;;) {
+        if (!wk.pop) {
+            const uint32_t ref = wk.ref;
+            if (ref & kTlasLeaf) {
+                wk.pop = true;
+                return ref & ~kTlasLeaf;
+            }
+            const float4 *n = S.tlas + 4 * (size_t)ref;
+            const float4 la = __ldg(&n[0]), ha = __ldg(&n[1]), lb = __ldg(&n[2]), hb = __ldg(&n[3]);
+            const float ea = tlas_entry(t, la, ha), eb = tlas_entry(t, lb, hb);
+            const bool ka = ea < INFINITY && tlas_keep(t, ea, bound), kb = eb < INFINITY && tlas_keep(t, eb, bound);
+            const uint32_t ra = __float_as_uint(la.w), rb = __float_as_uint(ha.w);
+            if (ka && kb) {
+                const bool a_first = ea <= eb;
+                if (wk.sp < kTlasStack) {
+                    wk.stack[wk.sp] = a_first ? rb : ra;
+                    wk.sent[wk.sp] = a_first ? eb : ea;
+                    wk.sp++;
+                } else {
+                    wk.ok = false;
+                }
+                wk.ref = a_first ? ra : rb;
+                continue;
+            }
+            if (ka || kb) {
+                wk.ref = ka ? ra : rb;
+                continue;
+            }
+        }
+        // pop the next subtree that may still hold a closer hit
+        wk.pop = false;
+        bool found = false;
+        while (wk.sp > 0) {
+            --wk.sp;
+            if (tlas_keep(t, wk.sent[wk.sp], bound)) {
+                wk.ref = wk.stack[wk.sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) return kNoInst;
+    }
+}
+
 // Closest hit over the placements (the reference's loops over models and
 // instances): h.t is the object-space parameter, h.inst the placement.
 template <int W, bool CNT>

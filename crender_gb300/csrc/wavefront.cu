@@ -88,7 +88,7 @@ struct Wf {
     uint32_t nchunks, P, fetch;
     uint32_t refill;       // extend: 0 = static fetch of `fetch` entries, else the per-lane refill threshold
     uint32_t refill_sh;    // shadow: the same (0 when a batch can produce sun requests)
-    uint32_t placed;       // 1: a scene of the batch has placements (the refill kernels loop over them)
+    uint32_t placed;       // placements in the batch: 0 none, 1 at most kLoopPlacements per scene, 2 more
     uint32_t pad_[2];
     float4 *o, *d, *T, *L; // T.w = prev_pdf
     uint4 *meta;           // x: view | depth << 16 | flags; y: pixel; z: sample; w: offset in the chunk
@@ -401,11 +401,15 @@ __global__ void __launch_bounds__(256) k_wf_shadow(Wf w) {
 }
 
 // Extend with per-lane ray refill (dyn_traverse): the same hits as k_wf_extend.
-// PL: batches whose scenes may have placements (at most kLoopPlacements of
-// them): a lane traces its ray through the placements one after the other, as
-// closest_placement_loop does, each placement a traversal of its own that the
-// lane resumes between refill checks.
-template <int W, bool CNT, bool PL>
+// PL: the scenes' placements.  0: none (one mesh per scene).  1: at most
+// kLoopPlacements per scene, traced one after the other as
+// closest_placement_loop does.  2: placements through the top-level tree, as
+// closest_placements does (the walk is resumed between placements).  Each
+// placement is a traversal of its own that the lane resumes between refill
+// checks; the lane keeps the world ray, the walk and the best hit so far.  A
+// ray that reaches no placement box runs one empty traversal (tmax below
+// tmin) so that every query passes through done.
+template <int W, bool CNT, int PL>
 __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->in_count;
@@ -417,6 +421,16 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
     v3 wo = mk(0.0f, 0.0f, 0.0f), wd = wo, oo = wo, od = wo;
     float dl = 0.0f, best = INFINITY, bt = 0.0f;
     uint32_t k = 0, bprim = 0xFFFFFFFFu, bslot = 0u, binst = kNoInst;
+    TlasRay tr;
+    TlasWalk wk;
+    // sets up placement k's traversal under the current best world distance
+    auto place = [&](RayPre &r, float &tmax, uint32_t &root) {
+        float len;
+        inst_ray(*Sp, k, wo, wd, oo, od, len);
+        tmax = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
+        r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+        root = __ldg(&Sp->inst_root[k]);
+    };
     dyn_traverse<W, false, CNT, 8>(
         &c->head_ext, n, w.refill,
         [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, uint32_t &root, const uint4 *&nodes,
@@ -430,30 +444,38 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
             path_ray(w, slot, m, o, d);
             tmax = INFINITY;
             root = 0u;
-            if (!PL || S.ninst == 0) {
+            if (PL) Sp = &S;
+            if (PL == 0 || S.ninst == 0) {
                 r = ray_prep(o.x, o.y, o.z, d.x, d.y, d.z, 1e-5f);
-                if (PL) Sp = &S;
                 return true;
             }
-            Sp = &S;
             wo = mk(o.x, o.y, o.z);
             wd = mk(d.x, d.y, d.z);
             dl = sqrtf(dot(wd, wd));
             best = INFINITY;
             bprim = 0xFFFFFFFFu;
             binst = kNoInst;
-            k = 0;
-            float len;
-            inst_ray(S, 0, wo, wd, oo, od, len);
-            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
-            root = __ldg(&S.inst_root[0]);
+            if (PL == 2) {
+                tr = tlas_ray(wo, wd, 1e-5f);
+                tlas_begin(S, wk);
+                k = tlas_next(S, tr, best, wk);
+                if (k == kNoInst) { // no placement box on the ray: one empty traversal
+                    r = ray_prep(wo.x, wo.y, wo.z, wd.x, wd.y, wd.z, 1e-5f);
+                    tmax = -1.0f;
+                    root = __ldg(&S.inst_root[0]);
+                    return true;
+                }
+            } else {
+                k = 0;
+            }
+            place(r, tmax, root);
             return true;
         },
         [&](uint32_t, const Trav &T, RayPre &r, float &tmax, uint32_t &root) {
-            if (!PL || Sp->ninst == 0) return false;
+            if (PL == 0 || Sp->ninst == 0 || k == kNoInst) return false;
             if (T.best_prim != 0xFFFFFFFFu) {
                 const float dist = vdist(inst_point(*Sp, k, oo, od, T.best_t), wo);
-                if (dist < best) {
+                if (dist < best || (PL == 2 && dist == best && binst != kNoInst && k < binst)) {
                     best = dist;
                     bt = T.best_t;
                     bprim = T.best_prim;
@@ -461,16 +483,18 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
                     binst = k;
                 }
             }
-            if (++k >= Sp->ninst) return false;
-            float len;
-            inst_ray(*Sp, k, wo, wd, oo, od, len);
-            tmax = best < INFINITY ? ((best * len) / dl) * kInstSlack : INFINITY;
-            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
-            root = __ldg(&Sp->inst_root[k]);
+            if (PL == 2) {
+                k = tlas_next(*Sp, tr, best, wk);
+                if (k == kNoInst) return false;
+            } else if (++k >= Sp->ninst) {
+                return false;
+            }
+            place(r, tmax, root);
             return true;
         },
         [&](uint32_t slot, const Trav &T) {
-            if (PL && Sp->ninst != 0) {
+            if (PL != 0 && Sp->ninst != 0) {
+                if (PL == 2 && !wk.ok) err = 1u;
                 w.hit[slot] = make_float4(bt, __uint_as_float(bprim), __uint_as_float(bslot),
                                           pack_found(bprim != 0xFFFFFFFFu, binst));
                 return;
@@ -489,10 +513,10 @@ __global__ void __launch_bounds__(256, 5) k_wf_extend_dyn(Wf w) {
 
 // Shadow tests with per-lane ray refill, for batches whose shadow requests
 // are all emitter tests (any hit below tmax); sun requests (faithful
-// estimator with the sun on) go through k_wf_shadow.  PL: as k_wf_extend_dyn,
-// the placements one after the other (occluded_placement_loop), stopping at
-// the first that occludes.
-template <int W, bool CNT, bool PL>
+// estimator with the sun on) go through k_wf_shadow.  PL: as k_wf_extend_dyn
+// (occluded_placement_loop, occluded_placements), stopping at the first
+// placement that occludes.
+template <int W, bool CNT, int PL>
 __global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
     Ctrl *c = w.ctrl;
     const unsigned int n = c->sh_count;
@@ -502,6 +526,16 @@ __global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
     v3 wo = mk(0.0f, 0.0f, 0.0f), wd = wo;
     float dl = 0.0f, tw = 0.0f;
     uint32_t k = 0;
+    TlasRay tr;
+    TlasWalk wk;
+    auto place = [&](RayPre &r, float &tmax, uint32_t &root) {
+        v3 oo, od;
+        float len;
+        inst_ray(*Sp, k, wo, wd, oo, od, len);
+        r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
+        tmax = (tw * len) / dl;
+        root = __ldg(&Sp->inst_root[k]);
+    };
     dyn_traverse<W, true, CNT, 8>(
         &c->head_sh, n, w.refill_sh,
         [&](unsigned int qi, uint32_t &slot, RayPre &r, float &tmax, uint32_t &root, const uint4 *&nodes,
@@ -512,38 +546,46 @@ __global__ void __launch_bounds__(256, 5) k_wf_shadow_dyn(Wf w) {
             nodes = S.nodes;
             tris = S.tris;
             root = 0u;
-            if (!PL || S.ninst == 0) {
+            if (PL) Sp = &S;
+            if (PL == 0 || S.ninst == 0) {
                 r = ray_prep(so.x, so.y, so.z, sd.x, sd.y, sd.z, 1e-5f);
                 tmax = so.w;
-                if (PL) Sp = &S;
                 return true;
             }
-            Sp = &S;
             wo = mk(so.x, so.y, so.z);
             wd = mk(sd.x, sd.y, sd.z);
             dl = sqrtf(dot(wd, wd));
             tw = so.w;
-            k = 0;
-            v3 oo, od;
-            float len;
-            inst_ray(S, 0, wo, wd, oo, od, len);
-            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
-            tmax = (tw * len) / dl;
-            root = __ldg(&S.inst_root[0]);
+            if (PL == 2) {
+                tr = tlas_ray(wo, wd, 1e-5f);
+                dl = tr.dl;
+                tlas_begin(S, wk);
+                k = tlas_next(S, tr, tw, wk);
+                if (k == kNoInst) { // no placement box on the ray: one empty traversal
+                    r = ray_prep(wo.x, wo.y, wo.z, wd.x, wd.y, wd.z, 1e-5f);
+                    tmax = -1.0f;
+                    root = __ldg(&S.inst_root[0]);
+                    return true;
+                }
+            } else {
+                k = 0;
+            }
+            place(r, tmax, root);
             return true;
         },
         [&](uint32_t, const Trav &T, RayPre &r, float &tmax, uint32_t &root) {
-            if (!PL || Sp->ninst == 0 || T.occluded) return false;
-            if (++k >= Sp->ninst) return false;
-            v3 oo, od;
-            float len;
-            inst_ray(*Sp, k, wo, wd, oo, od, len);
-            r = ray_prep(oo.x, oo.y, oo.z, od.x, od.y, od.z, 1e-5f);
-            tmax = (tw * len) / dl;
-            root = __ldg(&Sp->inst_root[k]);
+            if (PL == 0 || Sp->ninst == 0 || k == kNoInst || T.occluded) return false;
+            if (PL == 2) {
+                k = tlas_next(*Sp, tr, tw, wk);
+                if (k == kNoInst) return false;
+            } else if (++k >= Sp->ninst) {
+                return false;
+            }
+            place(r, tmax, root);
             return true;
         },
         [&](uint32_t slot, const Trav &T) {
+            if (PL == 2 && Sp->ninst != 0 && !wk.ok) err = 1u;
             const uint4 m = w.meta[slot];
             float4 Lv = w.L[slot];
             if (!T.occluded) {
@@ -708,45 +750,51 @@ uint32_t resident_grid(K kernel, uint32_t block, int sms) {
 }
 
 // INST: kernels for batches with a scene traced through the top-level tree
-// (the split stages without per-lane refill); batches whose scenes have at
-// most kLoopPlacements placements run the refill kernels' placement loop.
+// (split stages only; with refill, the traversal stages keep the walk per
+// lane); batches whose scenes have at most kLoopPlacements placements run the
+// placement loop.
 template <int W, int FUSE, bool CNT, bool INST>
 Grids bounce_grids(const Wf &wf, uint32_t block, int sms) {
     Grids g{0, 0, 0};
     if (FUSE <= 1)
-        g.ext = (!INST && wf.refill) ? (wf.placed ? resident_grid(k_wf_extend_dyn<W, CNT, true>, block, sms)
-                                                  : resident_grid(k_wf_extend_dyn<W, CNT, false>, block, sms))
-                                     : resident_grid(k_wf_extend<W, CNT, INST>, block, sms);
+        g.ext = wf.refill ? (INST ? resident_grid(k_wf_extend_dyn<W, CNT, 2>, block, sms)
+                                  : wf.placed ? resident_grid(k_wf_extend_dyn<W, CNT, 1>, block, sms)
+                                              : resident_grid(k_wf_extend_dyn<W, CNT, 0>, block, sms))
+                          : resident_grid(k_wf_extend<W, CNT, INST>, block, sms);
     g.shade = resident_grid(k_wf_shade<W, FUSE, CNT, INST>, block, sms);
     if (FUSE == 0)
-        g.shadow = (!INST && wf.refill_sh) ? (wf.placed ? resident_grid(k_wf_shadow_dyn<W, CNT, true>, block, sms)
-                                                        : resident_grid(k_wf_shadow_dyn<W, CNT, false>, block, sms))
-                                           : resident_grid(k_wf_shadow<W, CNT, INST>, block, sms);
+        g.shadow = wf.refill_sh ? (INST ? resident_grid(k_wf_shadow_dyn<W, CNT, 2>, block, sms)
+                                        : wf.placed ? resident_grid(k_wf_shadow_dyn<W, CNT, 1>, block, sms)
+                                                    : resident_grid(k_wf_shadow_dyn<W, CNT, 0>, block, sms))
+                                : resident_grid(k_wf_shadow<W, CNT, INST>, block, sms);
     return g;
 }
 
-// The traversal stages with per-lane refill.
-template <int W, bool CNT>
+// The traversal stages with per-lane refill: through the top-level tree (INST),
+// the placement loop (a scene with placements) or one mesh per scene.
+template <int W, bool CNT, bool INST>
 void launch_extend_dyn(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
-    if (wf.placed) k_wf_extend_dyn<W, CNT, true><<<grid, block, 0, st>>>(wf);
-    else k_wf_extend_dyn<W, CNT, false><<<grid, block, 0, st>>>(wf);
+    if (INST) k_wf_extend_dyn<W, CNT, 2><<<grid, block, 0, st>>>(wf);
+    else if (wf.placed) k_wf_extend_dyn<W, CNT, 1><<<grid, block, 0, st>>>(wf);
+    else k_wf_extend_dyn<W, CNT, 0><<<grid, block, 0, st>>>(wf);
 }
-template <int W, bool CNT>
+template <int W, bool CNT, bool INST>
 void launch_shadow_dyn(const Wf &wf, uint32_t grid, uint32_t block, cudaStream_t st) {
-    if (wf.placed) k_wf_shadow_dyn<W, CNT, true><<<grid, block, 0, st>>>(wf);
-    else k_wf_shadow_dyn<W, CNT, false><<<grid, block, 0, st>>>(wf);
+    if (INST) k_wf_shadow_dyn<W, CNT, 2><<<grid, block, 0, st>>>(wf);
+    else if (wf.placed) k_wf_shadow_dyn<W, CNT, 1><<<grid, block, 0, st>>>(wf);
+    else k_wf_shadow_dyn<W, CNT, 0><<<grid, block, 0, st>>>(wf);
 }
 
 // The per-bounce kernels of one loop iteration for a fusion level.
 template <int W, int FUSE, bool CNT, bool INST>
 void launch_bounce(const Wf &wf, const Grids &g, uint32_t block, cudaStream_t st) {
     if (FUSE <= 1) {
-        if (!INST && wf.refill) launch_extend_dyn<W, CNT>(wf, g.ext, block, st);
+        if (wf.refill) launch_extend_dyn<W, CNT, INST>(wf, g.ext, block, st);
         else k_wf_extend<W, CNT, INST><<<g.ext, block, 0, st>>>(wf);
     }
     k_wf_shade<W, FUSE, CNT, INST><<<g.shade, block, 0, st>>>(wf);
     if (FUSE == 0) {
-        if (!INST && wf.refill_sh) launch_shadow_dyn<W, CNT>(wf, g.shadow, block, st);
+        if (wf.refill_sh) launch_shadow_dyn<W, CNT, INST>(wf, g.shadow, block, st);
         else k_wf_shadow<W, CNT, INST><<<g.shadow, block, 0, st>>>(wf);
     }
 }
@@ -779,14 +827,14 @@ crg_status run_host(crg_context *ctx, const Wf &wf, uint32_t grid, const Grids &
     for (uint32_t it = 0; rc == CRG_OK && it < max_iters + 8; ++it) {
         mark(it, 0);
         if (FUSE <= 1) {
-            if (!INST && wf.refill) launch_extend_dyn<W, CNT>(wf, bg.ext, block, st);
+            if (wf.refill) launch_extend_dyn<W, CNT, INST>(wf, bg.ext, block, st);
             else k_wf_extend<W, CNT, INST><<<bg.ext, block, 0, st>>>(wf);
         }
         mark(it, 1);
         k_wf_shade<W, FUSE, CNT, INST><<<bg.shade, block, 0, st>>>(wf);
         mark(it, 2);
         if (FUSE == 0) {
-            if (!INST && wf.refill_sh) launch_shadow_dyn<W, CNT>(wf, bg.shadow, block, st);
+            if (wf.refill_sh) launch_shadow_dyn<W, CNT, INST>(wf, bg.shadow, block, st);
             else k_wf_shadow<W, CNT, INST><<<bg.shadow, block, 0, st>>>(wf);
         }
         mark(it, 3);
@@ -977,7 +1025,7 @@ crg_status run(crg_context *ctx, const Wf &wf, uint32_t grid, uint32_t block, ui
         if (rc0 != CRG_OK) return rc0;
         const uint64_t key = (uint64_t)W | (uint64_t)FUSE << 8 | (uint64_t)CNT << 12 | (uint64_t)INST << 13 |
                              (uint64_t)(wf.refill != 0) << 14 | (uint64_t)(wf.refill_sh != 0) << 15 | (uint64_t)block << 16 |
-                             (uint64_t)(wf.placed != 0) << 36;
+                             (uint64_t)wf.placed << 36;
         uint32_t found = 0;
         for (const auto &e : B->occupancy)
             if (e.first == (key | 1ull << 40) || e.first == (key | 2ull << 40) || e.first == (key | 3ull << 40)) found++;
@@ -1020,11 +1068,11 @@ int occupancy_of(int block) {
     a = b;
     if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
-    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false, false>, block, 0) == cudaSuccess)
+    if (FUSE <= 1 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_extend_dyn<W, false, 0>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow<W, false, false>, block, 0) == cudaSuccess)
         a = std::min(a, c);
-    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false, false>, block, 0) == cudaSuccess)
+    if (FUSE == 0 && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_shadow_dyn<W, false, 0>, block, 0) == cudaSuccess)
         a = std::min(a, c);
     cudaGetLastError();
     return std::max(a, 1);
@@ -1225,20 +1273,19 @@ crg_status render_batch(crg_context *ctx, crg_scene *const *scenes, uint32_t nsc
     wf.nchunks = (uint32_t)chunks.size();
     wf.P = P;
     wf.fetch = o.fetch;
-    // per-lane refill resumes a traversal: of one mesh, or of a placement in the
-    // loop over a few of them; a ray through the top-level tree is not resumable,
-    // so batches with such a scene use the static kernels
+    // per-lane refill resumes a traversal: of one mesh, or of one placement of a
+    // scene (the refill kernels keep the placement loop or the top-level walk)
     bool instanced = false, tree = false; // placements; more of them than the plain loop takes
     for (uint32_t i = 0; i < nscenes; ++i) {
         if (scenes[i]->ninst) instanced = true;
         if (scenes[i]->ninst > kLoopPlacements) tree = true;
     }
-    wf.refill = tree ? 0u : o.refill;
-    wf.placed = instanced && !tree ? 1u : 0u;
+    wf.refill = o.refill;
+    wf.placed = instanced ? (tree ? 2u : 1u) : 0u;
     bool sun_requests = false; // the faithful estimator's sun test steps through alpha surfaces
     for (uint32_t v = 0; v < nviews; ++v)
         if (vdev[v].set.mode == CRG_MODE_FAITHFUL && scenes[vdev[v].scene]->sun_enabled) sun_requests = true;
-    wf.refill_sh = (sun_requests || tree) ? 0u : o.refill;
+    wf.refill_sh = sun_requests ? 0u : o.refill;
     wf.o = (float4 *)take(n_f4);
     wf.d = (float4 *)take(n_f4);
     wf.T = (float4 *)take(n_f4);

@@ -84,11 +84,12 @@ def test_wavefront_equals_megakernel_in_a_mixed_batch(ctx):
         api.render((s, b)[si], cam, st, f)
         mega.append(f.download()["sum"])
         f.close()
-    for fuse in (1, 3):
+    # six placements: the top-level tree, walked per lane by the refill kernels (and the static fetch)
+    for fuse, refill in ((1, 16), (1, 4), (1, 32), (1, 0xFFFFFFFF), (3, 16)):
         films = [api.Film(ctx, st.width, st.height) for _, _, st in views]
-        ctx.check(api.render_batch([s, b], views, films, dict(fuse=fuse)))
+        ctx.check(api.render_batch([s, b], views, films, dict(fuse=fuse, refill=refill)))
         for f, m in zip(films, mega):
-            assert np.array_equal(f.download()["sum"].view(np.uint32), m.view(np.uint32)), fuse
+            assert np.array_equal(f.download()["sum"].view(np.uint32), m.view(np.uint32)), (fuse, refill)
             f.close()
     s.close()
     b.close()
