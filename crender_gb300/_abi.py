@@ -217,6 +217,7 @@ CRG_SIGNATURES = [
     ("crg_film_reset", C.c_int, [vp, c_stream]),
     ("crg_film_spp", C.c_int, [vp, P(C.c_uint64)]),
     ("crg_film_download", C.c_int, [vp, vp, vp, vp, vp, vp, vp, c_stream]),
+    ("crg_film_download_async", C.c_int, [vp, vp, vp, vp, vp, vp, vp, c_stream]),
     ("crg_film_device_ptrs", C.c_int, [vp, P(vp), P(vp), P(vp)]),
     ("crg_film_display", C.c_int, [vp, vp, c_stream]),
     ("crg_post_settings_default", C.c_int, [P(PostSettings)]),

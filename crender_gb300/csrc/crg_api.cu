@@ -1276,6 +1276,14 @@ crg_status crg_film_spp(const crg_film *film, uint64_t *spp) {
 
 crg_status crg_film_download(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64, float *aov_albedo,
                              float *aov_normal, float *aov_depth, crg_stream stream) {
+    const crg_status rc = crg_film_download_async(film, sum_rgb, sum64, sumsq64, aov_albedo, aov_normal, aov_depth, stream);
+    if (rc != CRG_OK) return rc;
+    CRG_CUDA(film->ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    return CRG_OK;
+}
+
+crg_status crg_film_download_async(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64, float *aov_albedo,
+                                   float *aov_normal, float *aov_depth, crg_stream stream) {
     if (!film) return CRG_ERR_INVALID_ARG;
     crg_context *ctx = film->ctx;
     cudaStream_t st = (cudaStream_t)stream;
@@ -1289,7 +1297,6 @@ crg_status crg_film_download(crg_film *film, float *sum_rgb, double *sum64, doub
     if (aov_albedo) CRG_CUDA(ctx, cudaMemcpyAsync(aov_albedo, film->aov_albedo.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
     if (aov_normal) CRG_CUDA(ctx, cudaMemcpyAsync(aov_normal, film->aov_normal.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
     if (aov_depth) CRG_CUDA(ctx, cudaMemcpyAsync(aov_depth, film->aov_depth.ptr, sizeof(float) * 4 * npix, cudaMemcpyDeviceToHost, st));
-    CRG_CUDA(ctx, cudaStreamSynchronize(st));
     return CRG_OK;
 }
 

@@ -437,6 +437,13 @@ crg_status crg_film_spp(const crg_film *film, uint64_t *spp);
  * sumsq64 double[W*H*3]; aov_* float[W*H*4] RGBA as cr::image stores them. */
 crg_status crg_film_download(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64,
                              float *aov_albedo, float *aov_normal, float *aov_depth, crg_stream stream);
+/* crg_film_download without the wait: the copies are only enqueued on
+ * `stream`, so the downloads of many films cost one synchronisation
+ * (crg_stream_sync) instead of one each.  The host arrays must stay valid
+ * until the stream has reached them; page-locked arrays (crg_host_alloc) make
+ * the copies asynchronous. */
+crg_status crg_film_download_async(crg_film *film, float *sum_rgb, double *sum64, double *sumsq64,
+                                   float *aov_albedo, float *aov_normal, float *aov_depth, crg_stream stream);
 /* Device pointers of the film arrays (valid until crg_film_destroy). */
 crg_status crg_film_device_ptrs(crg_film *film, float **sum_rgb, double **sum64, double **sumsq64);
 /* Display transform clamp(sum/spp, 0, 1)^(1/2.2) into a device RGBA32F

@@ -177,3 +177,32 @@ def test_edge_settings(ctx, orc, spp, max_bounces, mode):
     s.close()
     for k in ("sum", "sum64", "sumsq64"):
         assert np.array_equal(w[k].view(np.uint8), o[k].view(np.uint8)), k
+
+
+def test_film_download_async(ctx):
+    """crg_film_download_async enqueues the same copies as crg_film_download
+    without waiting: after one stream sync the host arrays hold the same
+    bytes, for several films downloaded back to back."""
+    sc = scenes.box_scene()
+    s = api.Scene(ctx, sc["verts"], sc["mat_idx"], sc["mats"]).build(8, 1)
+    films, outs = [], []
+    try:
+        for k, (w, h) in enumerate(((32, 24), (16, 16), (40, 8))):
+            f = api.Film(ctx, w, h, f64=True)
+            api.render(s, sc["camera"], api.make_settings(w, h, 4, 6, 3, 1, 20 + k, w / h), f)
+            films.append(f)
+            outs.append((api.PinnedArray(ctx, (w * h * 3,), np.float32), api.PinnedArray(ctx, (w * h * 3,), np.float64)))
+        for f, (o32, o64) in zip(films, outs):
+            ctx.check(ctx.lib.crg_film_download_async(f.h, o32.ptr, o64.ptr, None, None, None, None, None))
+        ctx.check(ctx.lib.crg_stream_sync(ctx.h, None))
+        for f, (o32, o64) in zip(films, outs):
+            ref = f.download(f64=True)
+            assert np.array_equal(o32.array.view(np.uint32), ref["sum"].reshape(-1).view(np.uint32))
+            assert np.array_equal(o64.array.view(np.uint64), ref["sum64"].reshape(-1).view(np.uint64))
+    finally:
+        for f in films:
+            f.close()
+        for a, b in outs:
+            a.free()
+            b.free()
+        s.close()
