@@ -486,6 +486,8 @@ def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
         backward()
         lb.download(lh, S)
         grad = gc.download(zc.copy(), S)[:105]  # 34 albedos (RGB) then the light colour
+        if it == 0:
+            g_first = np.abs(grad[:102]).copy()
         losses.append(float(lh[0]))
         m1 = 0.9 * m1 + 0.1 * grad
         m2 = 0.999 * m2 + 0.001 * grad * grad
@@ -499,6 +501,20 @@ def inverse_workload(ctx, api, scenes, timer, S, args, world, out, torch):
                    "albedo_mae_first": float(np.abs(0.5 - truth).mean()),
                    "albedo_mae_last": float(np.abs(theta[:102] - truth).mean()),
                    "light_radiance_last": (17 * theta[102:]).tolist(), "light_radiance_true": 17.0}
+    # which albedos the image constrains: the first step's gradient magnitude per parameter against
+    # the final error (a parameter whose gradient is tiny barely moves the loss, so Adam's steps on
+    # it follow noise)
+    err = np.abs(theta[:102] - truth)
+    weak = g_first < 1e-2 * g_first.max()
+    order = np.argsort(g_first)
+    third = len(order) // 3
+    out["adam"]["constraint"] = {
+        "how": "first-step |dL/d albedo| per parameter (34 triangles x RGB) against the final |albedo error|",
+        "weak_params": int(weak.sum()), "weak_threshold": "below 1e-2 of the largest gradient",
+        "mae_weak": float(err[weak].mean()) if weak.any() else None,
+        "mae_rest": float(err[~weak].mean()) if (~weak).any() else None,
+        "mae_by_gradient_third": [float(err[order[:third]].mean()), float(err[order[third:2 * third]].mean()),
+                                  float(err[order[2 * third:]].mean())]}
     h2d = nmat * 48 + nmat * 24 + nmat * 8
     out["e2e"] = {"value": units * world / (adam_s / 200) / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
                   "d2h_bytes_per_step": 8 + nmat * 24, "ms_per_step": adam_s / 200 * 1e3,
