@@ -17,6 +17,10 @@
 //            order, so films are bit-identical to the megakernel's
 //   generate seeds the pool with the next chunk's first samples
 //
+// A new sample stores only its meta word: extend and shade derive its camera
+// ray, throughput and radiance.  The traversal stages refill idle lanes ray
+// by ray and trace a ray through a scene's placements themselves.
+//
 // extend / shade / shadow are persistent kernels: a fixed grid whose warps
 // take `fetch` queue entries at a time with one atomic.  The order in which L
 // receives contributions (emission of bounce i, then NEE of bounce i, then
